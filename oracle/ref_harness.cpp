@@ -1,0 +1,161 @@
+// Test-oracle harness around the CIFlow reference sources (compiled unmodified
+// from the reference tree by oracle/Makefile into oracle/_ref/).
+//
+// This file is test infrastructure: only tests/, the smoke check and the CPU
+// baseline of bench.py load the library it builds. It exposes the reference's
+// own classes through a plain C API so that Python can:
+//   * build a Hamiltonian in memory (Hamiltonian(L,0,nup,ndown,Econst) plus
+//     setTmat/setVmat, Hamiltonian.cpp:77-113,255-320) or read a psi4 text dump
+//     (Hamiltonian(filename), Hamiltonian.cpp:157-171,707-885);
+//   * construct FCI/DOCI, which builds the upper-triangle CRS in the constructor
+//     (CIMethod.cpp:566-580 -> build_parallel :489-561);
+//   * read back the CRS arrays data/col/row (SparseMatrix_CRS.h:107-111);
+//   * call the reference SparseMatrix_CRS_Sym::mvprod (SparseMatrix_CRS.cpp:700-723)
+//     so scipy's ARPACK can drive the reference matvec;
+//   * install an eigenvector and run CIDens::construct_density
+//     (CIMethod.cpp:161-171, CIDens.cpp:323-334) and read the RDMs through
+//     get_one_rdm/get_two_rdm (CIDens.cpp:166-292).
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <iomanip>
+#include <iostream>
+#include <memory>
+#include <string>
+#include <vector>
+
+// Members the harness reads (CIMethod::_mat, SparseMatrix_CRS::data/col/row,
+// CIMethod::_cid, CIMethod::_solved) are protected in the reference; this TU
+// only reads them, with the same class layout.
+#define protected public
+#include "CIDens.h"
+#include "CIMethod.h"
+#include "Hamiltonian.h"
+#include "SparseMatrix_CRS.h"
+#undef protected
+
+namespace {
+
+struct RefCI {
+    Hamiltonian *ham = nullptr;
+    CIMethod *cim = nullptr;
+    int method = 0;  // 0 = FCI, 1 = DOCI
+};
+
+Hamiltonian *make_ham(int L, int nup, int ndown, double econst, const double *h, const double *eri) {
+    Hamiltonian *ham = new Hamiltonian(L, 0, nup, ndown, econst);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j) ham->setTmat(i, j, h[i * L + j]);
+    // eri is chemist (ij|kl), row-major L^4; the reference stores physics
+    // <ik|jl> = (ij|kl) exactly as its text reader does (Hamiltonian.cpp:873).
+    const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1;
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j)
+            for (int k = 0; k < L; ++k)
+                for (int l = 0; l < L; ++l) ham->setVmat(i, k, j, l, eri[i * L3 + j * L2 + k * L1 + l]);
+    return ham;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Reads a psi4 integral dump with the reference reader. Call once with h == NULL
+// to obtain L/nup/ndown/econst, then again with h (L*L) and eri (L^4, chemist).
+int ref_ham_read_file(const char *filename, int *L, int *nup, int *ndown, double *econst, double *h,
+                      double *eri) {
+    Hamiltonian ham{std::string(filename)};
+    *L = ham.getL();
+    *nup = ham.getnup();
+    *ndown = ham.getndown();
+    *econst = ham.getEconst();
+    if (!h) return 0;
+    const int n = *L;
+    const size_t L1 = n, L2 = L1 * L1, L3 = L2 * L1;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) h[i * n + j] = ham.getTmat(i, j);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k)
+                for (int l = 0; l < n; ++l) eri[i * L3 + j * L2 + k * L1 + l] = ham.getVmat(i, k, j, l);
+    return 0;
+}
+
+// method 0 = FCI, 1 = DOCI. When filename is non-NULL the Hamiltonian comes from
+// the reference text reader (with its point-group irreps); otherwise from h/eri.
+void *ref_ci_create(int method, const char *filename, int L, int nup, int ndown, double econst,
+                    const double *h, const double *eri) {
+    RefCI *r = new RefCI;
+    r->method = method;
+    r->ham = filename ? new Hamiltonian(std::string(filename)) : make_ham(L, nup, ndown, econst, h, eri);
+    if (method == 0)
+        r->cim = new FCI(r->ham);
+    else
+        r->cim = new DOCI(r->ham);
+    return r;
+}
+
+void ref_ci_destroy(void *p) {
+    RefCI *r = static_cast<RefCI *>(p);
+    delete r->cim;
+    delete r->ham;
+    delete r;
+}
+
+long long ref_ci_dim(void *p) { return static_cast<RefCI *>(p)->cim->get_dim(); }
+long long ref_ci_nnz(void *p) { return static_cast<RefCI *>(p)->cim->_mat.data.size(); }
+
+// Copies the reference CRS: row (dim+1), col (nnz), val (nnz).
+void ref_ci_export(void *p, unsigned *row, unsigned *col, double *val) {
+    const SparseMatrix_CRS &m = static_cast<RefCI *>(p)->cim->_mat;
+    std::memcpy(row, m.row.data(), m.row.size() * sizeof(unsigned));
+    std::memcpy(col, m.col.data(), m.col.size() * sizeof(unsigned));
+    std::memcpy(val, m.data.data(), m.data.size() * sizeof(double));
+}
+
+// The reference matvec y = (U + U^T - D) x, serial (SparseMatrix_CRS.cpp:700-723).
+void ref_ci_mvprod(void *p, const double *x, double *y) {
+    static_cast<RefCI *>(p)->cim->_mat.mvprod(x, y);
+}
+
+// Installs eigenpair (e without Econst, c of length dim) and builds the RDMs
+// with the reference CIDens (DensFCI / DensDOCI). rdm1: [2][L][L];
+// rdm2_aa/bb: [npair][npair] with pair(p<q) = p*L+q-(p+1)(p+2)/2; rdm2_ab: [L*L][L*L].
+// Returns CIDens::get_dens_energy().
+double ref_ci_density(void *p, double e, const double *c, double *rdm1, double *rdm2_aa, double *rdm2_ab,
+                      double *rdm2_bb) {
+    RefCI *r = static_cast<RefCI *>(p);
+    CIMethod *cim = r->cim;
+    const int dim = cim->get_dim();
+    cim->_eigval = matrix(1, 1);
+    cim->_eigval(0, 0) = e;
+    cim->_eigvec = matrix(dim, 1);
+    for (int i = 0; i < dim; ++i) cim->_eigvec(i, 0) = c[i];
+    cim->_solved = true;
+    cim->_cid->reset_density();
+    cim->construct_density(0, true);
+    CIDens *d = cim->_cid.get();
+    const int L = cim->get_l();
+    for (int s = 0; s < 2; ++s)
+        for (int i = 0; i < L; ++i)
+            for (int j = 0; j < L; ++j) rdm1[(s * L + i) * L + j] = d->get_one_rdm(s, i, j);
+    const int np = L * (L - 1) / 2;
+    for (int p_ = 0; p_ < L; ++p_)
+        for (int q = p_ + 1; q < L; ++q)
+            for (int r_ = 0; r_ < L; ++r_)
+                for (int s = r_ + 1; s < L; ++s) {
+                    const int a = p_ * L + q - (p_ + 1) * (p_ + 2) / 2;
+                    const int b = r_ * L + s - (r_ + 1) * (r_ + 2) / 2;
+                    rdm2_aa[a * np + b] = d->get_two_rdm(0, p_, q, r_, s);
+                    rdm2_bb[a * np + b] = d->get_two_rdm(2, p_, q, r_, s);
+                }
+    const int L2 = L * L;
+    for (int p_ = 0; p_ < L; ++p_)
+        for (int q = 0; q < L; ++q)
+            for (int r_ = 0; r_ < L; ++r_)
+                for (int s = 0; s < L; ++s)
+                    rdm2_ab[(p_ * L + q) * L2 + r_ * L + s] = d->get_two_rdm(1, p_, q, r_, s);
+    return d->get_dens_energy();
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+"""Generate the golden fixtures in tests/golden/ from the CIFlow reference.
+
+Run in a checkout where the reference tree is available (default
+/root/reference, override with CIGPU_REFERENCE_ROOT):
+
+    python tests/golden/make_golden.py [names...]
+
+For each case the reference itself (oracle/_ref, compiled unmodified from the
+reference sources) builds the upper-triangle CRS in its FCI/DOCI constructor;
+the lowest eigenpair comes from scipy ARPACK driving that CRS with the
+reference's arpackDiagonalize settings, and the RDMs from the reference
+CIDens (DensFCI/DensDOCI) where its O(dim^2) pair loop is affordable.
+
+Fixtures hold: integral checksum (or the integrals themselves for the BeH2
+file fixture), dimension and nnz, SHA-256 of the reference CRS arrays in the
+reference layout (uint32 row, uint32 col, float64 val), E0 (+Econst), and the
+RDMs in the CIDens packed conventions.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from ciflow_gb300.synthetic import CONFIGS, config_integrals  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def crs_sha256(m: O.UpperCRS) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(m.row, dtype=np.uint32).tobytes())
+    h.update(np.ascontiguousarray(m.col, dtype=np.uint32).tobytes())
+    h.update(np.ascontiguousarray(m.val, dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
+def solve_ref(r: O.RefCI, n: int, big: bool):
+    """Lowest eigenpair of the reference CRS with ARPACK (reference settings)."""
+    import scipy.sparse.linalg as sla
+    v0 = np.random.default_rng(12345).standard_normal(n)
+    if not big:
+        return O.lowest_eigenpair(r.crs(), v0=v0)
+    m = r.crs()
+    op = sla.LinearOperator((n, n), matvec=lambda x: O.sym_mvprod(m, x, threaded=True), dtype=np.float64)
+    w, v = sla.eigsh(op, k=1, which="SA", ncv=42, tol=0, maxiter=3 * n, v0=v0)
+    c = v[:, 0]
+    return float(w[0]), c / np.linalg.norm(c), m
+
+
+def case_file(name: str, fname: str):
+    path = os.path.join(O.REF_ROOT, "tests", "data", fname)
+    ints = O.ref_read_file(path)
+    out = {"h": ints.h, "eri": ints.eri}
+    meta = {"L": ints.L, "nup": ints.nup, "ndown": ints.ndown, "econst": ints.econst, "source": f"tests/data/{fname}"}
+    for method, tag in ((O.DOCI, "doci"), (O.FCI, "fci")):
+        r = O.RefCI(method, filename=path)
+        m = r.crs()
+        e, c = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
+        (r1, aa, ab, bb), ed = r.density(ints.L, e, c)
+        meta[tag] = {"dim": m.n, "nnz": m.nnz, "crs_sha256": crs_sha256(m), "e0": e + ints.econst, "dens_energy": ed}
+        out.update({f"{tag}_rdm1": r1, f"{tag}_aa": aa, f"{tag}_ab": ab, f"{tag}_bb": bb, f"{tag}_c": c})
+        r.close()
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+def case_config(name: str, rdm: bool):
+    cfg = CONFIGS[name]
+    method = O.FCI if cfg["method"] == "FCI" else O.DOCI
+    ints = config_integrals(name)
+    t0 = time.time()
+    r = O.RefCI(method, ints=ints)
+    t_build = time.time() - t0
+    n = int(r.lib.ref_ci_dim(r.h))
+    big = n > 200000
+    if big:
+        e, c, m = solve_ref(r, n, True)
+    else:
+        m = r.crs()
+        e, c = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(n))
+    meta = {"config": cfg, "integrals_sha": ints.checksum(), "dim": n, "nnz": m.nnz,
+            "crs_sha256": crs_sha256(m), "e0": e + ints.econst, "ref_build_s": t_build}
+    out = {}
+    if rdm:
+        (r1, aa, ab, bb), ed = r.density(ints.L, e, c)
+        meta["dens_energy"] = ed
+        out.update({"rdm1": r1, "aa": aa, "ab": ab, "bb": bb})
+    r.close()
+    if out:
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta))
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4"]
+    for nm in names:
+        if nm == "beh2_sto3g":
+            case_file(nm, "beh2_sto3g_1_5.dat")
+        elif nm == "be_ccpvdz":
+            case_file(nm, "Be_ccpVDZ.dat")
+        else:
+            case_config(nm, rdm=nm in ("c0", "c4", "c2"))

@@ -1,0 +1,106 @@
+"""The CPU oracle (C restatement) against the reference's golden vectors.
+
+The fixtures in tests/golden/ were produced by the CIFlow reference itself
+(tests/golden/make_golden.py). These tests run without a GPU and pin the
+oracle before it is trusted as the checker of the CUDA path:
+
+* the DOCI energy of BeH2/STO-3G equals the reference known answer
+  -15.225362047972723 (tests/src/TestDOCI.cpp:31 of the reference);
+* the oracle CRS is bit-identical to the reference CRS (SHA-256 of the
+  uint32 row / uint32 col / float64 val arrays);
+* oracle RDMs equal the reference DensFCI/DensDOCI RDMs, and the density
+  energy equals the CI energy (CIDens::test_invariants, CIDens.cpp:365-409).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from ciflow_gb300.synthetic import Integrals, config_integrals
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+from tests.golden.make_golden import crs_sha256
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        meta = json.load(f)
+    npz = os.path.join(GOLDEN, name + ".npz")
+    arrs = np.load(npz) if os.path.exists(npz) else None
+    return meta, arrs
+
+
+def beh2():
+    meta, a = load("beh2_sto3g")
+    return Integrals(meta["L"], meta["nup"], meta["ndown"], meta["econst"], a["h"], a["eri"]), meta, a
+
+
+def test_doci_known_answer():
+    ints, meta, _ = beh2()
+    m = O.build_upper(O.DOCI, ints)
+    e, _ = O.lowest_eigenpair(m)
+    # reference tests/src/TestDOCI.cpp:31, BOOST_CHECK_CLOSE 1e-10 percent
+    assert abs(e + ints.econst - (-15.225362047972723)) <= 1e-12 * 15.3
+    assert meta["doci"]["crs_sha256"] == crs_sha256(m)
+
+
+@pytest.mark.parametrize("tag,method", [("doci", O.DOCI), ("fci", O.FCI)])
+def test_beh2_crs_and_rdm(tag, method):
+    ints, meta, a = beh2()
+    m = O.build_upper(method, ints)
+    assert m.n == meta[tag]["dim"] and m.nnz == meta[tag]["nnz"]
+    assert crs_sha256(m) == meta[tag]["crs_sha256"]
+    c = a[f"{tag}_c"]
+    for literal in (True, False):
+        r1, aa, ab, bb = O.rdm(method, ints.L, ints.nup, ints.ndown, c, literal=literal)
+        np.testing.assert_allclose(r1, a[f"{tag}_rdm1"], atol=1e-13, rtol=0)
+        np.testing.assert_allclose(aa, a[f"{tag}_aa"], atol=1e-13, rtol=0)
+        np.testing.assert_allclose(ab, a[f"{tag}_ab"], atol=1e-13, rtol=0)
+        np.testing.assert_allclose(bb, a[f"{tag}_bb"], atol=1e-13, rtol=0)
+    ed = O.dens_energy(ints, r1, aa, ab, bb)
+    assert abs(ed - meta[tag]["dens_energy"]) < 1e-11
+    assert abs(ed - meta[tag]["e0"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["c0", "c4"])
+def test_config_crs_matches_reference(name):
+    meta, a = load(name)
+    ints = config_integrals(name)
+    assert ints.checksum() == meta["integrals_sha"]
+    m = O.build_upper(O.FCI, ints)
+    assert m.n == meta["dim"] and m.nnz == meta["nnz"]
+    assert crs_sha256(m) == meta["crs_sha256"]
+
+
+def test_c0_eigenpair_and_rdm():
+    meta, a = load("c0")
+    ints = config_integrals("c0")
+    m = O.build_upper(O.FCI, ints)
+    e, c = O.lowest_eigenpair(m)
+    assert abs(e - meta["e0"]) < 1e-10
+    r1, aa, ab, bb = O.rdm(O.FCI, ints.L, ints.nup, ints.ndown, c)
+    np.testing.assert_allclose(r1, a["rdm1"], atol=1e-10)
+    np.testing.assert_allclose(ab, a["ab"], atol=1e-10)
+    np.testing.assert_allclose(aa, a["aa"], atol=1e-10)
+    # CIDens::test_invariants: trace(1-RDM) = N, trace(2-RDM) = N(N-1)/2, E_dens = E_CI
+    N = ints.nup + ints.ndown
+    assert abs(np.trace(r1[0]) + np.trace(r1[1]) - N) < 1e-11
+    tr2 = np.trace(aa) + np.trace(bb) + np.trace(ab)
+    assert abs(tr2 - N * (N - 1) / 2) < 1e-9
+    assert abs(O.dens_energy(ints, r1, aa, ab, bb) - e) < 1e-10
+
+
+def test_mvprod_matches_full_matrix():
+    ints = config_integrals("c0")
+    m = O.build_upper(O.FCI, ints)
+    x = np.random.default_rng(1).standard_normal(m.n)
+    y_ref = m.full_csr() @ x
+    np.testing.assert_allclose(O.sym_mvprod(m, x), y_ref, rtol=0, atol=1e-11)
+    np.testing.assert_allclose(O.sym_mvprod(m, x, threaded=True), y_ref, rtol=0, atol=1e-11)
+
+
+def test_oracle_rejects_bad_sizes():
+    lib = O.port()
+    assert lib.orc_build_upper(O.FCI, 70, 3, 3, None, None, None, None, None) != 0
+    assert lib.orc_build_upper(O.DOCI, 8, 3, 2, None, None, None, None, None) != 0
