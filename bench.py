@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the lowest-eigenpair CI path: solves/s and p50/p99 latency at
+|dE0| <= 1e-6 Eh, mixed precision vs plain FP64, on one GB300 per rank.
+
+Workload (default): FCI, 12 orbitals, 6 alpha + 6 beta electrons, 853,776
+determinants, seeded synthetic integrals (no dataset), ~1.55e9 stored
+nonzeros. One step = one full solve: CRS build from device-resident integrals
++ GPU-resident Lanczos to the residual target (+ FP64 corrections for mixed).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Multi-GPU runs are replicas (each rank solves its own instance; no data-path
+collective), scaling "weak". Rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s and p50/p99 latency at |dE0|<=1e-6 Eh, mixed vs plain FP64 on 1 GB300"
+CLOCK_FIELDS = ("index,uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["cigpu", "reference"], default="cigpu")
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--tol", type=float, default=1e-5, help="FP64 residual target (|dE0| ~ tol^2/gap)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 10:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = [r for r in self.rows if self.uuid is None or self.uuid in r[1]] or self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[2]) for r in rows if num(r[2]) is not None]
+        mx = [num(r[3]) for r in rows if num(r[3]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[6:10]) if v.strip().lower() == "active"})
+        under = sorted(sm)[len(sm) // 4:] if sm else []  # drop idle samples at the edges
+        return {"sm_mhz": statistics.median(under) if under else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[4]) or 0) for r in rows)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_full_workload:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float, n_matvec: int) -> dict:
+    """The CPU implementation of the path (the oracle's restatement of the reference
+    build and serial Sym::mvprod), timed on a bounded sample of rows and
+    extrapolated to one full solve: t = t_build + n_matvec * t_mvprod."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as O
+    from ciflow_gb300.synthetic import CONFIGS
+    method = O.DOCI if CONFIGS[cfg_name]["method"] == "DOCI" else O.FCI
+    n = O.dim(method, ints.L, ints.nup, ints.ndown)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    # size the sample from a short probe
+    probe = max(200, min(n, 2000))
+    t0 = time.perf_counter()
+    O.build_rows(method, ints, 0, probe)
+    tp = time.perf_counter() - t0
+    rows = int(min(n, max(probe, probe * (0.6 * target_s) / max(tp, 1e-6))))
+    stride_start = (n - rows) // 2
+    t0 = time.perf_counter()
+    off, col, val = O.build_rows(method, ints, stride_start, stride_start + rows)
+    t_build = time.perf_counter() - t0
+    x = np.random.default_rng(0).standard_normal(n)
+    y = np.zeros(n)
+    t0 = time.perf_counter()
+    O.sym_mvprod_rows(stride_start, off, col, val, x, y)
+    t_mv = time.perf_counter() - t0
+    frac = rows / n
+    full_build = t_build / frac
+    full_mv = t_mv / frac
+    t_solve = full_build + n_matvec * full_mv
+    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": (f"rows {stride_start}..{stride_start + rows} of {n} ({100 * frac:.2f}%): build "
+                       f"{t_build:.2f}s with {threads} threads (reference build_parallel algorithm, sorted "
+                       f"row insertion), serial Sym::mvprod {t_mv:.3f}s; extrapolated full build "
+                       f"{full_build:.1f}s + {n_matvec} matvecs x {full_mv:.2f}s"),
+            "extrapolated_build_s": full_build, "extrapolated_mvprod_s": full_mv}
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank: int, world: int):
+    """--impl reference: the reference CPU implementation of the path on the host
+    cores (the oracle port of the reference build + serial matvec, all threads),
+    rank 0 only."""
+    if rank != 0:
+        return
+    from ciflow_gb300.synthetic import CONFIGS, config_integrals
+    ints = config_integrals(args.config)
+    threads = host_threads()
+    # ARPACK-like solve: matvec count of a Lanczos solve to the same residual target
+    n_mv = 60
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(args.config, ints, threads, min(args.cpu_seconds, 4.0), n_mv)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args.config, ints, threads, args.cpu_seconds / 2, n_mv))
+    v = statistics.median([b["value"] for b in vals])
+    cfg = CONFIGS[args.config]
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals)",
+           "config": {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b", **cfg},
+           "cpu_baseline": {**vals[-1], "value": v},
+           "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_cigpu(args, rank: int, world: int, dist):
+    import numpy as np
+    import torch
+
+    from ciflow_gb300 import _abi as A
+    from ciflow_gb300.synthetic import CONFIGS, config_integrals
+
+    torch.cuda.set_device(0)
+    lib = A.lib()
+    cfg = CONFIGS[args.config]
+    method = A.DOCI if cfg["method"] == "DOCI" else A.FCI
+    ints = config_integrals(args.config)
+    golden = None
+    gpath = os.path.join(ROOT, "tests", "golden", f"{args.config}.json")
+    if os.path.exists(gpath):
+        with open(gpath) as f:
+            golden = json.load(f)
+    stream = torch.cuda.Stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    h = np.ascontiguousarray(ints.h)
+    eri = np.ascontiguousarray(ints.eri)
+    ham = ctypes.c_void_p()
+    A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri), ctypes.byref(ham)))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def solve_once(precision):
+        crs = ctypes.c_void_p()
+        A.check(lib.cigpu_build(ham, method, precision, sh, ctypes.byref(crs)), "build")
+        info = A.SolveInfo()
+        st = lib.cigpu_solve(crs, args.tol, 0, None, None, ctypes.byref(info))
+        lib.cigpu_crs_destroy(crs)
+        if st not in (A.OK, A.ENOCONV):
+            A.check(st, "solve")
+        return info
+
+    def timed(precision):
+        for _ in range(args.warmup):
+            solve_once(precision)
+        barrier()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        infos = []
+        l0 = lib.cigpu_kernel_launches()
+        for e0, e1 in evs:
+            e0.record(stream)
+            infos.append(solve_once(precision))
+            e1.record(stream)
+        barrier()
+        launches = lib.cigpu_kernel_launches() - l0
+        ms = [a.elapsed_time(b) for a, b in evs]
+        tot = sum(ms) / 1000.0
+        if dist is not None:
+            t = torch.tensor([tot], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return ms, tot, infos, launches
+
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(0).uuid)
+    except Exception:
+        pass
+
+    with ClockSampler(uuid) as clk:
+        ms_mixed, tot_mixed, inf_mixed, launches_mixed = timed(A.MIXED)
+        ms_plain, tot_plain, inf_plain, launches_plain = timed(A.FP64)
+
+    def summary(ms, tot, infos):
+        srt = sorted(ms)
+        de = [abs(i.e0 - golden["e0"]) for i in infos] if golden else []
+        return {"solves_per_s": world * len(ms) / tot, "ms_per_solve": statistics.mean(ms),
+                "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
+                "max_abs_dE0": max(de) if de else None, "residual": max(i.residual for i in infos),
+                "matvecs_fp64": infos[-1].matvecs_fp64, "matvecs_fp32": infos[-1].matvecs_fp32,
+                "restarts": infos[-1].restarts, "corrections": infos[-1].corrections}
+
+    mixed = summary(ms_mixed, tot_mixed, inf_mixed)
+    plain = summary(ms_plain, tot_plain, inf_plain)
+
+    # dominant kernel: the CRS matvec, timed alone with CUDA events on its stream
+    roof = {}
+    peaks = measured_peaks()
+    for prec, tag in ((A.MIXED, "fp32"), (A.FP64, "fp64")):
+        crs = ctypes.c_void_p()
+        A.check(lib.cigpu_build(ham, method, prec, sh, ctypes.byref(crs)))
+        dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        lib.cigpu_crs_dims(crs, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf))
+        dt = torch.float32 if tag == "fp32" else torch.float64
+        x = torch.randn(dim.value, device="cuda", dtype=dt)
+        y = torch.empty_like(x)
+        dtype_code = 1 if tag == "fp32" else 0
+        for _ in range(3):
+            lib.cigpu_mvprod_device(crs, A.ptr(x), A.ptr(y), dtype_code, sh)
+        reps = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            lib.cigpu_mvprod_device(crs, A.ptr(x), A.ptr(y), dtype_code, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1000.0 / reps
+        sv = 4 if tag == "fp32" else 8
+        n = dim.value
+        bytes_alg = nf.value * (sv + 4) + 8 * (n + 1) + n * sv + n * sv
+        ach = bytes_alg / t / 1e9
+        roof[tag] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{args.config}"),
+                     "algorithmic_bytes": bytes_alg, "ms_per_launch": t * 1000, "nnz_full": nf.value,
+                     "peak_source": peaks["source"]}
+        lib.cigpu_crs_destroy(crs)
+
+    # e2e through the C ABI with host buffers, H2D of the integrals and D2H of c inside the region
+    def e2e_once():
+        hh = ctypes.c_void_p()
+        A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri),
+                                     ctypes.byref(hh)))
+        crs = ctypes.c_void_p()
+        A.check(lib.cigpu_build(hh, method, A.MIXED, None, ctypes.byref(crs)))
+        info = A.SolveInfo()
+        lib.cigpu_solve(crs, args.tol, 0, None, A.ptr(c_host), ctypes.byref(info))
+        lib.cigpu_crs_destroy(crs)
+        lib.cigpu_ham_destroy(hh)
+        return info
+
+    dimv = golden["dim"] if golden else None
+    c_host = np.empty(dimv if dimv else 1)
+    if not dimv:
+        crs = ctypes.c_void_p()
+        A.check(lib.cigpu_build(ham, method, A.MIXED, sh, ctypes.byref(crs)))
+        d = ctypes.c_int64()
+        lib.cigpu_crs_dims(crs, ctypes.byref(d), None, None)
+        lib.cigpu_crs_destroy(crs)
+        c_host = np.empty(d.value)
+    e2e_once()
+    barrier()
+    t0 = time.perf_counter()
+    n_e2e = max(1, min(args.steps, 3))
+    for _ in range(n_e2e):
+        e2e_once()
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * n_e2e / t_e2e, "unit": "solves/s",
+           "h2d_bytes_per_step": int(h.nbytes + eri.nbytes), "d2h_bytes_per_step": int(c_host.nbytes),
+           "path": "cigpu_ham_create + cigpu_build(MIXED) + cigpu_solve(c_out host), pageable host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
+
+    lib.cigpu_ham_destroy(ham)
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": mixed["solves_per_s"], "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["ms_per_solve"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)",
+        "data": "synthetic (seeded integrals, no dataset)",
+        "config": {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b "
+                               f"({golden['dim'] if golden else '?'} determinants)",
+                   "name": args.config, **cfg, "tol_residual": args.tol,
+                   "l2": "inputs larger than L2 (CRS of ~1.55e9 nonzeros, 12-19 GB)",
+                   "parallelism": f"replicas x{world}"},
+        "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"],
+        "mixed": mixed, "plain_fp64": plain,
+        "mixed_over_plain": mixed["solves_per_s"] / plain["solves_per_s"],
+        "roofline": roof["fp32"], "roofline_fp64": roof["fp64"],
+        "e2e": e2e, "gpu_launches": launches_mixed,
+        "gpu_launches_plain": launches_plain,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        # one GPU per process: the library and torch both see it as device 0
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(0)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    try:
+        run_cigpu(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

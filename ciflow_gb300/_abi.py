@@ -1,0 +1,116 @@
+"""ctypes binding of libcigpu.so (the C ABI declared in include/cigpu.h).
+
+The library is the only compute path: importing this module loads the in-tree
+``ciflow_gb300/_lib/libcigpu.so`` and raises if it is missing -- there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libcigpu.so")
+
+OK, EINVAL, ENOMEM, EAGAIN, ECANCELED, ETIMEDOUT, ENOTSUP, ENOCONV, ECUDA, ENOTFOUND = (
+    0, 22, 12, 11, 125, 110, 95, 200, 201, 202)
+FCI, DOCI = 0, 1
+FP64, MIXED = 0, 1
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("e0", _D), ("residual", _D), ("error_bound", _D), ("gap", _D),
+                ("matvecs_fp64", _I64), ("matvecs_fp32", _I64), ("restarts", ctypes.c_int32),
+                ("corrections", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("seconds", _D)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32), ("nup", ctypes.c_int32), ("ndown", ctypes.c_int32),
+                ("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("want_rdm", ctypes.c_int32),
+                ("econst", _D), ("tol", _D), ("h", _P), ("eri", _P), ("c0", _P)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("done", ctypes.c_int32), ("dim", _I64), ("info", SolveInfo),
+                ("queued_s", _D), ("latency_s", _D)]
+
+
+# name -> (restype, argtypes); every symbol include/cigpu.h declares
+SIGNATURES = {
+    "cigpu_get_version": (_I, []),
+    "cigpu_strerror": (ctypes.c_char_p, [_I]),
+    "cigpu_device_count": (_I, [_P]),
+    "cigpu_kernel_launches": (_I64, []),
+    "cigpu_ham_create": (_I, [_I, _I, _I, _D, _P, _P, _P]),
+    "cigpu_ham_destroy": (_I, [_P]),
+    "cigpu_build": (_I, [_P, _I, _I, _P, _P]),
+    "cigpu_crs_destroy": (_I, [_P]),
+    "cigpu_crs_dims": (_I, [_P, _P, _P, _P]),
+    "cigpu_crs_export_upper": (_I, [_P, _P, _P, _P]),
+    "cigpu_crs_export_full": (_I, [_P, _P, _P, _P]),
+    "cigpu_mvprod": (_I, [_P, _P, _P]),
+    "cigpu_mvprod_device": (_I, [_P, _P, _P, _I, _P]),
+    "cigpu_solve": (_I, [_P, _D, _I64, _P, _P, _P]),
+    "cigpu_rdm": (_I, [_P, _P, _P, _P, _P, _P]),
+    "cigpu_server_create": (_I, [_I, ctypes.c_size_t, _I, _I, _P]),
+    "cigpu_server_submit": (_I, [_P, _P, _P]),
+    "cigpu_server_poll": (_I, [_P, ctypes.c_uint64, _I, _P, _P, _P]),
+    "cigpu_server_cancel": (_I, [_P, ctypes.c_uint64]),
+    "cigpu_server_stats": (_I, [_P, _P, _P, _P, _P]),
+    "cigpu_server_destroy": (_I, [_P]),
+    "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
+}
+
+_lib = None
+
+
+class CigpuError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = lib().cigpu_strerror(status).decode() if _lib is not None else str(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+def lib():
+    """The loaded library; raises if the CUDA extension has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libcigpu.so is missing ({LIB_PATH}); build it with "
+                              "`python -m ciflow_gb300.build` (nvcc, sm_103a)")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        raise CigpuError(status, what)
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array (host) or torch tensor (device); None passes NULL."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def device_count() -> int:
+    n = ctypes.c_int(0)
+    lib().cigpu_device_count(ctypes.byref(n))
+    return n.value

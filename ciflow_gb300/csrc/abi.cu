@@ -1,0 +1,467 @@
+// C ABI of the cigpu library (include/cigpu.h): handles, build orchestration,
+// export, matvec and solve entry points.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+
+#include "crs.cuh"
+#include "spmv.cuh"
+
+namespace cigpu {
+
+std::atomic<int64_t> g_launches{0};
+
+void *dev_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();  // clear the sticky-free allocation error
+        throw std::bad_alloc();
+    }
+    return p;
+}
+
+void SpinDevStore::upload(const SpinTables &t, cudaStream_t s) {
+    auto up = [&](auto &buf, const auto &vec) {
+        using T = typename std::decay_t<decltype(vec)>::value_type;
+        buf.alloc(vec.size());
+        if (!vec.empty())
+            CIGPU_CUDA(cudaMemcpyAsync(buf.p, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    };
+    up(occ, t.occ);
+    up(diag, t.diag);
+    up(s_target, t.s_target);
+    up(s_part, t.s_part);
+    up(s_info, t.s_info);
+    up(d_target, t.d_target);
+    up(d_val, t.d_val);
+    up(nb_full, t.nb_full);
+    up(nb_sing, t.nb_sing);
+    view = SpinDev{t.D, t.n, t.ns, t.nd, t.nfull, t.nsing, occ.p, diag.p, s_target.p, s_part.p,
+                   s_info.p, d_target.p, d_val.p, nb_full.p, nb_sing.p};
+}
+
+int status_from_exception() {
+    try {
+        throw;
+    } catch (const CudaError &e) {
+        std::fprintf(stderr, "cigpu: CUDA error %s in %s\n", cudaGetErrorString(e.err), e.what);
+        return CIGPU_ECUDA;
+    } catch (const std::bad_alloc &) {
+        return CIGPU_ENOMEM;
+    } catch (const std::invalid_argument &) {
+        return CIGPU_EINVAL;
+    } catch (...) {
+        return CIGPU_ECUDA;
+    }
+}
+
+static int64_t binom64(int n, int k) { return d_binom(n, k); }
+
+size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
+    int64_t dim, W;
+    if (method == CIGPU_DOCI) {
+        dim = binom64(L, nup);
+        W = 1 + (int64_t)nup * (L - nup);
+    } else {
+        dim = binom64(L, nup) * binom64(L, ndown);
+        const int64_t sa = (int64_t)nup * (L - nup), sb = (int64_t)ndown * (L - ndown);
+        W = 1 + sa + sb + sa * sb + binom64(nup, 2) * binom64(L - nup, 2) + binom64(ndown, 2) * binom64(L - ndown, 2);
+    }
+    const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
+    size_t b = (size_t)dim * W * (4 + vbytes);    // col + values
+    b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
+    b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
+    b += (size_t)dim * 8 * 5;                    // c, refinement vectors
+    b += (size_t)L * L * L * L * 8 + (64u << 20);  // integrals + tables/slack
+    return b;
+}
+
+void build_crs(cigpu_crs &c, cudaStream_t s) {
+    const auto t0 = std::chrono::steady_clock::now();
+    cigpu_ham &h = *c.ham;
+    const int64_t dim = c.dim;
+    c.diag.alloc(dim);
+    DevBuf<uint32_t> count(dim);
+    c.upper_off.alloc(dim);
+    c.row_ptr.alloc(dim + 1);
+    if (c.method == CIGPU_FCI) {
+        build_spin_tables(c.L, c.nup, h.h.data(), h.eri.data(), c.ta);
+        c.da.upload(c.ta, s);
+        if (c.ndown == c.nup) {
+            c.db.view = c.da.view;
+        } else {
+            build_spin_tables(c.L, c.ndown, h.h.data(), h.eri.data(), c.tb);
+            c.db.upload(c.tb, s);
+        }
+        FciParams &p = c.fp;
+        p.L = c.L;
+        p.Db = c.db.view.D;
+        p.a = c.da.view;
+        p.b = c.db.view;
+        p.eri = h.d_eri.p;
+        p.diag = c.diag.p;
+        fci_diag_launch(p, c.diag.p, s);
+        p.row_count = count.p;
+        p.upper_off = c.upper_off.p;
+        fci_launch(kCount, p, s);
+    } else {
+        c.strings.alloc(dim);
+        doci_strings_launch(c.L, c.nup, dim, c.strings.p, s);
+        DociParams &p = c.dp;
+        p.L = c.L;
+        p.n = c.nup;
+        p.W = 1 + c.nup * (c.L - c.nup);
+        p.D = dim;
+        p.fullmask = c.L >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << c.L) - 1);
+        p.strings = c.strings.p;
+        p.h = h.d_h.p;
+        p.eri = h.d_eri.p;
+        p.diag = c.diag.p;
+        doci_diag_launch(p, c.diag.p, s);
+        p.row_count = count.p;
+        p.upper_off = c.upper_off.p;
+        doci_launch(kCount, p, s);
+    }
+    exclusive_scan_u32(count.p, c.row_ptr.p, dim, s);
+    CIGPU_CUDA(cudaMemcpyAsync(&c.nnz_full, c.row_ptr.p + dim, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    // upper-triangle size (the reference CRS)
+    {
+        upper_counts_launch(dim, c.row_ptr.p, c.upper_off.p, count.p, s);
+        DevBuf<int64_t> urow(dim + 1);
+        exclusive_scan_u32(count.p, urow.p, dim, s);
+        CIGPU_CUDA(cudaMemcpyAsync(&c.nnz_upper, urow.p + dim, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+    }
+    count.release();
+    c.col.alloc(c.nnz_full);
+    const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
+    if (mode == kFill64)
+        c.val64.alloc(c.nnz_full);
+    else
+        c.val32.alloc(c.nnz_full);
+    if (c.method == CIGPU_FCI) {
+        c.fp.row_ptr = c.row_ptr.p;
+        c.fp.col = c.col.p;
+        c.fp.val64 = c.val64.p;
+        c.fp.val32 = c.val32.p;
+        fci_launch(mode, c.fp, s);
+    } else {
+        c.dp.row_ptr = c.row_ptr.p;
+        c.dp.col = c.col.p;
+        c.dp.val64 = c.val64.p;
+        c.dp.val32 = c.val32.p;
+        doci_launch(mode, c.dp, s);
+    }
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    c.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
+    if (c.precision == CIGPU_FP64) {
+        spmv_f64(c.dim, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
+        return;
+    }
+    // MIXED CRS stores FP32 values: regenerate the FP64 elements on the fly.
+    if (c.method == CIGPU_FCI) {
+        FciParams p = c.fp;
+        p.x = x;
+        p.y = y;
+        fci_launch(kMatvec64, p, s);
+    } else {
+        DociParams p = c.dp;
+        p.x = x;
+        p.y = y;
+        doci_launch(kMatvec64, p, s);
+    }
+}
+
+void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
+    if (c.precision != CIGPU_MIXED) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
+    spmv_f32(c.dim, c.row_ptr.p, c.col.p, c.val32.p, x, y, s);
+}
+
+}  // namespace cigpu
+
+using namespace cigpu;
+
+#define CIGPU_TRY try {
+#define CIGPU_CATCH \
+    }               \
+    catch (...) { return status_from_exception(); }
+
+extern "C" {
+
+int cigpu_get_version(void) { return CIGPU_ABI_VERSION; }
+
+const char *cigpu_strerror(int st) {
+    switch (st) {
+        case CIGPU_OK: return "ok";
+        case CIGPU_EINVAL: return "invalid argument";
+        case CIGPU_ENOMEM: return "out of memory or over the HBM budget";
+        case CIGPU_EAGAIN: return "queue full, retry";
+        case CIGPU_ECANCELED: return "cancelled";
+        case CIGPU_ETIMEDOUT: return "timed out";
+        case CIGPU_ENOTSUP: return "not supported";
+        case CIGPU_ENOCONV: return "eigensolver did not converge";
+        case CIGPU_ECUDA: return "CUDA error or no usable GPU";
+        case CIGPU_ENOTFOUND: return "unknown request";
+        default: return "unknown status";
+    }
+}
+
+int cigpu_device_count(int *count) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    if (count) *count = n;
+    return n > 0 ? CIGPU_OK : CIGPU_ECUDA;
+}
+
+int64_t cigpu_kernel_launches(void) { return g_launches.load(); }
+
+int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, const double *eri, cigpu_ham **out) {
+    if (!out || !h || !eri) return CIGPU_EINVAL;
+    *out = nullptr;
+    if (L < 1 || L > kMaxL || nup < 0 || ndown < 0 || nup > L || ndown > L) return CIGPU_EINVAL;
+    if (!std::isfinite(econst)) return CIGPU_EINVAL;
+    const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
+    // host validation: finite, h symmetric, eri 8-fold symmetric (relative 1e-10)
+    double hmax = 0, emax = 0;
+    for (size_t i = 0; i < L2; ++i) {
+        if (!std::isfinite(h[i])) return CIGPU_EINVAL;
+        hmax = std::max(hmax, std::fabs(h[i]));
+    }
+    for (size_t i = 0; i < L4; ++i) {
+        if (!std::isfinite(eri[i])) return CIGPU_EINVAL;
+        emax = std::max(emax, std::fabs(eri[i]));
+    }
+    const double htol = 1e-10 * std::max(1.0, hmax), etol = 1e-10 * std::max(1.0, emax);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j)
+            if (std::fabs(h[i * L1 + j] - h[j * L1 + i]) > htol) return CIGPU_EINVAL;
+    bool exact = true;
+    for (int p = 0; p < L; ++p)
+        for (int q = 0; q < L; ++q)
+            for (int r = 0; r < L; ++r)
+                for (int s = 0; s < L; ++s) {
+                    const double v = eri[p * L3 + q * L2 + r * L1 + s];
+                    const double a = eri[q * L3 + p * L2 + r * L1 + s];
+                    const double b = eri[r * L3 + s * L2 + p * L1 + q];
+                    const double c = eri[p * L3 + q * L2 + s * L1 + r];
+                    if (std::fabs(v - a) > etol || std::fabs(v - b) > etol || std::fabs(v - c) > etol)
+                        return CIGPU_EINVAL;
+                    exact = exact && v == a && v == b && v == c;
+                }
+    CIGPU_TRY
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return CIGPU_ECUDA;
+    }
+    std::unique_ptr<cigpu_ham> H(new cigpu_ham);
+    H->L = L;
+    H->nup = nup;
+    H->ndown = ndown;
+    H->econst = econst;
+    H->h.assign(h, h + L2);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < i; ++j) H->h[i * L1 + j] = H->h[j * L1 + i];
+    H->eri.assign(eri, eri + L4);
+    if (!exact) {
+        // tolerate round-off asymmetry: every permutation takes the value of its
+        // canonical representative (p>=q, r>=s, pq>=rs)
+        for (int p = 0; p < L; ++p)
+            for (int q = 0; q < L; ++q)
+                for (int r = 0; r < L; ++r)
+                    for (int s = 0; s < L; ++s) {
+                        int a = std::max(p, q), b = std::min(p, q), c = std::max(r, s), d = std::min(r, s);
+                        if (a * L + b < c * L + d) {
+                            std::swap(a, c);
+                            std::swap(b, d);
+                        }
+                        H->eri[p * L3 + q * L2 + r * L1 + s] = eri[a * L3 + b * L2 + c * L1 + d];
+                    }
+    }
+    H->d_h.alloc(L2);
+    H->d_eri.alloc(L4);
+    CIGPU_CUDA(cudaMemcpy(H->d_h.p, H->h.data(), L2 * sizeof(double), cudaMemcpyHostToDevice));
+    CIGPU_CUDA(cudaMemcpy(H->d_eri.p, H->eri.data(), L4 * sizeof(double), cudaMemcpyHostToDevice));
+    *out = H.release();
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_ham_destroy(cigpu_ham *ham) {
+    delete ham;
+    return CIGPU_OK;
+}
+
+int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes) {
+    if (!bytes || L < 1 || L > kMaxL || nup < 0 || ndown < 0 || nup > L || ndown > L) return CIGPU_EINVAL;
+    if (method != CIGPU_FCI && method != CIGPU_DOCI) return CIGPU_EINVAL;
+    *bytes = estimate_bytes(L, nup, ndown, method, precision);
+    return CIGPU_OK;
+}
+
+int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, cigpu_crs **out) {
+    if (!ham || !out) return CIGPU_EINVAL;
+    *out = nullptr;
+    if (method != CIGPU_FCI && method != CIGPU_DOCI) return CIGPU_EINVAL;
+    if (precision != CIGPU_FP64 && precision != CIGPU_MIXED) return CIGPU_EINVAL;
+    if (method == CIGPU_DOCI && ham->nup != ham->ndown) return CIGPU_EINVAL;
+    if (method == CIGPU_DOCI && ham->nup > 32) return CIGPU_ENOTSUP;
+    const int64_t dim = method == CIGPU_DOCI ? binom64(ham->L, ham->nup)
+                                             : binom64(ham->L, ham->nup) * binom64(ham->L, ham->ndown);
+    if (dim < 1 || dim > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
+    CIGPU_TRY
+    std::unique_ptr<cigpu_crs> c(new cigpu_crs);
+    c->ham = ham;
+    c->method = method;
+    c->precision = precision;
+    c->L = ham->L;
+    c->nup = ham->nup;
+    c->ndown = ham->ndown;
+    c->dim = dim;
+    if (stream) {
+        c->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        CIGPU_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    build_crs(*c, c->stream);
+    *out = c.release();
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_crs_destroy(cigpu_crs *crs) {
+    if (crs && crs->stream) cudaStreamSynchronize(crs->stream);
+    delete crs;
+    return CIGPU_OK;
+}
+
+int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full) {
+    if (!crs) return CIGPU_EINVAL;
+    if (dim) *dim = crs->dim;
+    if (nnz_upper) *nnz_upper = crs->nnz_upper;
+    if (nnz_full) *nnz_full = crs->nnz_full;
+    return CIGPU_OK;
+}
+
+int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val) {
+    if (!crs || !row || !col || !val) return CIGPU_EINVAL;
+    if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
+    CIGPU_TRY
+    cudaStream_t s = crs->stream;
+    const int64_t dim = crs->dim;
+    DevBuf<uint32_t> ucnt(dim);
+    DevBuf<int64_t> urow(dim + 1);
+    upper_counts_launch(dim, crs->row_ptr.p, crs->upper_off.p, ucnt.p, s);
+    exclusive_scan_u32(ucnt.p, urow.p, dim, s);
+    DevBuf<uint32_t> ucol(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
+    DevBuf<double> uval(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
+    extract_upper_launch(dim, crs->row_ptr.p, crs->upper_off.p, crs->col.p, crs->val64.p, crs->val32.p, urow.p,
+                         ucol.p, uval.p, s);
+    std::vector<int64_t> hr(dim + 1);
+    CIGPU_CUDA(cudaMemcpyAsync(hr.data(), urow.p, sizeof(int64_t) * (dim + 1), cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaMemcpyAsync(col, ucol.p, sizeof(uint32_t) * crs->nnz_upper, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaMemcpyAsync(val, uval.p, sizeof(double) * crs->nnz_upper, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i <= dim; ++i) row[i] = (uint32_t)hr[i];
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *val) {
+    if (!crs || !row || !col || !val) return CIGPU_EINVAL;
+    CIGPU_TRY
+    cudaStream_t s = crs->stream;
+    CIGPU_CUDA(cudaMemcpyAsync(row, crs->row_ptr.p, sizeof(int64_t) * (crs->dim + 1), cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaMemcpyAsync(col, crs->col.p, sizeof(uint32_t) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+    if (crs->precision == CIGPU_FP64) {
+        CIGPU_CUDA(cudaMemcpyAsync(val, crs->val64.p, sizeof(double) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+    } else {
+        std::vector<float> tmp(crs->nnz_full);
+        CIGPU_CUDA(cudaMemcpyAsync(tmp.data(), crs->val32.p, sizeof(float) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+        for (int64_t i = 0; i < crs->nnz_full; ++i) val[i] = tmp[i];
+    }
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y) {
+    if (!crs || !x || !y) return CIGPU_EINVAL;
+    CIGPU_TRY
+    cudaStream_t s = crs->stream;
+    DevBuf<double> dx(crs->dim), dy(crs->dim);
+    CIGPU_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
+    crs_mv64(*crs, dx.p, dy.p, s);
+    CIGPU_CUDA(cudaMemcpyAsync(y, dy.p, sizeof(double) * crs->dim, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_mvprod_device(cigpu_crs *crs, const void *x, void *y, int dtype, cigpu_stream stream) {
+    if (!crs || !x || !y || (dtype != 0 && dtype != 1)) return CIGPU_EINVAL;
+    if (dtype == 1 && crs->precision != CIGPU_MIXED) return CIGPU_EINVAL;
+    CIGPU_TRY
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : crs->stream;
+    if (dtype == 0)
+        crs_mv64(*crs, static_cast<const double *>(x), static_cast<double *>(y), s);
+    else
+        crs_mv32(*crs, static_cast<const float *>(x), static_cast<float *>(y), s);
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0, double *c_out,
+                cigpu_solve_info *info) {
+    if (!crs || !(tol > 0) || max_matvec < 0) return CIGPU_EINVAL;
+    CIGPU_TRY
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = crs->stream;
+    DevBuf<double> c(crs->dim);
+    if (c0) CIGPU_CUDA(cudaMemcpyAsync(c.p, c0, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
+    SolveProblem P;
+    P.n = crs->dim;
+    P.stream = s;
+    P.diag = crs->diag.p;
+    P.mv64 = [crs](const double *x, double *y, cudaStream_t st) { crs_mv64(*crs, x, y, st); };
+    if (crs->precision == CIGPU_MIXED)
+        P.mv32 = [crs](const float *x, float *y, cudaStream_t st) { crs_mv32(*crs, x, y, st); };
+    SolveOptions o;
+    o.tol = tol;
+    o.max_matvec = max_matvec;
+    cigpu_solve_info inf{};
+    const int st = crs->precision == CIGPU_MIXED ? solve_mixed(P, o, c.p, c0 != nullptr, inf)
+                                                 : solve_fp64(P, o, c.p, c0 != nullptr, inf);
+    inf.e0 += crs->ham->econst;
+    if (c_out) CIGPU_CUDA(cudaMemcpyAsync(c_out, c.p, sizeof(double) * crs->dim, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = inf;
+    return st;
+    CIGPU_CATCH
+}
+
+int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *aa, double *ab, double *bb) {
+    if (!crs || !c) return CIGPU_EINVAL;
+    CIGPU_TRY
+    cudaStream_t s = crs->stream;
+    DevBuf<double> dc(crs->dim);
+    CIGPU_CUDA(cudaMemcpyAsync(dc.p, c, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
+    crs_rdm(*crs, dc.p, rdm1, aa, ab, bb, s);
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+}  // extern "C"

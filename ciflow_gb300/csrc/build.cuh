@@ -1,0 +1,81 @@
+// Device-side parameter blocks and launchers of the CRS build.
+#pragma once
+
+#include "cigpu_internal.h"
+
+namespace cigpu {
+
+enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2, kMatvec64 = 3 };
+
+constexpr int kFciThreads = 128;
+constexpr int kFciRowsPerBlock = 32;
+constexpr int kDociThreads = 128;
+
+struct FciParams {
+    int L;
+    int64_t Db;
+    SpinDev a, b;
+    const double *eri;  // chemist (pq|rs), L^4
+    const double *diag; // [dim] row diagonals
+    // COUNT outputs
+    uint32_t *row_count;
+    uint32_t *upper_off;
+    // FILL inputs / outputs
+    const int64_t *row_ptr;
+    uint32_t *col;
+    double *val64;
+    float *val32;
+    // MATVEC
+    const double *x;
+    double *y;
+};
+
+struct DociParams {
+    int L, n, W;
+    int64_t D;
+    uint64_t fullmask;
+    const uint64_t *strings;
+    const double *h;
+    const double *eri;
+    const double *diag;
+    uint32_t *row_count;
+    uint32_t *upper_off;
+    const int64_t *row_ptr;
+    uint32_t *col;
+    double *val64;
+    float *val32;
+    const double *x;
+    double *y;
+};
+
+__host__ __device__ inline int64_t d_binom(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    if (k > n - k) k = n - k;
+    int64_t r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    return r;
+}
+
+// Position of the a-th (0-based) set bit of x.
+__device__ __forceinline__ int nth_set(uint64_t x, int a) {
+    for (int i = 0; i < a; ++i) x &= x - 1;
+    return __ffsll((long long)x) - 1;
+}
+
+size_t fci_smem_bytes(const FciParams &p);
+void fci_launch(int mode, const FciParams &p, cudaStream_t s);
+void fci_diag_launch(const FciParams &p, double *diag, cudaStream_t s);
+size_t doci_smem_bytes(int W, int warps);
+void doci_strings_launch(int L, int n, int64_t D, uint64_t *strings, cudaStream_t s);
+void doci_diag_launch(const DociParams &p, double *diag, cudaStream_t s);
+void doci_launch(int mode, const DociParams &p, cudaStream_t s);
+void upper_counts_launch(int64_t dim, const int64_t *row_ptr, const uint32_t *upper_off, uint32_t *ucnt,
+                         cudaStream_t s);
+void extract_upper_launch(int64_t dim, const int64_t *row_ptr, const uint32_t *upper_off, const uint32_t *col,
+                          const double *val64, const float *val32, const int64_t *urow, uint32_t *ucol, double *uval,
+                          cudaStream_t s);
+// out[0] = 0, out[i+1] = in[0] + ... + in[i]; out has n+1 entries.
+void exclusive_scan_u32(const uint32_t *in, int64_t *out, int64_t n, cudaStream_t s);
+int sm_count();
+
+}  // namespace cigpu

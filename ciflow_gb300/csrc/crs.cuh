@@ -1,0 +1,46 @@
+// The CRS handle shared by the ABI, RDM and server translation units.
+#pragma once
+
+#include "build.cuh"
+#include "lanczos.cuh"
+
+struct cigpu_crs {
+    cigpu_ham *ham = nullptr;
+    int method = CIGPU_FCI, precision = CIGPU_FP64;
+    int L = 0, nup = 0, ndown = 0;
+    int64_t dim = 0, nnz_full = 0, nnz_upper = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // FCI string tables (host copies kept for the RDM code)
+    cigpu::SpinTables ta, tb;
+    cigpu::SpinDevStore da, db;
+    // DOCI pair strings
+    cigpu::DevBuf<uint64_t> strings;
+    // matrix
+    cigpu::DevBuf<double> diag;
+    cigpu::DevBuf<int64_t> row_ptr;
+    cigpu::DevBuf<uint32_t> col, upper_off;
+    cigpu::DevBuf<double> val64;
+    cigpu::DevBuf<float> val32;
+    cigpu::FciParams fp{};
+    cigpu::DociParams dp{};
+    double build_seconds = 0;
+
+    ~cigpu_crs() {
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace cigpu {
+// Builds the CRS for `ham` on stream `s` (throws on failure).
+void build_crs(cigpu_crs &c, cudaStream_t s);
+// FP64 product y = H x on the CRS stream (device pointers).
+void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s);
+// FP32 product (MIXED CRS only).
+void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s);
+// Device bytes a build + solve of this shape needs.
+size_t estimate_bytes(int L, int nup, int ndown, int method, int precision);
+// RDMs of device vector c (normalised); host outputs as in cigpu_rdm.
+void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s);
+int status_from_exception();
+}  // namespace cigpu

@@ -1,0 +1,626 @@
+// GPU-resident lowest-eigenpair solver.
+//
+// Replaces CIMethod::solve -> SparseMatrix_CRS::arpackDiagonalize
+// (CIMethod.cpp:241-264, SparseMatrix_CRS.cpp:360-481), where ARPACK's
+// implicitly restarted Lanczos (which='SA', ncv=42, tol=0) calls the serial
+// matvec through reverse communication. Here the Krylov basis lives in HBM and
+// every vector operation is a device kernel; the host only holds the small
+// projected matrix (<= 43 x 43) and diagonalises it.
+//
+// Plain (FP64): thick-restart Lanczos (Wu & Simon) with full classical
+// Gram-Schmidt re-orthogonalisation done twice per step; FP64 vectors and matvec.
+//
+// Mixed: the same Lanczos with FP32 vectors and the FP32 CRS (FP32 row
+// accumulation), FP64 dot products / recurrence / projected eigensolve. The
+// FP32 Ritz vector is then refined in FP64: w = H c with an FP64 matvec,
+// E = c.w (Rayleigh quotient), r = w - E c; while ||r|| > tol a correction cycle
+// runs an FP32 Krylov space from the diagonally preconditioned residual
+// t = r / (E - H_ii) and does the Rayleigh-Ritz step over [c, K(t)] in FP64
+// (the coupling column uses the FP64 product H c). The FP32 error only enters
+// the small correction, so each cycle gains several digits.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "lanczos.cuh"
+
+namespace cigpu {
+
+int sm_count();
+
+namespace {
+
+constexpr int kVecThreads = 256;
+constexpr int kMaxBasis = 64;
+constexpr int kDotChunk = 8;
+constexpr int kMaxKeep = 32;
+
+int vec_grid() { return sm_count() * 4; }
+
+template <typename VT, typename WT>
+__global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__ V, int64_t ld, int nvec,
+                                                          const WT *__restrict__ w, int64_t n,
+                                                          double *__restrict__ partial, int G) {
+    const int v0 = blockIdx.y * kDotChunk;
+    const int nv = min(kDotChunk, nvec - v0);
+    double acc[kDotChunk];
+#pragma unroll
+    for (int i = 0; i < kDotChunk; ++i) acc[i] = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const double wr = (double)w[r];
+#pragma unroll
+        for (int i = 0; i < kDotChunk; ++i)
+            if (i < nv) acc[i] += (double)V[(int64_t)(v0 + i) * ld + r] * wr;
+    }
+    __shared__ double sh[kDotChunk][kVecThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < kDotChunk; ++i) {
+        double a = acc[i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[i][warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double s = 0;
+        for (int k = 0; k < kVecThreads / 32; ++k) s += sh[threadIdx.x][k];
+        partial[(int64_t)(v0 + threadIdx.x) * G + blockIdx.x] = s;
+    }
+}
+
+// out[v] = sum_b partial[v*G + b], one warp per entry, fixed order.
+__global__ void k_reduce_partials(const double *__restrict__ partial, int G, int nvec, double *__restrict__ out) {
+    const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (v >= nvec) return;
+    double s = 0;
+    for (int b = lane; b < G; b += 32) s += partial[(int64_t)v * G + b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[v] = s;
+}
+
+// w -= sum_{i<nvec} V_i coef_i (FP64 arithmetic); partial ||w||^2 per block when nrm != nullptr.
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
+                                                        const double *__restrict__ coef, VT *__restrict__ w, int64_t n,
+                                                        double *__restrict__ nrm) {
+    __shared__ double c[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = coef[i];
+    __syncthreads();
+    double acc = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double x = (double)w[r];
+        for (int i = 0; i < nvec; ++i) x -= (double)V[(int64_t)i * ld + r] * c[i];
+        const VT xv = (VT)x;
+        w[r] = xv;
+        acc += (double)xv * (double)xv;
+    }
+    if (nrm) {
+        __shared__ double sh[kVecThreads / 32];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int k = 0; k < kVecThreads / 32; ++k) s += sh[k];
+            nrm[blockIdx.x] = s;
+        }
+    }
+}
+
+template <typename VT>
+__global__ void k_scale(VT *__restrict__ w, int64_t n, const double *__restrict__ nrm2) {
+    const double inv = 1.0 / sqrt(*nrm2);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        w[r] = (VT)((double)w[r] * inv);
+}
+
+// out_i = sum_{l<m} V_l Y[l + m*i], i < k (Y column-major on the device).
+template <typename VT, typename OT>
+__global__ void __launch_bounds__(kVecThreads) k_combine(const VT *__restrict__ V, int64_t ld, int m,
+                                                         const double *__restrict__ Y, int k, OT *__restrict__ out,
+                                                         int64_t ldo, int64_t n) {
+    __shared__ double y[kMaxBasis * kMaxKeep];
+    for (int i = threadIdx.x; i < m * k; i += blockDim.x) y[i] = Y[i];
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double acc[kMaxKeep];
+#pragma unroll
+        for (int i = 0; i < kMaxKeep; ++i) acc[i] = 0;
+        for (int l = 0; l < m; ++l) {
+            const double v = (double)V[(int64_t)l * ld + r];
+#pragma unroll
+            for (int i = 0; i < kMaxKeep; ++i)
+                if (i < k) acc[i] += v * y[l + m * i];
+        }
+#pragma unroll
+        for (int i = 0; i < kMaxKeep; ++i)
+            if (i < k) out[(int64_t)i * ldo + r] = (OT)acc[i];
+    }
+}
+
+// r = w - E c; partial ||r||^2.
+__global__ void __launch_bounds__(kVecThreads) k_residual(const double *__restrict__ w, const double *__restrict__ c,
+                                                          double E, double *__restrict__ r, int64_t n,
+                                                          double *__restrict__ nrm) {
+    double acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = w[i] - E * c[i];
+        r[i] = x;
+        acc += x * x;
+    }
+    __shared__ double sh[kVecThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int k = 0; k < kVecThreads / 32; ++k) s += sh[k];
+        nrm[blockIdx.x] = s;
+    }
+}
+
+// Davidson-type diagonal preconditioner t = r / (E - H_ii), guarded away from 0.
+__global__ void k_precond(const double *__restrict__ r, const double *__restrict__ diag, double E,
+                          double *__restrict__ t, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = E - diag[i];
+        if (fabs(d) < 1e-2) d = d < 0 ? -1e-2 : 1e-2;
+        t[i] = r[i] / d;
+    }
+}
+
+__global__ void k_axpby64(double a, const double *__restrict__ x, double b, double *__restrict__ y, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_random(double *v, int64_t n, uint64_t seed) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = splitmix64(seed * 0x100000001B3ull ^ (uint64_t)i);
+        v[i] = (double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    }
+}
+
+template <typename S, typename D>
+__global__ void k_convert(const S *__restrict__ s, D *__restrict__ d, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = (D)s[i];
+}
+
+// ---------------------------------------------------------------------------
+// Host-side helpers around the kernels.
+struct VecOps {
+    cudaStream_t s;
+    int G;
+    DevBuf<double> partial;  // [(kMaxBasis+1) * G]
+    DevBuf<double> out;      // [4 * (kMaxBasis+1)]
+    double *h_out = nullptr; // pinned
+    explicit VecOps(cudaStream_t st) : s(st), G(vec_grid()), partial((size_t)(kMaxBasis + 2) * vec_grid()),
+                                       out(4 * (kMaxBasis + 2)) {
+        CIGPU_CUDA(cudaMallocHost(&h_out, sizeof(double) * 4 * (kMaxBasis + 2)));
+    }
+    ~VecOps() {
+        if (h_out) cudaFreeHost(h_out);
+    }
+    // out[dst .. dst+nvec) = V_i . w
+    template <typename VT, typename WT>
+    void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst) {
+        dim3 grid(G, (nvec + kDotChunk - 1) / kDotChunk);
+        k_multidot<VT, WT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, G);
+        k_reduce_partials<<<(nvec + 7) / 8, 256, 0, s>>>(partial.p, G, nvec, out.p + dst);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch(2);
+    }
+    template <typename VT>
+    void update(const VT *V, int64_t ld, int nvec, int coef_at, VT *w, int64_t n, int nrm_at) {
+        k_update<VT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n, nrm_at >= 0 ? partial.p : nullptr);
+        count_launch();
+        if (nrm_at >= 0) {
+            k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p + nrm_at);
+            count_launch();
+        }
+        CIGPU_CUDA(cudaGetLastError());
+    }
+    template <typename VT>
+    void scale(VT *w, int64_t n, int nrm_at) {
+        k_scale<VT><<<G, kVecThreads, 0, s>>>(w, n, out.p + nrm_at);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+    }
+    // fetch out[0..cnt) to the host (synchronises the stream)
+    const double *fetch(int cnt) {
+        CIGPU_CUDA(cudaMemcpyAsync(h_out, out.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+        return h_out;
+    }
+    double residual(const double *w, const double *c, double E, double *r, int64_t n) {
+        k_residual<<<G, kVecThreads, 0, s>>>(w, c, E, r, n, partial.p);
+        k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch(2);
+        return std::sqrt(fetch(1)[0]);
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+void small_eigh(int n, std::vector<double> &a, std::vector<double> &w, std::vector<double> &z) {
+    z.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
+    double fro = 0;
+    for (double x : a) fro += x * x;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off += a[(size_t)p * n + q] * a[(size_t)p * n + q];
+        if (off <= 1e-30 * fro || off == 0.0) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = a[(size_t)p * n + q];
+                if (std::fabs(apq) < 1e-300) continue;
+                const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
+                // Rutishauser's rotation: zero a_pq with t = tan(phi), the smaller root of
+                // t^2 + 2 theta t - 1 = 0, theta = (a_qq - a_pp) / (2 a_pq)
+                const double theta = (aqq - app) / (2.0 * apq);
+                double t = 1.0 / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                if (theta < 0) t = -t;
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
+                    a[(size_t)k * n + p] = c * akp - s * akq;
+                    a[(size_t)k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
+                    a[(size_t)p * n + k] = c * apk - s * aqk;
+                    a[(size_t)q * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double zkp = z[(size_t)k * n + p], zkq = z[(size_t)k * n + q];
+                    z[(size_t)k * n + p] = c * zkp - s * zkq;
+                    z[(size_t)k * n + q] = s * zkp + c * zkq;
+                }
+            }
+    }
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
+    w.resize(n);
+    std::vector<double> zs((size_t)n * n);
+    for (int k = 0; k < n; ++k) {
+        w[k] = a[(size_t)idx[k] * n + idx[k]];
+        for (int i = 0; i < n; ++i) zs[(size_t)i * n + k] = z[(size_t)i * n + idx[k]];
+    }
+    z.swap(zs);
+}
+
+void dev_fill_random(double *v, int64_t n, uint64_t seed, cudaStream_t s) {
+    k_random<<<vec_grid(), kVecThreads, 0, s>>>(v, n, seed);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+void dev_convert(const double *src, float *dst, int64_t n, cudaStream_t s) {
+    k_convert<double, float><<<vec_grid(), kVecThreads, 0, s>>>(src, dst, n);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+void dev_convert(const float *src, double *dst, int64_t n, cudaStream_t s) {
+    k_convert<float, double><<<vec_grid(), kVecThreads, 0, s>>>(src, dst, n);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+namespace {
+
+// Thick-restart Lanczos on storage type VT.
+template <typename VT>
+struct TRLanczos {
+    int64_t n;
+    int m, keep;
+    cudaStream_t s;
+    VecOps &ops;
+    DevBuf<VT> V;     // (m+1) vectors of n
+    DevBuf<VT> tmp;   // keep vectors
+    DevBuf<double> Yd;
+    std::vector<double> T;  // (m+1) x (m+1) row-major
+    int j = 0;              // next vector to expand; V[0..j] valid, T columns [0, j) known
+    int64_t matvecs = 0;
+    int restarts = 0;
+    double theta0 = 0, theta1 = 0, resid_est = 1e300;
+    std::vector<double> y0;  // lowest Ritz vector of T[0..j)
+    std::function<void(const VT *, VT *, cudaStream_t)> mv;
+
+    TRLanczos(int64_t n_, int m_, int keep_, cudaStream_t s_, VecOps &o)
+        : n(n_), m(m_), keep(keep_), s(s_), ops(o), V((size_t)(m_ + 1) * n_), tmp((size_t)keep_ * n_),
+          Yd((size_t)m_ * keep_), T((size_t)(m_ + 1) * (m_ + 1), 0.0) {}
+
+    double &t(int i, int k) { return T[(size_t)i * (m + 1) + k]; }
+    VT *vec(int i) { return V.p + (size_t)i * n; }
+
+    // V[0] = normalised start
+    void start(const VT *v0) {
+        CIGPU_CUDA(cudaMemcpyAsync(vec(0), v0, sizeof(VT) * n, cudaMemcpyDeviceToDevice, s));
+        ops.dots(vec(0), n, 1, vec(0), n, 0);
+        ops.scale(vec(0), n, 0);
+        std::fill(T.begin(), T.end(), 0.0);
+        j = 0;
+    }
+
+    // One Lanczos step: expand V[j] -> V[j+1]. Returns the new beta.
+    double step() {
+        VT *w = vec(j + 1);
+        mv(vec(j), w, s);
+        ++matvecs;
+        const int nv = j + 1;
+        const int H1 = 0, H2 = kMaxBasis + 1, NR = 2 * (kMaxBasis + 1);
+        ops.dots(V.p, n, nv, w, n, H1);
+        ops.update(V.p, n, nv, H1, w, n, -1);
+        ops.dots(V.p, n, nv, w, n, H2);
+        ops.update(V.p, n, nv, H2, w, n, NR);
+        ops.scale(w, n, NR);
+        const double *h = ops.fetch(NR + 1);
+        for (int i = 0; i <= j; ++i) {
+            const double v = h[H1 + i] + h[H2 + i];
+            t(i, j) = v;
+            t(j, i) = v;
+        }
+        const double beta = std::sqrt(h[NR]);
+        t(j + 1, j) = beta;
+        t(j, j + 1) = beta;
+        ++j;
+        return beta;
+    }
+
+    // Ritz analysis of T[0..j); updates theta0/theta1/y0/resid_est.
+    void analyse(std::vector<double> *W = nullptr, std::vector<double> *Z = nullptr) {
+        std::vector<double> a((size_t)j * j), w, z;
+        for (int i = 0; i < j; ++i)
+            for (int k = 0; k < j; ++k) a[(size_t)i * j + k] = t(i, k);
+        small_eigh(j, a, w, z);
+        theta0 = w[0];
+        theta1 = j > 1 ? w[1] : w[0];
+        y0.resize(j);
+        for (int i = 0; i < j; ++i) y0[i] = z[(size_t)i * j];
+        resid_est = std::fabs(t(j, j - 1) * y0[j - 1]);
+        if (W) *W = w;
+        if (Z) *Z = z;
+    }
+
+    void restart() {
+        std::vector<double> w, z;
+        analyse(&w, &z);
+        const int kk = std::min(keep, m - 1);
+        std::vector<double> Y((size_t)m * kk);
+        for (int i = 0; i < kk; ++i)
+            for (int l = 0; l < m; ++l) Y[(size_t)i * m + l] = z[(size_t)l * m + i];
+        CIGPU_CUDA(cudaMemcpyAsync(Yd.p, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, s));
+        k_combine<VT, VT><<<ops.G, kVecThreads, 0, s>>>(V.p, n, m, Yd.p, kk, tmp.p, n, n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+        CIGPU_CUDA(cudaMemcpyAsync(vec(0), tmp.p, sizeof(VT) * n * kk, cudaMemcpyDeviceToDevice, s));
+        CIGPU_CUDA(cudaMemcpyAsync(vec(kk), vec(m), sizeof(VT) * n, cudaMemcpyDeviceToDevice, s));
+        const double beta = t(m, m - 1);
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int i = 0; i < kk; ++i) {
+            t(i, i) = w[i];
+            t(kk, i) = t(i, kk) = beta * z[(size_t)(m - 1) * m + i];
+        }
+        j = kk;
+        ++restarts;
+        CIGPU_CUDA(cudaStreamSynchronize(s));  // Y staging buffer is host memory
+    }
+
+    // c = V[0..j) y0 (FP64 output)
+    void ritz_vector(double *c_dev) {
+        CIGPU_CUDA(cudaMemcpyAsync(Yd.p, y0.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        k_combine<VT, double><<<ops.G, kVecThreads, 0, s>>>(V.p, n, j, Yd.p, 1, c_dev, n, n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+    }
+
+    // Iterate until resid_est <= max(abs_target, rel_target * max(1, |theta0|)), the
+    // matvec budget is spent, breakdown, or stagnation (no 10% gain in 3 cycles).
+    // Returns true when the target was met.
+    bool run(double abs_target, double rel_target, int64_t budget) {
+        using clk = std::chrono::steady_clock;
+        int check_every = 1, since = 0;
+        double best = 1e300;
+        int64_t best_at = matvecs;
+        auto target = [&] { return std::max(abs_target, rel_target * std::max(1.0, std::fabs(theta0))); };
+        while (matvecs < budget) {
+            const auto t0 = clk::now();
+            const double beta = step();
+            const auto t1 = clk::now();
+            ++since;
+            const bool full = (j == m) || (j >= n);
+            const bool breakdown = beta <= 1e-13 * std::max(1.0, std::fabs(theta0));
+            if (since >= check_every || full || breakdown) {
+                analyse();
+                const auto t2 = clk::now();
+                since = 0;
+                // keep the host eigensolve under ~10% of the device step time
+                const double ts = std::chrono::duration<double>(t1 - t0).count();
+                const double te = std::chrono::duration<double>(t2 - t1).count();
+                check_every = std::max(1, std::min(8, (int)(te / std::max(ts * 0.1, 1e-9))));
+                if (breakdown) resid_est = 0.0;
+                if (resid_est <= target()) return true;
+                if (resid_est < 0.9 * best) {
+                    best = resid_est;
+                    best_at = matvecs;
+                } else if (matvecs - best_at > 3 * m) {
+                    return false;  // stagnated (e.g. at the FP32 accuracy floor)
+                }
+            }
+            if (j >= n) return true;  // the whole space is spanned
+            if (j == m) restart();
+        }
+        analyse();
+        return resid_est <= target();
+    }
+};
+
+// FP64 Rayleigh quotient and residual of c (normalised in place).
+struct Refine {
+    int64_t n;
+    cudaStream_t s;
+    VecOps &ops;
+    DevBuf<double> w, r, t;
+    Refine(int64_t n_, cudaStream_t s_, VecOps &o) : n(n_), s(s_), ops(o), w(n_), r(n_), t(n_) {}
+    // returns (E, ||r||) with w = H c, r = w - E c
+    std::pair<double, double> eval(const SolveProblem &P, double *c) {
+        ops.dots(c, n, 1, c, n, 0);
+        ops.scale(c, n, 0);
+        P.mv64(c, w.p, s);
+        ops.dots(c, n, 1, w.p, n, 0);
+        const double E = ops.fetch(1)[0];
+        const double rn = ops.residual(w.p, c, E, r.p, n);
+        return {E, rn};
+    }
+};
+
+}  // namespace
+
+int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info) {
+    const int64_t n = P.n;
+    const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
+    const int m = (int)std::min<int64_t>(std::min(o.basis, kMaxBasis), std::max<int64_t>(n, 1));
+    const int keep = std::max(1, std::min({o.keep, m - 1, kMaxKeep}));
+    cudaStream_t s = P.stream;
+    VecOps ops(s);
+    if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
+    Refine ref(n, s, ops);
+    if (n == 1) {
+        auto er = ref.eval(P, c_dev);
+        info.e0 = er.first;
+        info.residual = er.second;
+        info.matvecs_fp64 = 1;
+        info.converged = 1;
+        return CIGPU_OK;
+    }
+    TRLanczos<double> lz(n, m, keep, s, ops);
+    lz.mv = [&](const double *x, double *y, cudaStream_t st) { P.mv64(x, y, st); };
+    lz.start(c_dev);
+    double target = o.tol;
+    std::pair<double, double> er{0, 1e300};
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        const bool ok = lz.run(target, 0.0, budget);
+        lz.ritz_vector(c_dev);
+        er = ref.eval(P, c_dev);
+        if (er.second <= o.tol || !ok) break;
+        // the estimate was optimistic: tighten it and keep iterating
+        target = std::max(target * 0.1, 1e-15);
+    }
+    info.e0 = er.first;
+    info.residual = er.second;
+    info.gap = lz.theta1 - lz.theta0;
+    info.error_bound = info.gap > 0 ? er.second * er.second / info.gap : er.second;
+    info.matvecs_fp64 = lz.matvecs + 1 + 0;
+    info.restarts = lz.restarts;
+    info.converged = er.second <= o.tol;
+    return info.converged ? CIGPU_OK : CIGPU_ENOCONV;
+}
+
+int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info) {
+    const int64_t n = P.n;
+    const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
+    const int m = (int)std::min<int64_t>(std::min(o.basis, kMaxBasis), std::max<int64_t>(n, 1));
+    const int keep = std::max(1, std::min({o.keep, m - 1, kMaxKeep}));
+    cudaStream_t s = P.stream;
+    VecOps ops(s);
+    Refine ref(n, s, ops);
+    if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
+    if (n <= 2 || !P.mv32) return solve_fp64(P, o, c_dev, true, info);
+
+    // Phase 1: FP32 thick-restart Lanczos to the FP32 accuracy floor.
+    int64_t mv32 = 0, mv64 = 0;
+    int restarts = 0, corrections = 0;
+    double gap = 0;
+    {
+        TRLanczos<float> lz(n, m, keep, s, ops);
+        lz.mv = [&](const float *x, float *y, cudaStream_t st) { P.mv32(x, y, st); };
+        DevBuf<float> v0(n);
+        dev_convert(c_dev, v0.p, n, s);
+        lz.start(v0.p);
+        // FP32 vectors stall near a residual of ~1e-6 |E|; stop above that floor and
+        // let the FP64 corrections finish.
+        lz.run(o.tol, o.mixed_rel, budget);
+        lz.ritz_vector(c_dev);
+        mv32 += lz.matvecs;
+        restarts = lz.restarts;
+        gap = lz.theta1 - lz.theta0;
+    }
+    // Phase 2: FP64 Rayleigh quotient / residual and correction cycles.
+    auto er = ref.eval(P, c_dev);
+    ++mv64;
+    const int p = std::max(2, std::min(o.corr_steps, m - 1));
+    while (er.second > o.tol && corrections < o.max_corrections && mv32 + mv64 < budget) {
+        ++corrections;
+        const double E = er.first;
+        // t = preconditioned residual, orthogonalised against c in FP64
+        k_precond<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, ref.t.p, n);
+        count_launch();
+        ops.dots(c_dev, n, 1, ref.t.p, n, 0);
+        ops.update(c_dev, n, 1, 0, ref.t.p, n, 1);
+        ops.scale(ref.t.p, n, 1);
+        // FP32 Krylov space from t with c as a locked first vector
+        TRLanczos<float> lz(n, p + 1, 1, s, ops);
+        lz.mv = [&](const float *x, float *y, cudaStream_t st) { P.mv32(x, y, st); };
+        dev_convert(c_dev, lz.vec(0), n, s);
+        dev_convert(ref.t.p, lz.vec(1), n, s);
+        lz.j = 1;
+        for (int k = 1; k < p && lz.matvecs + mv32 + mv64 < budget; ++k) {
+            const double beta = lz.step();
+            if (beta <= 1e-10) break;
+        }
+        mv32 += lz.matvecs;
+        const int q = lz.j;  // basis [c, v_1 .. v_{q-1}] (v_q is the unused next direction)
+        // projected matrix: FP64 coupling of c (w = H c), FP32-accurate Lanczos block elsewhere
+        ops.dots(lz.V.p, n, q, ref.w.p, n, 0);
+        const double *hc = ops.fetch(q);
+        std::vector<double> G((size_t)q * q, 0.0);
+        G[0] = E;
+        for (int i = 1; i < q; ++i) G[i] = G[(size_t)i * q] = hc[i];
+        for (int i = 1; i < q; ++i)
+            for (int k = 1; k < q; ++k) G[(size_t)i * q + k] = lz.t(i, k);
+        std::vector<double> w, z;
+        small_eigh(q, G, w, z);
+        // c <- y0 c + sum_i y_i v_i  (FP64)
+        std::vector<double> y(q);
+        for (int i = 0; i < q; ++i) y[i] = z[(size_t)i * q];
+        if (q > 1) {
+            y[0] = 0;
+            CIGPU_CUDA(cudaMemcpyAsync(lz.Yd.p, y.data(), sizeof(double) * q, cudaMemcpyHostToDevice, s));
+            k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(lz.V.p, n, q, lz.Yd.p, 1, ref.t.p, n, n);
+            count_launch();
+            k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, z[0], c_dev, n);
+            count_launch();
+            CIGPU_CUDA(cudaGetLastError());
+            CIGPU_CUDA(cudaStreamSynchronize(s));
+        }
+        er = ref.eval(P, c_dev);
+        ++mv64;
+    }
+    info.e0 = er.first;
+    info.residual = er.second;
+    info.gap = gap;
+    info.error_bound = gap > 0 ? er.second * er.second / gap : er.second;
+    info.matvecs_fp64 = mv64;
+    info.matvecs_fp32 = mv32;
+    info.restarts = restarts;
+    info.corrections = corrections;
+    info.converged = er.second <= o.tol;
+    return info.converged ? CIGPU_OK : CIGPU_ENOCONV;
+}
+
+}  // namespace cigpu

@@ -1,0 +1,114 @@
+// CRS matrix-vector product on the device.
+//
+// Replaces SparseMatrix_CRS_Sym::mvprod (SparseMatrix_CRS.cpp:700-723), the
+// serial symmetric scatter over the upper triangle. The device keeps the full
+// symmetric matrix, so y = H x is a plain row gather with no atomics and a
+// fixed summation order (bit-reproducible run to run):
+//   * one warp per row, rows dealt round-robin to a persistent grid;
+//   * col/val are streamed once (ld.global.cs: they are not reused, so they
+//     must not evict x from L2); x is gathered through the read-only path and
+//     stays L2-resident (853,776 doubles = 6.8 MB for the L=12 FCI space);
+//   * 16-byte vector loads for the aligned body of each row.
+// FP64: double values, double x/y, double accumulation.
+// FP32 (mixed method): float values, float x/y, float row accumulation.
+#include "spmv.cuh"
+
+namespace cigpu {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p) {
+    return __ldcs(p);
+}
+
+// Row body with 16-byte loads: 4 columns (uint4) and 4 values (2x double2 or float4).
+template <typename VT>
+struct Vec4;
+template <>
+struct Vec4<double> {
+    __device__ __forceinline__ static void load(const double *p, double v[4]) {
+        const double2 a = __ldcs(reinterpret_cast<const double2 *>(p));
+        const double2 b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+};
+template <>
+struct Vec4<float> {
+    __device__ __forceinline__ static void load(const float *p, float v[4]) {
+        const float4 a = __ldcs(reinterpret_cast<const float4 *>(p));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+};
+
+template <typename VT>
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv_warp(int64_t n, const int64_t *__restrict__ row_ptr,
+                                                            const uint32_t *__restrict__ col,
+                                                            const VT *__restrict__ val, const VT *__restrict__ x,
+                                                            VT *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = wid; r < n; r += nw) {
+        const int64_t s = row_ptr[r], e = row_ptr[r + 1];
+        VT acc = 0;
+        // scalar head up to a multiple of 4 elements (16-byte boundary for both arrays)
+        const int64_t s4 = (s + 3) & ~(int64_t)3;
+        const int64_t head_end = s4 < e ? s4 : e;
+        if (s + lane < head_end) {
+            const int64_t k = s + lane;
+            acc += ld_stream(val + k) * __ldg(x + ld_stream(col + k));
+        }
+        // vector body: each lane takes 4 consecutive elements per iteration
+        const int64_t nb = (e > s4) ? ((e - s4) >> 2) : 0;
+        for (int64_t b = lane; b < nb; b += 32) {
+            const int64_t k = s4 + (b << 2);
+            const uint4 c = __ldcs(reinterpret_cast<const uint4 *>(col + k));
+            VT v[4];
+            Vec4<VT>::load(val + k, v);
+            acc += v[0] * __ldg(x + c.x);
+            acc += v[1] * __ldg(x + c.y);
+            acc += v[2] * __ldg(x + c.z);
+            acc += v[3] * __ldg(x + c.w);
+        }
+        // scalar tail
+        const int64_t t0 = s4 + (nb << 2);
+        if (t0 >= s4 && t0 + lane < e && t0 + lane >= head_end) {
+            const int64_t k = t0 + lane;
+            acc += ld_stream(val + k) * __ldg(x + ld_stream(col + k));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) y[r] = acc;
+    }
+}
+
+}  // namespace
+
+int spmv_grid() { return sm_count_spmv() * kSpmvBlocksPerSM; }
+
+int sm_count_spmv() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
+void spmv_f64(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x, double *y,
+              cudaStream_t s) {
+    k_spmv_warp<double><<<spmv_grid(), kSpmvThreads, 0, s>>>(n, row_ptr, col, val, x, y);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void spmv_f32(int64_t n, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
+              cudaStream_t s) {
+    k_spmv_warp<float><<<spmv_grid(), kSpmvThreads, 0, s>>>(n, row_ptr, col, val, x, y);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+}  // namespace cigpu

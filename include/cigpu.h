@@ -1,0 +1,180 @@
+/* cigpu: GB300-native lowest-eigenpair CI core, C ABI.
+ *
+ * This is the drop-in boundary for CIFlow's lowest-eigenpair path. Each entry
+ * point names the reference interface (file:line in the CIFlow tree) whose job
+ * it takes over. All compute runs in hand-written sm_103a CUDA kernels; there is
+ * no CPU fallback: without a usable GPU every compute call returns
+ * CIGPU_ECUDA.
+ *
+ * Conventions
+ *  - Every call returns an int status (CIGPU_OK == 0). Nothing exits or traps.
+ *  - Handles own their device memory; the caller owns every host buffer.
+ *  - Integrals: h is L*L row-major and symmetric; eri is the chemist-notation
+ *    tensor (pq|rs), L^4 row-major, 8-fold symmetric. The physics element the
+ *    reference uses is V(i,j,k,l) = <ij|kl> = (ik|jl).
+ *  - Determinants are ordered like CIFlow: row = I_alpha * D_beta + I_beta, each
+ *    string ranked in colex (Gosper) order; DOCI rows are pair strings.
+ *  - Energies returned by the solvers include Econst.
+ *  - A handle is used by one host thread at a time; distinct handles may be
+ *    used concurrently. The server object is internally synchronised.
+ */
+#ifndef CIGPU_H
+#define CIGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CIGPU_ABI_VERSION 1
+
+typedef struct cigpu_ham cigpu_ham;
+typedef struct cigpu_crs cigpu_crs;
+typedef struct cigpu_server cigpu_server;
+/* A cudaStream_t passed as an opaque pointer; NULL selects the handle's own stream. */
+typedef void *cigpu_stream;
+
+enum cigpu_status {
+    CIGPU_OK = 0,
+    CIGPU_EINVAL = 22,     /* bad argument, size or non-symmetric / non-finite integrals */
+    CIGPU_ENOMEM = 12,     /* device or host allocation failed, or HBM budget exceeded */
+    CIGPU_EAGAIN = 11,     /* server queue full: retry later */
+    CIGPU_ECANCELED = 125, /* request cancelled */
+    CIGPU_ETIMEDOUT = 110, /* a bounded wait expired */
+    CIGPU_ENOTSUP = 95,    /* combination not supported (e.g. L > 63) */
+    CIGPU_ENOCONV = 200,   /* eigensolver hit its matvec limit before the tolerance */
+    CIGPU_ECUDA = 201,     /* CUDA error or no usable GPU */
+    CIGPU_ENOTFOUND = 202  /* unknown request id */
+};
+
+enum cigpu_method { CIGPU_FCI = 0, CIGPU_DOCI = 1 };
+/* FP64: FP64 CRS values, FP64 Krylov vectors, FP64 matvec.
+ * MIXED: FP32 CRS values and FP32 Krylov vectors with FP32 row accumulation;
+ *        FP64 orthogonalisation coefficients, recurrence, projected eigensolve,
+ *        Rayleigh quotient and residual (FP64 matvec) with residual-correction
+ *        restarts. */
+enum cigpu_precision { CIGPU_FP64 = 0, CIGPU_MIXED = 1 };
+
+typedef struct {
+    double e0;               /* lowest eigenvalue including Econst */
+    double residual;         /* ||H c - E c||_2 with ||c|| = 1, computed with an FP64 matvec */
+    double error_bound;      /* residual^2 / gap estimate (bound on |E - E_exact|) */
+    double gap;              /* estimated gap to the next Ritz value */
+    int64_t matvecs_fp64;    /* FP64 matrix-vector products */
+    int64_t matvecs_fp32;    /* FP32 matrix-vector products */
+    int32_t restarts;        /* thick restarts */
+    int32_t corrections;     /* FP64 residual-correction cycles (MIXED) */
+    int32_t converged;       /* 1 when residual <= tol */
+    int32_t reserved;
+    double seconds;          /* wall time of the solve */
+} cigpu_solve_info;
+
+/* ---- library ---- */
+int cigpu_get_version(void);
+const char *cigpu_strerror(int status);
+/* Number of CUDA devices visible (0 without a GPU; returns CIGPU_ECUDA then). */
+int cigpu_device_count(int *count);
+/* Kernels this library launched since load (for launch accounting). */
+int64_t cigpu_kernel_launches(void);
+
+/* ---- Hamiltonian: replaces Hamiltonian(L, nGroup=0, nup, ndown, Econst) plus
+ * setTmat/setVmat (Hamiltonian.cpp:77-113, 255-320) and the getTmat/getVmat
+ * lookups every matrix element goes through (FourIndex.cpp:175-315). The tensors
+ * are copied to the device as dense tables. ---- */
+int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, const double *eri,
+                     cigpu_ham **out);
+int cigpu_ham_destroy(cigpu_ham *ham);
+
+/* ---- CRS build: replaces new FCI(ham) / new DOCI(ham), i.e.
+ * CIMethod::build_parallel + FCI::construct_CI_matrix / DOCI::construct_CI_matrix
+ * (CIMethod.cpp:489-561, 749-888, 611-660) filling SparseMatrix_CRS_Sym.
+ * The device keeps the full symmetric matrix (both triangles, columns ascending);
+ * its upper triangle is CIFlow's CRS exactly (same 1e-14 drop threshold).
+ * The ham handle is borrowed and must outlive the CRS. ---- */
+int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, cigpu_crs **out);
+int cigpu_crs_destroy(cigpu_crs *crs);
+int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full);
+/* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
+ * SparseMatrix_CRS.h:107-111): row[dim+1], col[nnz_upper], val[nnz_upper]. Host buffers. */
+int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val);
+/* Full matrix as stored on the device: row[dim+1] (64-bit), col/val[nnz_full]. Host buffers. */
+int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *val);
+
+/* ---- matvec: replaces SparseMatrix_CRS_Sym::mvprod(const double*, double*)
+ * (SparseMatrix_CRS.cpp:700-723; virtual at SparseMatrix_CRS.h:126).
+ * Host buffers x, y of length dim; FP64 arithmetic (for a MIXED CRS the FP64
+ * product regenerates the elements on the fly). ---- */
+int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y);
+/* Device-buffer form on the given stream. dtype 0: FP64 x/y (FP64 matvec);
+ * dtype 1: FP32 x/y (FP32 values, FP32 accumulation; MIXED CRS only). */
+int cigpu_mvprod_device(cigpu_crs *crs, const void *x, void *y, int dtype, cigpu_stream stream);
+
+/* ---- eigensolver: replaces CIMethod::solve + SparseMatrix_CRS::arpackDiagonalize
+ * (CIMethod.cpp:241-264, SparseMatrix_CRS.cpp:360-481) for neig = 1. GPU-resident
+ * thick-restart Lanczos with full orthogonalisation (basis 42, like ARPACK's ncv).
+ * tol: FP64 residual norm target. max_matvec: limit (0 = 3*dim like iparam[2]).
+ * c0: optional start vector (host, dim; NULL = seeded random). c_out: optional
+ * host buffer (dim) for the normalised eigenvector. Unlike the reference, the
+ * CRS stays resident after the solve (the reference frees it, CIMethod.cpp:262). ---- */
+int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0, double *c_out,
+                cigpu_solve_info *info);
+
+/* ---- RDMs: replaces CIMethod::construct_density / CIDens::construct_density with
+ * DensFCI / DensDOCI (CIMethod.cpp:161-171, CIDens.cpp:323-334, 1073-1224, 1530-1631).
+ * c: host, dim (normalised state). Outputs (host, any may be NULL to skip):
+ *   rdm1 [2][L][L]         = CIDens::get_one_rdm(spin, i, j)
+ *   rdm2_aa, rdm2_bb [np][np], np = L(L-1)/2, pair(p<q) = p*L+q-(p+1)(p+2)/2
+ *                          = get_two_rdm(0|2, p, q, r, s) for p<q, r<s
+ *   rdm2_ab [L*L][L*L]     = get_two_rdm(1, p, q, r, s) at (p*L+q, r*L+s) ---- */
+int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa, double *rdm2_ab, double *rdm2_bb);
+
+/* ---- serving: continuous batching of independent solves (the served analogue of
+ * the set_ham -> solve loop of the orbital optimisers, SimulatedAnnealing.cpp:72-86,
+ * 130-134; CIMethod::set_ham CIMethod.cpp:117-126). Requests are admitted as
+ * device memory (the HBM budget) and slots free up; admitted requests run
+ * concurrently on separate streams; small ones are packed into batched launches. ---- */
+typedef struct {
+    int32_t L, nup, ndown;
+    int32_t method;      /* cigpu_method */
+    int32_t precision;   /* cigpu_precision */
+    int32_t want_rdm;    /* 1: also compute the 1-RDM */
+    double econst;
+    double tol;          /* FP64 residual target */
+    const double *h;     /* copied at submit */
+    const double *eri;   /* copied at submit */
+    const double *c0;    /* optional warm start (dim), copied at submit */
+} cigpu_request;
+
+typedef struct {
+    int32_t status;      /* CIGPU_OK, CIGPU_ENOCONV, CIGPU_ECANCELED, ... */
+    int32_t done;        /* 1 when finished */
+    int64_t dim;
+    cigpu_solve_info info;
+    double queued_s;     /* submit -> admission */
+    double latency_s;    /* submit -> completion */
+} cigpu_result;
+
+int cigpu_server_create(int device, size_t hbm_budget_bytes, int max_inflight, int max_queue,
+                        cigpu_server **out);
+/* Returns CIGPU_EAGAIN when the queue is full, CIGPU_ENOMEM when the request can
+ * never fit the budget, CIGPU_EINVAL on bad input. */
+int cigpu_server_submit(cigpu_server *srv, const cigpu_request *req, uint64_t *id);
+/* Waits up to wait_ms (0 = poll, <0 = until done) for request id. c_out (dim)
+ * and rdm1 ([2][L][L]) are optional host buffers filled when done. The request
+ * is released after a completed poll. */
+int cigpu_server_poll(cigpu_server *srv, uint64_t id, int wait_ms, cigpu_result *out, double *c_out,
+                      double *rdm1);
+int cigpu_server_cancel(cigpu_server *srv, uint64_t id);
+int cigpu_server_stats(cigpu_server *srv, int64_t *admitted, int64_t *completed, int64_t *inflight,
+                       size_t *hbm_in_use);
+int cigpu_server_destroy(cigpu_server *srv);
+
+/* Device memory a request of this shape needs (bytes), as used by admission. */
+int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CIGPU_H */

@@ -801,3 +801,63 @@ int orc_rdm_excitations(int method, int L, int nup, int ndown, const double *c, 
     pool_reduce(&P, L, rdm1, aa, ab, bb);
     return 0;
 }
+
+/* Rows [r0, r1) of the upper CRS, built with the same row generator as
+ * orc_build_upper (bounded samples for the CPU baseline). With col == NULL
+ * only counts[0..r1-r0) is filled; otherwise counts must hold the prefix
+ * offsets (r1-r0+1 entries, counts[0] = 0) and col/val are filled. Rows are
+ * spread over OpenMP threads. Returns the number of stored elements. */
+int64_t orc_build_rows(int method, int L, int nup, int ndown, const double *h, const double *eri, int64_t r0,
+                       int64_t r1, int64_t *counts, uint32_t *col, double *val) {
+    if (L < 1 || L > 62 || r1 < r0) return -1;
+    ham_t H = {L, nup, ndown, h, eri, (size_t)L, (size_t)L * L, (size_t)L * L * L};
+    int64_t *bt = make_binom_tab();
+    const int64_t Du = orc_binom(L, nup), Dd = (method == ORC_DOCI) ? 1 : orc_binom(L, ndown);
+    bits_t *us = enumerate_strings(L, nup, Du);
+    bits_t *ds = (method == ORC_DOCI) ? NULL : enumerate_strings(L, ndown, Dd);
+    const int64_t sa = (int64_t)nup * (L - nup), sb = (int64_t)ndown * (L - ndown);
+    const int64_t wmax = 2 + sa + sb + sa * sb + orc_binom(nup, 2) * orc_binom(L - nup, 2) +
+                         orc_binom(ndown, 2) * orc_binom(L - ndown, 2);
+    int64_t total = 0;
+#pragma omp parallel reduction(+ : total)
+    {
+        rowbuf_t r;
+        r.col = (uint32_t *)malloc((size_t)wmax * sizeof(uint32_t));
+        r.val = (double *)malloc((size_t)wmax * sizeof(double));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t rr = r0; rr < r1; ++rr) {
+            if (method == ORC_DOCI) {
+                doci_row(&H, bt, us[rr], (long)rr, &r);
+            } else {
+                const int64_t i = rr / Dd, k = rr % Dd;
+                fci_row(&H, bt, us[i], ds[k], (long)i, (long)k, (long)Dd, &r);
+            }
+            total += r.n;
+            if (col == NULL) {
+                counts[rr - r0] = r.n;
+            } else {
+                memcpy(col + counts[rr - r0], r.col, (size_t)r.n * sizeof(uint32_t));
+                memcpy(val + counts[rr - r0], r.val, (size_t)r.n * sizeof(double));
+            }
+        }
+        free(r.col);
+        free(r.val);
+    }
+    free(us);
+    free(ds);
+    free(bt);
+    return total;
+}
+
+/* The reference serial symmetric matvec restricted to rows [r0, r0+nrows) of
+ * the upper CRS (local row pointers), accumulating into full-length y. */
+void orc_sym_mvprod_rows(int64_t r0, int64_t nrows, const int64_t *row, const uint32_t *col, const double *val,
+                         const double *x, double *y) {
+    for (int64_t i = 0; i < nrows; ++i) {
+        const int64_t gi = r0 + i;
+        for (int64_t k = row[i]; k < row[i + 1]; ++k) {
+            y[gi] += val[k] * x[col[k]];
+            if ((uint32_t)gi != col[k]) y[col[k]] += val[k] * x[gi];
+        }
+    }
+}

@@ -51,6 +51,12 @@ int orc_rdm_pairs(int method, int L, int nup, int ndown, const double *c, double
 int orc_rdm_excitations(int method, int L, int nup, int ndown, const double *c, double *rdm1, double *aa,
                         double *ab, double *bb);
 
+/* Bounded samples for the CPU baseline: rows [r0, r1) of the upper CRS (see the .c file). */
+int64_t orc_build_rows(int method, int L, int nup, int ndown, const double *h, const double *eri, int64_t r0,
+                       int64_t r1, int64_t *counts, uint32_t *col, double *val);
+void orc_sym_mvprod_rows(int64_t r0, int64_t nrows, const int64_t *row, const uint32_t *col, const double *val,
+                         const double *x, double *y);
+
 #ifdef __cplusplus
 }
 #endif

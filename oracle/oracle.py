@@ -61,6 +61,9 @@ def port():
         lib.orc_build_upper.argtypes = [ctypes.c_int] * 4 + [_P] * 5
         lib.orc_sym_mvprod.argtypes = [ctypes.c_int64] + [_P] * 5
         lib.orc_sym_mvprod_omp.argtypes = [ctypes.c_int64] + [_P] * 5
+        lib.orc_build_rows.restype = ctypes.c_int64
+        lib.orc_build_rows.argtypes = [ctypes.c_int] * 4 + [_P, _P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P]
+        lib.orc_sym_mvprod_rows.argtypes = [ctypes.c_int64, ctypes.c_int64] + [_P] * 5
         for f in (lib.orc_rdm_pairs, lib.orc_rdm_excitations):
             f.restype = ctypes.c_int
             f.argtypes = [ctypes.c_int] * 4 + [_P] * 5
@@ -135,6 +138,25 @@ def build_upper(method: int, ints) -> UpperCRS:
     val = np.empty(row[-1], np.float64)
     lib.orc_build_upper(method, ints.L, ints.nup, ints.ndown, _ptr(h), _ptr(eri), _ptr(row), _ptr(col), _ptr(val))
     return UpperCRS(row, col, val)
+
+
+def build_rows(method: int, ints, r0: int, r1: int):
+    """Rows [r0, r1) of the upper CRS: (local row pointers, col, val)."""
+    lib = port()
+    h = np.ascontiguousarray(ints.h, dtype=np.float64)
+    eri = np.ascontiguousarray(ints.eri, dtype=np.float64)
+    cnt = np.zeros(r1 - r0 + 1, np.int64)
+    lib.orc_build_rows(method, ints.L, ints.nup, ints.ndown, _ptr(h), _ptr(eri), r0, r1, _ptr(cnt[1:]), None, None)
+    off = np.concatenate([[0], np.cumsum(cnt[1:])]).astype(np.int64)
+    col = np.empty(off[-1], np.uint32)
+    val = np.empty(off[-1], np.float64)
+    lib.orc_build_rows(method, ints.L, ints.nup, ints.ndown, _ptr(h), _ptr(eri), r0, r1, _ptr(off), _ptr(col),
+                       _ptr(val))
+    return off, col, val
+
+
+def sym_mvprod_rows(r0: int, off, col, val, x, y) -> None:
+    port().orc_sym_mvprod_rows(r0, len(off) - 1, _ptr(off), _ptr(col), _ptr(val), _ptr(x), _ptr(y))
 
 
 def sym_mvprod(m: UpperCRS, x: np.ndarray, threaded: bool = False) -> np.ndarray:

@@ -1,0 +1,68 @@
+"""CPU-side checks of the C ABI boundary: the library loads, exports every
+symbol include/cigpu.h declares, and rejects invalid arguments before touching
+a device. No compute call is made here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ciflow_gb300 import _abi as A
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "cigpu.h")).read()
+    return sorted(set(re.findall(r"\b(cigpu_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(A.LIB_PATH):
+        from ciflow_gb300 import build
+        build.build()
+    return A.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover include/cigpu.h exactly"
+
+
+def test_version_and_strerror(lib):
+    assert lib.cigpu_get_version() == 1
+    assert lib.cigpu_strerror(A.EINVAL) == b"invalid argument"
+    assert lib.cigpu_strerror(A.ENOCONV).startswith(b"eigensolver")
+
+
+def test_invalid_arguments_rejected_on_host(lib):
+    out = ctypes.c_void_p()
+    h = np.eye(4)
+    e = np.zeros((4,) * 4)
+    assert lib.cigpu_ham_create(0, 1, 1, 0.0, A.ptr(h), A.ptr(e), ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_ham_create(4, 5, 1, 0.0, A.ptr(h), A.ptr(e), ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_ham_create(70, 1, 1, 0.0, A.ptr(h), A.ptr(e), ctypes.byref(out)) == A.EINVAL
+    bad = h.copy(); bad[0, 1] = 1.0
+    assert lib.cigpu_ham_create(4, 1, 1, 0.0, A.ptr(bad), A.ptr(e), ctypes.byref(out)) == A.EINVAL
+    nan = e.copy(); nan[0, 0, 0, 0] = np.nan
+    assert lib.cigpu_ham_create(4, 1, 1, 0.0, A.ptr(h), A.ptr(nan), ctypes.byref(out)) == A.EINVAL
+    asym = e.copy(); asym[0, 1, 2, 3] = 0.5
+    assert lib.cigpu_ham_create(4, 1, 1, 0.0, A.ptr(h), A.ptr(asym), ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_build(None, 0, 0, None, ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_solve(None, 1e-8, 0, None, None, None) == A.EINVAL
+
+
+def test_estimate_bytes(lib):
+    b = ctypes.c_size_t()
+    assert lib.cigpu_estimate_bytes(12, 6, 6, A.FCI, A.FP64, ctypes.byref(b)) == A.OK
+    # full FP64 CRS of the L=12 FCI space alone is 853,776 x 1,819 x 12 bytes
+    assert b.value > 853776 * 1819 * 12
+    b32 = ctypes.c_size_t()
+    lib.cigpu_estimate_bytes(12, 6, 6, A.FCI, A.MIXED, ctypes.byref(b32))
+    assert b32.value < b.value
+    assert lib.cigpu_estimate_bytes(12, 6, 6, 7, A.FP64, ctypes.byref(b)) == A.EINVAL

@@ -1,0 +1,113 @@
+"""GPU matvec and eigensolver parity.
+
+mvprod must equal the reference SparseMatrix_CRS_Sym::mvprod (restated by the
+oracle) to FP64 round-off; E0 must match the reference ARPACK energy to 1e-8 Eh
+(plain FP64) and to 1e-6 Eh (mixed), including the DOCI known answer
+-15.225362047972723 (reference tests/src/TestDOCI.cpp:31).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.ciflow import DOCI, FCI, Hamiltonian
+from tests.helpers import beh2_integrals, integrals, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def build(cls, ints, precision=A.FP64):
+    return cls(Hamiltonian.from_integrals(ints), precision=precision)
+
+
+@pytest.mark.parametrize("name", ["c0", "c4"])
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_mvprod_matches_reference_matvec(name, precision):
+    ints = integrals(name)
+    ref = O.build_upper(O.FCI, ints)
+    m = build(FCI, ints, precision).get_mat()
+    x = np.random.default_rng(7).standard_normal(m.n)
+    y_ref = O.sym_mvprod(ref, x, threaded=True)
+    y = m.mvprod(x)
+    scale = np.abs(y_ref).max()
+    # FP64 product (regenerated elements for the mixed CRS): summation order only
+    assert np.abs(y - y_ref).max() <= 1e-12 * scale
+
+
+def test_fp32_device_matvec():
+    torch = pytest.importorskip("torch")
+    ints = integrals("c0")
+    ref = O.build_upper(O.FCI, ints)
+    m = build(FCI, ints, A.MIXED).get_mat()
+    x = np.random.default_rng(3).standard_normal(m.n)
+    y_ref = O.sym_mvprod(ref, x)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    m.mvprod_device(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy().astype(np.float64)
+    # FP32 values and FP32 accumulation over ~361 terms per row
+    assert np.abs(y - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
+
+
+def test_doci_known_answer():
+    ints, meta, _ = beh2_integrals()
+    cim = build(DOCI, ints)
+    cim.solve(tol=1e-10)
+    # reference tests/src/TestDOCI.cpp:31 (BOOST_CHECK_CLOSE 1e-10 percent)
+    assert abs(cim.get_ci_energy() - (-15.225362047972723)) <= 1e-12 * 15.3 + 1e-11
+    assert cim.info["residual"] <= 1e-10
+
+
+@pytest.mark.parametrize("tag,cls", [("doci", DOCI), ("fci", FCI)])
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_beh2_energy(tag, cls, precision):
+    ints, meta, _ = beh2_integrals()
+    cim = build(cls, ints, precision)
+    cim.solve(tol=1e-8)
+    tol = 1e-8 if precision == A.FP64 else 1e-6
+    assert abs(cim.get_ci_energy() - meta[tag]["e0"]) <= tol
+
+
+@pytest.mark.parametrize("name", ["c0", "c4", "c1", "c2"])
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_config_energy(name, precision):
+    meta, _ = load_golden(name)
+    ints = integrals(name)
+    cls = DOCI if meta["config"]["method"] == "DOCI" else FCI
+    cim = build(cls, ints, precision)
+    cim.solve(tol=1e-6 if name in ("c1", "c2") else 1e-8)
+    err = abs(cim.get_ci_energy() - meta["e0"])
+    assert err <= (1e-8 if precision == A.FP64 else 1e-6), (err, cim.info)
+    c = cim.get_eigvec()
+    assert abs(np.linalg.norm(c) - 1) < 1e-10
+
+
+def test_residual_is_true_fp64_residual():
+    ints = integrals("c0")
+    ref = O.build_upper(O.FCI, ints)
+    cim = build(FCI, ints, A.MIXED)
+    cim.solve(tol=1e-9)
+    c = cim.get_eigvec()
+    e = cim.get_ci_energy() - ints.econst
+    r = O.sym_mvprod(ref, c) - e * c
+    assert np.linalg.norm(r) <= 2e-9
+    assert cim.info["matvecs_fp32"] > 0
+
+
+def test_warm_start_converges_faster():
+    ints = integrals("c4")
+    cim = build(FCI, ints)
+    cim.solve(tol=1e-8)
+    n_cold = cim.info["matvecs_fp64"]
+    c = cim.get_eigvec()
+    cim.solve(tol=1e-8, c0=c)
+    assert cim.info["matvecs_fp64"] < n_cold
+
+
+def test_matvec_limit_reports_no_convergence():
+    ints = integrals("c4")
+    cim = build(FCI, ints)
+    cim.solve(tol=1e-12, max_matvec=5)
+    assert cim.info["status"] == A.ENOCONV
+    assert not cim.info["converged"]
