@@ -585,25 +585,35 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         }
         mv32 += lz.matvecs;
         const int q = lz.j;  // basis [c, v_1 .. v_{q-1}] (v_q is the unused next direction)
-        // projected matrix: FP64 coupling of c (w = H c), FP32-accurate Lanczos block elsewhere
-        ops.dots(lz.V.p, n, q, ref.w.p, n, 0);
-        const double *hc = ops.fetch(q);
+        // Projected matrix over [c, v_1 .. v_{q-1}]. The v_i are orthogonal to fp32(c),
+        // not to c: with eta_i = c.v_i, the vectors v_i - eta_i c span the same space
+        // and couple to c through r.v_i exactly (r = H c - E c, FP64), so the FP32
+        // rounding of c does not leak into the coupling column. The v-v block is the
+        // FP32 Lanczos projection (its error only scales the small correction).
+        ops.dots(lz.V.p, n, q, ref.r.p, n, 0);
+        ops.dots(lz.V.p, n, q, c_dev, n, q);
+        const double *hd = ops.fetch(2 * q);
+        std::vector<double> hr(hd, hd + q), eta(hd + q, hd + 2 * q);
         std::vector<double> G((size_t)q * q, 0.0);
         G[0] = E;
-        for (int i = 1; i < q; ++i) G[i] = G[(size_t)i * q] = hc[i];
+        for (int i = 1; i < q; ++i) G[i] = G[(size_t)i * q] = hr[i];
         for (int i = 1; i < q; ++i)
             for (int k = 1; k < q; ++k) G[(size_t)i * q + k] = lz.t(i, k);
         std::vector<double> w, z;
         small_eigh(q, G, w, z);
-        // c <- y0 c + sum_i y_i v_i  (FP64)
+        // c <- (y0 - sum_i y_i eta_i) c + sum_i y_i v_i  (FP64)
         std::vector<double> y(q);
-        for (int i = 0; i < q; ++i) y[i] = z[(size_t)i * q];
+        double a0 = z[0];
+        for (int i = 1; i < q; ++i) {
+            y[i] = z[(size_t)i * q];
+            a0 -= y[i] * eta[i];
+        }
         if (q > 1) {
             y[0] = 0;
             CIGPU_CUDA(cudaMemcpyAsync(lz.Yd.p, y.data(), sizeof(double) * q, cudaMemcpyHostToDevice, s));
             k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(lz.V.p, n, q, lz.Yd.p, 1, ref.t.p, n, n);
             count_launch();
-            k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, z[0], c_dev, n);
+            k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
             count_launch();
             CIGPU_CUDA(cudaGetLastError());
             CIGPU_CUDA(cudaStreamSynchronize(s));

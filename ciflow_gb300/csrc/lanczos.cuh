@@ -18,7 +18,7 @@ struct SolveOptions {
     int keep = 14;              // Ritz vectors kept at a thick restart
     int corr_steps = 24;        // FP32 Krylov steps per FP64 correction (mixed)
     int max_corrections = 12;   // FP64 correction cycles (mixed)
-    double mixed_rel = 1e-5;    // FP32 phase target, relative to max(1, |E|) (mixed)
+    double mixed_rel = 1e-6;    // FP32 phase target, relative to max(1, |E|) (mixed)
     uint64_t seed = 12345;      // random start vector
 };
 

@@ -1,0 +1,92 @@
+"""Kernel microbenchmark: launch one hot kernel of the CI path a few times on a
+named configuration (used for profiler captures and roofline timing).
+
+    python -m ciflow_gb300.kernel_bench --config c4 --kernel spmv_f32 --reps 3
+
+Kernels: spmv_f32, spmv_f64 (CRS matvec), build_f64, build_f32 (CRS build:
+count + fill passes), matvec_regen (FP64 product with regenerated elements).
+Prints one JSON line with the CUDA-event time per launch and the algorithmic
+bytes of the matvec.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+
+import numpy as np
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="c4")
+    ap.add_argument("--kernel", default="spmv_f32",
+                    choices=["spmv_f32", "spmv_f64", "build_f64", "build_f32", "matvec_regen"])
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=1)
+    args = ap.parse_args()
+
+    import torch
+
+    from . import _abi as A
+    from .synthetic import CONFIGS, config_integrals
+
+    lib = A.lib()
+    cfg = CONFIGS[args.config]
+    method = A.DOCI if cfg["method"] == "DOCI" else A.FCI
+    ints = config_integrals(args.config)
+    h = np.ascontiguousarray(ints.h)
+    eri = np.ascontiguousarray(ints.eri)
+    ham = ctypes.c_void_p()
+    A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri), ctypes.byref(ham)))
+    stream = torch.cuda.Stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    prec = A.MIXED if args.kernel in ("spmv_f32", "build_f32", "matvec_regen") else A.FP64
+
+    def build():
+        crs = ctypes.c_void_p()
+        A.check(lib.cigpu_build(ham, method, prec, sh, ctypes.byref(crs)))
+        return crs
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"config": args.config, "kernel": args.kernel, "reps": args.reps}
+    if args.kernel.startswith("build"):
+        for _ in range(args.warmup):
+            lib.cigpu_crs_destroy(build())
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.reps):
+            lib.cigpu_crs_destroy(build())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["ms_per_build"] = e0.elapsed_time(e1) / args.reps
+    else:
+        crs = build()
+        dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        lib.cigpu_crs_dims(crs, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf))
+        f32 = args.kernel == "spmv_f32"
+        dt = torch.float32 if f32 else torch.float64
+        x = torch.randn(dim.value, device="cuda", dtype=dt)
+        y = torch.empty_like(x)
+        code = 1 if f32 else 0
+        for _ in range(args.warmup):
+            A.check(lib.cigpu_mvprod_device(crs, A.ptr(x), A.ptr(y), code, sh))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.reps):
+            lib.cigpu_mvprod_device(crs, A.ptr(x), A.ptr(y), code, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / args.reps
+        sv = 4 if f32 else 8
+        n = dim.value
+        alg = nf.value * (sv + 4) + 8 * (n + 1) + 2 * n * sv if args.kernel != "matvec_regen" else 8 * (n + 1) + 16 * n
+        out.update({"dim": n, "nnz_full": nf.value, "ms_per_launch": t, "algorithmic_bytes": alg,
+                    "achieved_gbs": alg / (t / 1000) / 1e9})
+        lib.cigpu_crs_destroy(crs)
+    lib.cigpu_ham_destroy(ham)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
