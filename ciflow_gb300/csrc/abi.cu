@@ -71,7 +71,7 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
         W = 1 + sa + sb + sa * sb + binom64(nup, 2) * binom64(L - nup, 2) + binom64(ndown, 2) * binom64(L - ndown, 2);
     }
     const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
-    size_t b = (size_t)dim * W * (4 + vbytes);    // col + values
+    size_t b = (size_t)dim * W * 12;              // col + values (FP64, or FP32 hi + lo)
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
     b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
     b += (size_t)dim * 8 * 5;                    // c, refinement vectors
@@ -140,19 +140,23 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
     if (mode == kFill64)
         c.val64.alloc(c.nnz_full);
-    else
+    else {
         c.val32.alloc(c.nnz_full);
+        c.val32lo.alloc(c.nnz_full);
+    }
     if (c.method == CIGPU_FCI) {
         c.fp.row_ptr = c.row_ptr.p;
         c.fp.col = c.col.p;
         c.fp.val64 = c.val64.p;
         c.fp.val32 = c.val32.p;
+        c.fp.val32lo = c.val32lo.p;
         fci_launch(mode, c.fp, s);
     } else {
         c.dp.row_ptr = c.row_ptr.p;
         c.dp.col = c.col.p;
         c.dp.val64 = c.val64.p;
         c.dp.val32 = c.val32.p;
+        c.dp.val32lo = c.val32lo.p;
         doci_launch(mode, c.dp, s);
     }
     CIGPU_CUDA(cudaStreamSynchronize(s));
@@ -164,7 +168,12 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         spmv_f64(c.dim, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
         return;
     }
-    // MIXED CRS stores FP32 values: regenerate the FP64 elements on the fly.
+    if (c.val32lo.p) {
+        // MIXED CRS: FP64 product with values hi + lo (|v - hi - lo| <= 2^-48 |v|)
+        spmv_hilo(c.dim, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
+        return;
+    }
+    // without the remainder array: regenerate the FP64 elements on the fly
     if (c.method == CIGPU_FCI) {
         FciParams p = c.fp;
         p.x = x;

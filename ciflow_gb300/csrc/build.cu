@@ -192,10 +192,13 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                 if (keep) {
                     const int64_t pos = base + running + __popc(mask & ((1u << lane) - 1u));
                     p.col[pos] = col;
-                    if (MODE == kFill64)
+                    if (MODE == kFill64) {
                         p.val64[pos] = v;
-                    else
-                        p.val32[pos] = (float)v;
+                    } else {
+                        const float hi = (float)v;
+                        p.val32[pos] = hi;
+                        p.val32lo[pos] = (float)(v - (double)hi);
+                    }
                 }
             } else {
                 if (keep) acc += v * __ldg(p.x + col);
@@ -357,10 +360,13 @@ __global__ void __launch_bounds__(kDociThreads) k_doci_rows(DociParams p) {
             if (keep) {
                 const int64_t pos = base + running + __popc(mask & ((1u << lane) - 1u));
                 p.col[pos] = col;
-                if (MODE == kFill64)
+                if (MODE == kFill64) {
                     p.val64[pos] = v;
-                else
-                    p.val32[pos] = (float)v;
+                } else {
+                    const float hi = (float)v;
+                    p.val32[pos] = hi;
+                    p.val32lo[pos] = (float)(v - (double)hi);
+                }
             }
             running += __popc(mask);
         }

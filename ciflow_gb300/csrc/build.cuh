@@ -25,6 +25,7 @@ struct FciParams {
     uint32_t *col;
     double *val64;
     float *val32;
+    float *val32lo;  // v - (double)hi, rounded to FP32 (FP32 fill only)
     // MATVEC
     const double *x;
     double *y;
@@ -44,6 +45,7 @@ struct DociParams {
     uint32_t *col;
     double *val64;
     float *val32;
+    float *val32lo;
     const double *x;
     double *y;
 };

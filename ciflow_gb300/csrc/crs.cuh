@@ -22,6 +22,7 @@ struct cigpu_crs {
     cigpu::DevBuf<uint32_t> col, upper_off;
     cigpu::DevBuf<double> val64;
     cigpu::DevBuf<float> val32;
+    cigpu::DevBuf<float> val32lo;  // MIXED: FP32 rounding remainder of each value
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};
     double build_seconds = 0;

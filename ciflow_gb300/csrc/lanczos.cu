@@ -81,9 +81,9 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int G, int
 }
 
 // w -= sum_{i<nvec} V_i coef_i (FP64 arithmetic); partial ||w||^2 per block when nrm != nullptr.
-template <typename VT>
+template <typename VT, typename WT>
 __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
-                                                        const double *__restrict__ coef, VT *__restrict__ w, int64_t n,
+                                                        const double *__restrict__ coef, WT *__restrict__ w, int64_t n,
                                                         double *__restrict__ nrm) {
     __shared__ double c[kMaxBasis + 1];
     for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = coef[i];
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         double x = (double)w[r];
         for (int i = 0; i < nvec; ++i) x -= (double)V[(int64_t)i * ld + r] * c[i];
-        const VT xv = (VT)x;
+        const WT xv = (WT)x;
         w[r] = xv;
         acc += (double)xv * (double)xv;
     }
@@ -107,6 +107,105 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
             nrm[blockIdx.x] = s;
         }
     }
+}
+
+// out = (OT)(t / sqrt(nrm2))
+template <typename IT, typename OT>
+__global__ void k_scale_to(const IT *__restrict__ t, int64_t n, const double *__restrict__ nrm2, OT *__restrict__ out) {
+    const double inv = 1.0 / sqrt(*nrm2);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        out[r] = (OT)((double)t[r] * inv);
+}
+
+// Davidson residual of u = a0 c + sum_i y_i v_i with H u ~ a0 w + sum_i y_i (H v_i):
+//   ru = a0 (w - theta c) + sum_i y_i (HV_i - theta V_i)      (FP64 arithmetic)
+//   t  = ru / (theta - H_ii)   (diagonal preconditioner, guarded)
+// and partial ||ru||^2.
+__global__ void __launch_bounds__(kVecThreads) k_dav_residual(const double *__restrict__ w, const double *__restrict__ c,
+                                                              const float *__restrict__ V, const float *__restrict__ HV,
+                                                              int64_t ld, int k, const double *__restrict__ y,
+                                                              double a0, double theta, const double *__restrict__ diag,
+                                                              double *__restrict__ t, int64_t n,
+                                                              double *__restrict__ nrm) {
+    __shared__ double ys[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = y[i];
+    __syncthreads();
+    double acc = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double ru = a0 * (w[r] - theta * c[r]);
+        for (int i = 0; i < k; ++i) {
+            const int64_t o = (int64_t)i * ld + r;
+            ru += ys[i] * ((double)HV[o] - theta * (double)V[o]);
+        }
+        acc += ru * ru;
+        double d = theta - diag[r];
+        if (fabs(d) < 1e-2) d = d < 0 ? -1e-2 : 1e-2;
+        t[r] = ru / d;
+    }
+    __shared__ double sh[kVecThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int q = 0; q < kVecThreads / 32; ++q) s += sh[q];
+        nrm[blockIdx.x] = s;
+    }
+}
+
+// Block-wise (min value, index) of diag, then a single-block reduction.
+__global__ void k_argmin_partial(const double *__restrict__ d, int64_t n, double *__restrict__ pv,
+                                 int64_t *__restrict__ pi) {
+    double best = 1e308;
+    int64_t bi = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        if (d[r] < best || (d[r] == best && r < bi)) {
+            best = d[r];
+            bi = r;
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob < best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    __shared__ double sv[kVecThreads / 32];
+    __shared__ int64_t si[kVecThreads / 32];
+    if ((threadIdx.x & 31) == 0) {
+        sv[threadIdx.x >> 5] = best;
+        si[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < kVecThreads / 32; ++q)
+            if (sv[q] < best || (sv[q] == best && si[q] < bi)) {
+                best = sv[q];
+                bi = si[q];
+            }
+        pv[blockIdx.x] = best;
+        pi[blockIdx.x] = bi;
+    }
+}
+
+// v = e_{argmin}: zero everywhere except 1 at the lowest diagonal element.
+__global__ void k_unit_at_argmin(const double *__restrict__ pv, const int64_t *__restrict__ pi, int G,
+                                 double *__restrict__ v, int64_t n) {
+    __shared__ int64_t at;
+    if (threadIdx.x == 0) {
+        double best = 1e308;
+        int64_t bi = 0;
+        for (int b = 0; b < G; ++b)
+            if (pv[b] < best || (pv[b] == best && pi[b] < bi)) {
+                best = pv[b];
+                bi = pi[b];
+            }
+        at = bi;
+    }
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        v[r] = (r == at) ? 1.0 : 0.0;
 }
 
 template <typename VT>
@@ -220,9 +319,9 @@ struct VecOps {
         CIGPU_CUDA(cudaGetLastError());
         count_launch(2);
     }
-    template <typename VT>
-    void update(const VT *V, int64_t ld, int nvec, int coef_at, VT *w, int64_t n, int nrm_at) {
-        k_update<VT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n, nrm_at >= 0 ? partial.p : nullptr);
+    template <typename VT, typename WT>
+    void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at) {
+        k_update<VT, WT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n, nrm_at >= 0 ? partial.p : nullptr);
         count_launch();
         if (nrm_at >= 0) {
             k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p + nrm_at);
@@ -532,104 +631,143 @@ int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool
 }
 
 int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info) {
+    // Anchored mixed-precision Davidson.
+    //   anchor c (FP64) with w = H c from an FP64 matvec, E = c.w, r = w - E c (exact);
+    //   corrections v_1..v_k stored in FP32 with H v_i from the FP32 CRS matvec;
+    //   projected matrix over [c, v_i - eta_i c] (eta_i = c.v_i):
+    //       G = [[E, r.v_j], [r.v_i, v_i.H32 v_j]]   (FP64 accumulation)
+    //   new direction t = ru / (theta - H_ii) (diagonal preconditioner) where ru is the
+    //   Davidson residual assembled from FP32 vectors. The FP32 error in ru scales with
+    //   the correction size |y_v|, so once ru approaches eps32 |H| |y_v| (or the basis is
+    //   full) the correction is folded into the anchor and the residual is recomputed
+    //   exactly with an FP64 matvec (residual-correction restart).
     const int64_t n = P.n;
     const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
-    const int m = (int)std::min<int64_t>(std::min(o.basis, kMaxBasis), std::max<int64_t>(n, 1));
-    const int keep = std::max(1, std::min({o.keep, m - 1, kMaxKeep}));
     cudaStream_t s = P.stream;
+    if (n <= 2 || !P.mv32 || !P.diag) {
+        if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
+        return solve_fp64(P, o, c_dev, true, info);
+    }
     VecOps ops(s);
     Refine ref(n, s, ops);
-    if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
-    if (n <= 2 || !P.mv32) return solve_fp64(P, o, c_dev, true, info);
-
-    // Phase 1: FP32 thick-restart Lanczos to the FP32 accuracy floor.
-    int64_t mv32 = 0, mv64 = 0;
-    int restarts = 0, corrections = 0;
-    double gap = 0;
-    {
-        TRLanczos<float> lz(n, m, keep, s, ops);
-        lz.mv = [&](const float *x, float *y, cudaStream_t st) { P.mv32(x, y, st); };
-        DevBuf<float> v0(n);
-        dev_convert(c_dev, v0.p, n, s);
-        lz.start(v0.p);
-        // FP32 vectors stall near a residual of ~1e-6 |E|; stop above that floor and
-        // let the FP64 corrections finish.
-        lz.run(o.tol, o.mixed_rel, budget);
-        lz.ritz_vector(c_dev);
-        mv32 += lz.matvecs;
-        restarts = lz.restarts;
-        gap = lz.theta1 - lz.theta0;
+    const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 1), n - 1);
+    if (!have_start) {
+        DevBuf<double> pv(ops.G);
+        DevBuf<int64_t> pi(ops.G);
+        k_argmin_partial<<<ops.G, kVecThreads, 0, s>>>(P.diag, n, pv.p, pi.p);
+        k_unit_at_argmin<<<ops.G, kVecThreads, 0, s>>>(pv.p, pi.p, ops.G, c_dev, n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch(2);
+        CIGPU_CUDA(cudaStreamSynchronize(s));
     }
-    // Phase 2: FP64 Rayleigh quotient / residual and correction cycles.
+    DevBuf<float> V((size_t)mmax * n), HV((size_t)mmax * n);
+    DevBuf<double> yd(kMaxBasis + 1);
+    std::vector<double> A((size_t)kMaxBasis * kMaxBasis, 0.0), eta(kMaxBasis, 0.0), bvec(kMaxBasis, 0.0);
+    int64_t mv32 = 0, mv64 = 0;
+    int collapses = 0;
     auto er = ref.eval(P, c_dev);
     ++mv64;
-    const int p = std::max(2, std::min(o.corr_steps, m - 1));
-    while (er.second > o.tol && corrections < o.max_corrections && mv32 + mv64 < budget) {
-        ++corrections;
-        const double E = er.first;
-        // t = preconditioned residual, orthogonalised against c in FP64
-        k_precond<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, ref.t.p, n);
-        count_launch();
-        ops.dots(c_dev, n, 1, ref.t.p, n, 0);
-        ops.update(c_dev, n, 1, 0, ref.t.p, n, 1);
-        ops.scale(ref.t.p, n, 1);
-        // FP32 Krylov space from t with c as a locked first vector
-        TRLanczos<float> lz(n, p + 1, 1, s, ops);
-        lz.mv = [&](const float *x, float *y, cudaStream_t st) { P.mv32(x, y, st); };
-        dev_convert(c_dev, lz.vec(0), n, s);
-        dev_convert(ref.t.p, lz.vec(1), n, s);
-        lz.j = 1;
-        for (int k = 1; k < p && lz.matvecs + mv32 + mv64 < budget; ++k) {
-            const double beta = lz.step();
-            if (beta <= 1e-10) break;
-        }
-        mv32 += lz.matvecs;
-        const int q = lz.j;  // basis [c, v_1 .. v_{q-1}] (v_q is the unused next direction)
-        // Projected matrix over [c, v_1 .. v_{q-1}]. The v_i are orthogonal to fp32(c),
-        // not to c: with eta_i = c.v_i, the vectors v_i - eta_i c span the same space
-        // and couple to c through r.v_i exactly (r = H c - E c, FP64), so the FP32
-        // rounding of c does not leak into the coupling column. The v-v block is the
-        // FP32 Lanczos projection (its error only scales the small correction).
-        ops.dots(lz.V.p, n, q, ref.r.p, n, 0);
-        ops.dots(lz.V.p, n, q, c_dev, n, q);
-        const double *hd = ops.fetch(2 * q);
-        std::vector<double> hr(hd, hd + q), eta(hd + q, hd + 2 * q);
-        std::vector<double> G((size_t)q * q, 0.0);
-        G[0] = E;
-        for (int i = 1; i < q; ++i) G[i] = G[(size_t)i * q] = hr[i];
-        for (int i = 1; i < q; ++i)
-            for (int k = 1; k < q; ++k) G[(size_t)i * q + k] = lz.t(i, k);
-        std::vector<double> w, z;
-        small_eigh(q, G, w, z);
-        // c <- (y0 - sum_i y_i eta_i) c + sum_i y_i v_i  (FP64)
-        std::vector<double> y(q);
-        double a0 = z[0];
-        for (int i = 1; i < q; ++i) {
-            y[i] = z[(size_t)i * q];
-            a0 -= y[i] * eta[i];
-        }
-        if (q > 1) {
-            y[0] = 0;
-            CIGPU_CUDA(cudaMemcpyAsync(lz.Yd.p, y.data(), sizeof(double) * q, cudaMemcpyHostToDevice, s));
-            k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(lz.V.p, n, q, lz.Yd.p, 1, ref.t.p, n, n);
+    double E = er.first, rho = er.second, gap = 0;
+    double last_rho = 1e300;
+    int k = 0;
+    double theta = E, a0 = 1.0;
+    std::vector<double> y(kMaxBasis + 1, 0.0);
+    bool fresh = true;  // next direction comes from the exact residual r
+    bool force_fold = false;
+    while (rho > o.tol && mv32 + mv64 < budget) {
+        // preconditioned direction
+        if (fresh) {
+            k_precond<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, ref.t.p, n);
             count_launch();
-            k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
-            count_launch();
+        } else {
+            CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+            k_dav_residual<<<ops.G, kVecThreads, 0, s>>>(ref.w.p, c_dev, V.p, HV.p, n, k, yd.p, a0, theta, P.diag,
+                                                          ref.t.p, n, ops.partial.p);
+            k_reduce_partials<<<1, 32, 0, s>>>(ops.partial.p, ops.G, 1, ops.out.p);
+            count_launch(2);
             CIGPU_CUDA(cudaGetLastError());
-            CIGPU_CUDA(cudaStreamSynchronize(s));
+            const double rho_u = std::sqrt(ops.fetch(1)[0]);
+            double yv = 0;
+            for (int i = 1; i <= k; ++i) yv += y[i] * y[i];
+            yv = std::sqrt(yv);
+            const double floor = 30.0 * 6e-8 * std::max(1.0, std::fabs(theta)) * yv;
+            if (rho_u <= std::max(0.5 * o.tol, floor) || k >= mmax || force_fold) {
+                force_fold = false;
+                // fold the correction into the anchor: c <- a0 c + sum_i y_i v_i (FP64)
+                CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+                k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(V.p, n, k, yd.p, 1, ref.t.p, n, n);
+                k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
+                CIGPU_CUDA(cudaGetLastError());
+                count_launch(2);
+                er = ref.eval(P, c_dev);
+                ++mv64;
+                ++collapses;
+                E = er.first;
+                rho = er.second;
+                k = 0;
+                fresh = true;
+                if (rho > 0.7 * last_rho && collapses > 3) break;  // no progress between collapses
+                last_rho = rho;
+                continue;
+            }
         }
-        er = ref.eval(P, c_dev);
-        ++mv64;
+        // orthonormalise t against c (FP64) and the FP32 corrections, twice
+        for (int pass = 0; pass < 2; ++pass) {
+            ops.dots(c_dev, n, 1, ref.t.p, n, 0);
+            ops.update(c_dev, n, 1, 0, ref.t.p, n, (k == 0 && pass == 1) ? 1 : -1);
+            if (k > 0) {
+                ops.dots(V.p, n, k, ref.t.p, n, 2);
+                ops.update(V.p, n, k, 2, ref.t.p, n, pass == 1 ? 1 : -1);
+            }
+        }
+        const double tn = std::sqrt(ops.fetch(2)[1]);
+        if (!(tn > 1e-14)) {
+            // the search space is invariant: nothing new to add
+            if (k == 0) break;
+            force_fold = true;  // fold the current correction on the next pass
+            continue;
+        }
+        k_scale_to<double, float><<<ops.G, kVecThreads, 0, s>>>(ref.t.p, n, ops.out.p + 1, V.p + (size_t)k * n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+        P.mv32(V.p + (size_t)k * n, HV.p + (size_t)k * n, s);
+        ++mv32;
+        // new column of the projection and the couplings of v_k to the anchor
+        ops.dots(V.p, n, k + 1, HV.p + (size_t)k * n, n, 0);
+        ops.dots(V.p + (size_t)k * n, n, 1, c_dev, n, k + 1);
+        ops.dots(V.p + (size_t)k * n, n, 1, ref.r.p, n, k + 2);
+        const double *h = ops.fetch(k + 3);
+        for (int i = 0; i <= k; ++i) {
+            A[(size_t)i * kMaxBasis + k] = h[i];
+            A[(size_t)k * kMaxBasis + i] = h[i];
+        }
+        eta[k] = h[k + 1];
+        bvec[k] = h[k + 2];
+        ++k;
+        // Rayleigh-Ritz over [c, v_1..v_k]
+        const int q = k + 1;
+        std::vector<double> G((size_t)q * q, 0.0), wv, zv;
+        G[0] = E;
+        for (int i = 0; i < k; ++i) G[(size_t)(i + 1)] = G[(size_t)(i + 1) * q] = bvec[i];
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) G[(size_t)(i + 1) * q + (j + 1)] = A[(size_t)i * kMaxBasis + j];
+        small_eigh(q, G, wv, zv);
+        theta = wv[0];
+        gap = q > 1 ? wv[1] - wv[0] : gap;
+        for (int i = 0; i < q; ++i) y[i] = zv[(size_t)i * q];
+        a0 = y[0];
+        for (int i = 1; i <= k; ++i) a0 -= y[i] * eta[i - 1];
+        fresh = false;
     }
-    info.e0 = er.first;
-    info.residual = er.second;
+    info.e0 = E;
+    info.residual = rho;
     info.gap = gap;
-    info.error_bound = gap > 0 ? er.second * er.second / gap : er.second;
+    info.error_bound = gap > 0 ? rho * rho / gap : rho;
     info.matvecs_fp64 = mv64;
     info.matvecs_fp32 = mv32;
-    info.restarts = restarts;
-    info.corrections = corrections;
-    info.converged = er.second <= o.tol;
+    info.restarts = 0;
+    info.corrections = collapses;
+    info.converged = rho <= o.tol;
     return info.converged ? CIGPU_OK : CIGPU_ENOCONV;
 }
 

@@ -18,7 +18,7 @@ struct SolveOptions {
     int keep = 14;              // Ritz vectors kept at a thick restart
     int corr_steps = 24;        // FP32 Krylov steps per FP64 correction (mixed)
     int max_corrections = 12;   // FP64 correction cycles (mixed)
-    double mixed_rel = 1e-6;    // FP32 phase target, relative to max(1, |E|) (mixed)
+    int dav_basis = 30;         // FP32 correction vectors before folding into the anchor (mixed)
     uint64_t seed = 12345;      // random start vector
 };
 
@@ -33,8 +33,8 @@ struct SolveProblem {
 // Plain FP64 thick-restart Lanczos. c_dev: [n] output (and optional start when
 // `have_start`). Returns CIGPU_OK or CIGPU_ENOCONV; fills info (without Econst).
 int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info);
-// Mixed: FP32 thick-restart Lanczos, then FP64 Rayleigh quotient / residual with
-// preconditioned residual-correction cycles in an FP32 Krylov space.
+// Mixed: anchored Davidson -- FP32 correction vectors and FP32 CRS matvecs, FP64
+// projected problem and diagonal preconditioner, FP64 residual-correction restarts.
 int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info);
 
 // Symmetric eigen-decomposition of a small dense matrix (cyclic Jacobi):

@@ -1,13 +1,568 @@
-// RDM construction on the device (filled in below).
+// 1- and 2-RDMs of a CI vector on the device.
+//
+// Replaces CIDens::construct_density with DensFCI / DensDOCI (CIDens.cpp:323-334,
+// 1073-1224, 1530-1631). The reference loops over all determinant pairs and
+// classifies each by popcount (O(dim^2)); here only connected pairs contribute and
+// every sum has a fixed order (no atomics, bit-reproducible).
+//
+// FCI. Write C[Ia][Ib] for the CI vector. Every contribution of fill_density_matrix
+// (CIDens.cpp:676-881) with a pair (I, J), I <= J in row order, is one of
+//   * alpha pair (Ia, Ja >= Ia, same Ib): diagonal, single or alpha-alpha double.
+//     Its weight only needs the string-pair densities
+//        Da0[Ia,Ja]    = sum_b C[Ia][b] C[Ja][b]
+//        Daz[Ia,Ja][z] = sum_b C[Ia][b] C[Ja][b] n_z(b)    (beta spectators z)
+//   * beta pair (Ib, Jb > Ib, same Ia): the mirror image with C transposed;
+//   * alpha-beta double (Ia -> Ja = Ia - ar + ac, ac > ar; Ib -> Jb = Ib - br + bc):
+//        Gamma_ab[(ar,br),(ac,bc)] += s_a s_b C[Ia][Ib] C[Ja][Jb].
+// Step 1 computes the pair densities (one warp per string pair). Step 2 sums, for
+// each RDM element, a host-built list of (density, +/-1) terms -- the list encodes
+// the reference's orbital ordering and antisymmetry signs (add_one_rdm /
+// add_two_rdm, CIDens.cpp:227-292). Step 3 handles the alpha-beta doubles: one
+// block per alpha excitation (ar, ac) (split in a few parts), one thread per beta
+// excitation type (br, bc), looping over the strings that admit it.
+//
+// DOCI: one block of L*L threads per slice of pair strings; thread (j, k)
+// accumulates c_I^2 n_j n_k and the pair-hop products c_I c_J (DensDOCI,
+// CIDens.cpp:1073-1224).
+//
+// Storage follows CIDens: the 1-RDM and each 2-RDM block are symmetric pair
+// matrices (Vector2d, matrix.cpp:674-690), accumulated on (min, max) and mirrored.
+#include <algorithm>
 #include <stdexcept>
 
 #include "crs.cuh"
 
 namespace cigpu {
+namespace {
+
+constexpr int kRdmThreads = 256;
+
+inline int pidx(int p, int q, int L) { return p * L + q - (p + 1) * (p + 2) / 2; }
+
+int64_t hbinom(int n, int k) { return d_binom(n, k); }
+
+uint32_t hrank(uint64_t s) {
+    int64_t r = 0;
+    int m = 0;
+    while (s) {
+        ++m;
+        r += hbinom(__builtin_ctzll(s), m);
+        s &= s - 1;
+    }
+    return (uint32_t)r;
+}
+
+int hnstacked(int a, int b, uint64_t common) {
+    const int lo = std::min(a, b), hi = std::max(a, b);
+    int c = 0;
+    for (int i = lo + 1; i < hi; ++i) c += (int)((common >> i) & 1);
+    return c;
+}
+
+// One spin's pair list and its RDM terms.
+struct PairPlan {
+    std::vector<uint32_t> I, J;  // pairs: [self..., singles..., doubles...]
+    int nz = 0;                  // the first nz pairs (self + singles) also need Dz
+};
+
+struct Plan {
+    int L, np;
+    int64_t Da, Db;
+    PairPlan a, b;
+    size_t off_ga, off_gb, off_g0, off_g1, off_g2, nslots;
+    // density layout: [Da0 | Daz | Db0 | Dbz]
+    size_t off_da0, off_daz, off_db0, off_dbz, ndens;
+    std::vector<std::vector<std::pair<uint32_t, int8_t>>> terms;  // per slot
+    // alpha-beta doubles
+    std::vector<uint32_t> ap_ptr;   // [np+1] alpha pairs per (ar<ac)
+    std::vector<uint64_t> ap;       // Ia | Ja << 32
+    std::vector<int8_t> ap_sign;
+    std::vector<uint32_t> bx_ptr;   // [L*L+1] beta excitations per (br, bc)
+    std::vector<uint64_t> bx;       // Ib | Jb << 32
+    std::vector<int8_t> bx_sign;
+};
+
+void add_term(Plan &P, size_t slot, size_t dens, int coef) {
+    P.terms[slot].push_back({(uint32_t)dens, (int8_t)coef});
+}
+
+// Slot of a symmetric pair matrix entry (min, max) of dimension dimx at offset off.
+size_t sym_slot(size_t off, size_t dimx, size_t A, size_t B) {
+    return off + std::min(A, B) * dimx + std::max(A, B);
+}
+
+// add_two_rdm for a same-spin block (CIDens.cpp:240-255): sorts both pairs with sign flips.
+void add_two_same(Plan &P, size_t off, int o1, int o2, int o3, int o4, size_t dens, int coef) {
+    if (o1 == o2 || o3 == o4) return;
+    if (o1 > o2) { std::swap(o1, o2); coef = -coef; }
+    if (o3 > o4) { std::swap(o3, o4); coef = -coef; }
+    add_term(P, sym_slot(off, P.np, pidx(o1, o2, P.L), pidx(o3, o4, P.L)), dens, coef);
+}
+
+void add_two_ab(Plan &P, int o1, int o2, int o3, int o4, size_t dens, int coef) {
+    const size_t L = P.L;
+    add_term(P, sym_slot(P.off_g1, L * L, o1 * L + o2, o3 * L + o4), dens, coef);
+}
+
+// Pairs and terms of one spin. `alpha` selects which 1-RDM / same-spin block and
+// where the opposite-spin spectators go in Gamma_ab.
+void plan_spin(Plan &P, const SpinTables &t, bool alpha) {
+    const int L = P.L, n = t.n;
+    PairPlan &pp = alpha ? P.a : P.b;
+    const int64_t D = t.D;
+    // self pairs
+    for (int64_t I = 0; I < D; ++I) {
+        pp.I.push_back((uint32_t)I);
+        pp.J.push_back((uint32_t)I);
+    }
+    // upper singles
+    struct Single { uint32_t I, J; int lo, hi, sign; uint64_t common; };
+    std::vector<Single> singles;
+    for (int64_t I = 0; I < D; ++I) {
+        const uint64_t s = t.strings[I];
+        for (int j = 0; j < L; ++j) {
+            if (!((s >> j) & 1)) continue;
+            for (int l = j + 1; l < L; ++l) {
+                if ((s >> l) & 1) continue;
+                const uint64_t u = s ^ ((uint64_t)1 << j) ^ ((uint64_t)1 << l);
+                const uint32_t J = hrank(u);  // > I since l > j
+                singles.push_back({(uint32_t)I, J, j, l, (hnstacked(j, l, s & u) & 1) ? -1 : 1, s & u});
+            }
+        }
+    }
+    for (auto &x : singles) {
+        pp.I.push_back(x.I);
+        pp.J.push_back(x.J);
+    }
+    pp.nz = (int)pp.I.size();
+    // upper same-spin doubles
+    struct Dbl { uint32_t I, J; int o[4]; int sign; };
+    std::vector<Dbl> dbls;
+    for (int64_t I = 0; I < D; ++I) {
+        const uint64_t s = t.strings[I];
+        for (int j1 = 0; j1 < L; ++j1) {
+            if (!((s >> j1) & 1)) continue;
+            for (int j2 = j1 + 1; j2 < L; ++j2) {
+                if (!((s >> j2) & 1)) continue;
+                for (int l1 = 0; l1 < L; ++l1) {
+                    if ((s >> l1) & 1) continue;
+                    for (int l2 = l1 + 1; l2 < L; ++l2) {
+                        if ((s >> l2) & 1) continue;
+                        const uint64_t u = s ^ ((uint64_t)1 << j1) ^ ((uint64_t)1 << j2) ^ ((uint64_t)1 << l1) ^
+                                           ((uint64_t)1 << l2);
+                        const uint32_t J = hrank(u);
+                        if (J <= (uint32_t)I) continue;
+                        // fill_two_dense (CIDens.cpp:756-779): row orbitals first, ascending
+                        const uint64_t c = s & u;
+                        const int diff = hnstacked(j1, j2, c) + hnstacked(l1, l2, c);
+                        dbls.push_back({(uint32_t)I, J, {j1, j2, l1, l2}, (diff & 1) ? -1 : 1});
+                    }
+                }
+            }
+        }
+    }
+    for (auto &x : dbls) {
+        pp.I.push_back(x.I);
+        pp.J.push_back(x.J);
+    }
+    (void)n;
+    // terms
+    const size_t d0 = alpha ? P.off_da0 : P.off_db0;
+    const size_t dz = alpha ? P.off_daz : P.off_dbz;
+    const size_t g1 = alpha ? P.off_ga : P.off_gb;
+    const size_t gs = alpha ? P.off_g0 : P.off_g2;
+    for (int64_t I = 0; I < D; ++I) {  // self pairs (fill_diagonal, CIDens.cpp:808-853)
+        const uint64_t s = t.strings[I];
+        int o[64], k = 0;
+        for (int b = 0; b < L; ++b)
+            if ((s >> b) & 1) o[k++] = b;
+        for (int i = 0; i < k; ++i) add_term(P, sym_slot(g1, L, o[i], o[i]), d0 + I, 1);
+        for (int i = 0; i < k; ++i)
+            for (int j = i + 1; j < k; ++j) add_two_same(P, gs, o[i], o[j], o[i], o[j], d0 + I, 1);
+        if (alpha)  // mixed diagonal part, once (alpha side): Gamma_ab(u z, u z) += sum c^2 n_u n_z
+            for (int i = 0; i < k; ++i)
+                for (int z = 0; z < L; ++z) add_two_ab(P, o[i], z, o[i], z, dz + (size_t)I * L + z, 1);
+    }
+    for (size_t q = 0; q < singles.size(); ++q) {  // fill_one_dense (CIDens.cpp:676-754)
+        const Single &x = singles[q];
+        const size_t pi = (size_t)D + q;
+        add_term(P, sym_slot(g1, L, x.lo, x.hi), d0 + pi, x.sign);
+        for (int z = 0; z < L; ++z) {
+            if ((x.common >> z) & 1) add_two_same(P, gs, x.lo, z, x.hi, z, d0 + pi, x.sign);
+            if (alpha)
+                add_two_ab(P, x.lo, z, x.hi, z, dz + pi * L + z, x.sign);
+            else
+                add_two_ab(P, z, x.lo, z, x.hi, dz + pi * L + z, x.sign);
+        }
+    }
+    for (size_t q = 0; q < dbls.size(); ++q) {
+        const Dbl &x = dbls[q];
+        const size_t pi = (size_t)D + singles.size() + q;
+        add_two_same(P, gs, x.o[0], x.o[1], x.o[2], x.o[3], d0 + pi, x.sign);
+    }
+}
+
+void plan_ab(Plan &P, const SpinTables &ta, const SpinTables &tb) {
+    const int L = P.L;
+    // alpha excitations ar -> ac with ac > ar (the row is the lower-ranked string)
+    std::vector<std::vector<std::pair<uint64_t, int8_t>>> apl(P.np);
+    for (int64_t I = 0; I < ta.D; ++I) {
+        const uint64_t s = ta.strings[I];
+        for (int ar = 0; ar < L; ++ar) {
+            if (!((s >> ar) & 1)) continue;
+            for (int ac = ar + 1; ac < L; ++ac) {
+                if ((s >> ac) & 1) continue;
+                const uint64_t u = s ^ ((uint64_t)1 << ar) ^ ((uint64_t)1 << ac);
+                const int sign = (hnstacked(ar, ac, s & u) & 1) ? -1 : 1;
+                apl[pidx(ar, ac, L)].push_back({(uint64_t)I | ((uint64_t)hrank(u) << 32), (int8_t)sign});
+            }
+        }
+    }
+    P.ap_ptr.assign(P.np + 1, 0);
+    for (int q = 0; q < P.np; ++q) {
+        P.ap_ptr[q + 1] = P.ap_ptr[q] + (uint32_t)apl[q].size();
+        for (auto &e : apl[q]) {
+            P.ap.push_back(e.first);
+            P.ap_sign.push_back(e.second);
+        }
+    }
+    // beta excitations br -> bc (any order)
+    std::vector<std::vector<std::pair<uint64_t, int8_t>>> bxl((size_t)L * L);
+    for (int64_t I = 0; I < tb.D; ++I) {
+        const uint64_t s = tb.strings[I];
+        for (int br = 0; br < L; ++br) {
+            if (!((s >> br) & 1)) continue;
+            for (int bc = 0; bc < L; ++bc) {
+                if ((s >> bc) & 1) continue;
+                const uint64_t u = s ^ ((uint64_t)1 << br) ^ ((uint64_t)1 << bc);
+                const int sign = (hnstacked(br, bc, s & u) & 1) ? -1 : 1;
+                bxl[(size_t)br * L + bc].push_back({(uint64_t)I | ((uint64_t)hrank(u) << 32), (int8_t)sign});
+            }
+        }
+    }
+    P.bx_ptr.assign((size_t)L * L + 1, 0);
+    for (size_t q = 0; q < (size_t)L * L; ++q) {
+        P.bx_ptr[q + 1] = P.bx_ptr[q] + (uint32_t)bxl[q].size();
+        for (auto &e : bxl[q]) {
+            P.bx.push_back(e.first);
+            P.bx_sign.push_back(e.second);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Step 1: pair densities. C is D1 x D2 row-major; other = strings of the D2 spin.
+__global__ void k_pair_dens(const double *__restrict__ C, int64_t D2, const uint32_t *__restrict__ pI,
+                            const uint32_t *__restrict__ pJ, int64_t npairs, int64_t nz,
+                            const uint64_t *__restrict__ other, int L, double *__restrict__ d0,
+                            double *__restrict__ dz) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = wid; p < npairs; p += nw) {
+        const double *ri = C + (int64_t)pI[p] * D2;
+        const double *rj = C + (int64_t)pJ[p] * D2;
+        double acc = 0;
+        for (int64_t b = lane; b < D2; b += 32) acc += ri[b] * rj[b];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) d0[p] = acc;
+        if (p < nz) {
+            for (int z0 = 0; z0 < L; z0 += 32) {
+                const int z = z0 + lane;
+                double az = 0;
+                for (int64_t b = 0; b < D2; ++b)
+                    if (z < L && ((other[b] >> z) & 1)) az += ri[b] * rj[b];
+                if (z < L) dz[p * L + z] = az;
+            }
+        }
+    }
+}
+
+// Step 2: per-slot ordered sums of +/- densities.
+__global__ void k_slot_gather(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ idx,
+                              const int8_t *__restrict__ coef, const double *__restrict__ dens, int64_t nslots,
+                              double *__restrict__ acc) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nslots; s += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0;
+        for (uint32_t e = ptr[s]; e < ptr[s + 1]; ++e) v += (double)coef[e] * dens[idx[e]];
+        acc[s] = v;
+    }
+}
+
+// Step 3: alpha-beta doubles. Block = (alpha excitation q = pidx(ar,ac), split);
+// thread = beta excitation type (br, bc). slices[(q*nsplit + split)*L*L + br*L + bc].
+__global__ void k_ab_doubles(const double *__restrict__ C, int64_t Db, const uint32_t *__restrict__ ap_ptr,
+                             const uint64_t *__restrict__ ap, const int8_t *__restrict__ ap_sign,
+                             const uint32_t *__restrict__ bx_ptr, const uint64_t *__restrict__ bx,
+                             const int8_t *__restrict__ bx_sign, int L, int nsplit, double *__restrict__ slices) {
+    extern __shared__ double rows[];  // [2][Db]
+    const int q = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
+    const uint32_t a0 = ap_ptr[q], a1 = ap_ptr[q + 1];
+    const uint32_t cnt = a1 - a0, per = (cnt + nsplit - 1) / nsplit;
+    const uint32_t s0 = a0 + min(cnt, split * per), s1 = a0 + min(cnt, (split + 1) * per);
+    const int ntypes = L * L;
+    constexpr int kMaxTypesPerThread = 8;
+    double acc[kMaxTypesPerThread];
+    for (int i = 0; i < kMaxTypesPerThread; ++i) acc[i] = 0;
+    for (uint32_t e = s0; e < s1; ++e) {
+        const uint64_t pr = ap[e];
+        const double *ri = C + (int64_t)(uint32_t)pr * Db;
+        const double *rj = C + (int64_t)(uint32_t)(pr >> 32) * Db;
+        __syncthreads();
+        for (int64_t b = threadIdx.x; b < Db; b += blockDim.x) {
+            rows[b] = ri[b];
+            rows[Db + b] = rj[b];
+        }
+        __syncthreads();
+        const double sa = (double)ap_sign[e];
+        for (int i = 0; i < kMaxTypesPerThread; ++i) {
+            const int ty = threadIdx.x + i * blockDim.x;
+            if (ty >= ntypes) break;
+            double part = 0;
+            for (uint32_t x = bx_ptr[ty]; x < bx_ptr[ty + 1]; ++x) {
+                const uint64_t bb = bx[x];
+                part += (double)bx_sign[x] * rows[(uint32_t)bb] * rows[Db + (uint32_t)(bb >> 32)];
+            }
+            acc[i] += sa * part;
+        }
+    }
+    for (int i = 0; i < kMaxTypesPerThread; ++i) {
+        const int ty = threadIdx.x + i * blockDim.x;
+        if (ty < ntypes) slices[((int64_t)q * nsplit + split) * ntypes + ty] = acc[i];
+    }
+}
+
+// Assemble the outputs: gather sums + alpha-beta double slices, mirrored.
+__global__ void k_rdm_assemble(const double *__restrict__ acc, const double *__restrict__ slices, int nsplit, int L,
+                               int np, size_t off_ga, size_t off_gb, size_t off_g0, size_t off_g1, size_t off_g2,
+                               double *__restrict__ rdm1, double *__restrict__ aa, double *__restrict__ ab,
+                               double *__restrict__ bb) {
+    const int64_t L2 = (int64_t)L * L;
+    const int64_t n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;
+    const int64_t total = n1 + 2 * n2 + n3;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < n1) {
+            const int s = (int)(i / L2), a = (int)((i % L2) / L), b = (int)(i % L);
+            rdm1[i] = acc[(s == 0 ? off_ga : off_gb) + (size_t)min(a, b) * L + max(a, b)];
+        } else if (i < n1 + 2 * n2) {
+            const int64_t j = i - n1;
+            const int blk = (int)(j / n2);
+            const int A = (int)((j % n2) / np), B = (int)(j % np);
+            const double v = acc[(blk == 0 ? off_g0 : off_g2) + (size_t)min(A, B) * np + max(A, B)];
+            (blk == 0 ? aa : bb)[j % n2] = v;
+        } else {
+            const int64_t j = i - n1 - 2 * n2;
+            const int64_t A = j / L2, B = j % L2;
+            const int64_t lo = min(A, B), hi = max(A, B);
+            double v = acc[off_g1 + (size_t)lo * L2 + hi];
+            const int ar = (int)(lo / L), ac = (int)(hi / L);
+            if (ar < ac) {
+                const int q = ar * L + ac - (ar + 1) * (ar + 2) / 2;
+                const int64_t ty = (lo % L) * L + (hi % L);
+                for (int sp = 0; sp < nsplit; ++sp) v += slices[((int64_t)q * nsplit + sp) * L2 + ty];
+            }
+            ab[j] = v;
+        }
+    }
+}
+
+__global__ void k_transpose(const double *__restrict__ a, int64_t rows, int64_t cols, double *__restrict__ t) {
+    __shared__ double tile[32][33];
+    const int64_t r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+        if (r0 + i < rows && c0 + threadIdx.x < cols) tile[i][threadIdx.x] = a[(r0 + i) * cols + c0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+        if (c0 + i < cols && r0 + threadIdx.x < rows) t[(c0 + i) * rows + r0 + threadIdx.x] = tile[threadIdx.x][i];
+}
+
+// ---------------------------------------------------------------------------
+// DOCI: thread (j,k) of an L*L block accumulates, over a slice of pair strings,
+//   A_jk = sum c_I^2 n_j n_k   and   B_jk = sum_{j in I, k not in I, k > j} c_I c_J.
+__global__ void k_doci_rdm(const double *__restrict__ c, const uint64_t *__restrict__ strings, int64_t D, int L,
+                           int n, double *__restrict__ partial) {
+    __shared__ uint32_t binom[64 * 33];
+    for (int i = threadIdx.x; i < 64 * 33; i += blockDim.x) {
+        const int nn = i / 33, kk = i % 33;
+        binom[i] = (nn <= L && kk <= n) ? (uint32_t)d_binom(nn, kk) : 0u;
+    }
+    __syncthreads();
+    const int t = threadIdx.x;
+    const int j = t / L, k = t % L;
+    double A = 0, B = 0;
+    if (t < L * L) {
+        for (int64_t I = blockIdx.x; I < D; I += gridDim.x) {
+            const uint64_t s = strings[I];
+            const double cI = c[I];
+            const bool nj = (s >> j) & 1, nk = (s >> k) & 1;
+            if (nj && nk) A += cI * cI;
+            if (nj && !nk && k > j) {
+                const uint64_t u = s ^ ((uint64_t)1 << j) ^ ((uint64_t)1 << k);
+                uint32_t r = 0;
+                int m = 0;
+                for (uint64_t x = u; x; x &= x - 1) {
+                    ++m;
+                    r += binom[(__ffsll((long long)x) - 1) * 33 + m];
+                }
+                B += cI * c[r];
+            }
+        }
+        partial[((int64_t)blockIdx.x * 2) * L * L + t] = A;
+        partial[((int64_t)blockIdx.x * 2 + 1) * L * L + t] = B;
+    }
+}
+
+__global__ void k_doci_rdm_finish(const double *__restrict__ partial, int G, int L, int np, double *__restrict__ rdm1,
+                                  double *__restrict__ aa, double *__restrict__ ab, double *__restrict__ bb) {
+    const int L2 = L * L;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L2) return;
+    double A = 0, B = 0;
+    for (int b = 0; b < G; ++b) {
+        A += partial[((int64_t)b * 2) * L2 + t];
+        B += partial[((int64_t)b * 2 + 1) * L2 + t];
+    }
+    const int j = t / L, k = t % L;
+    // 1-RDM (both spins): gamma_jj = A_jj
+    if (j == k) {
+        rdm1[j * L + j] = A;
+        rdm1[L2 + j * L + j] = A;
+    }
+    // Gamma_ab(jk,jk) = A_jk; Gamma_ab(jj,kk) = Gamma_ab(kk,jj) = B_jk (j < k)
+    ab[(int64_t)(j * L + k) * L2 + j * L + k] = A;
+    if (j < k) {
+        ab[(int64_t)(j * L + j) * L2 + k * L + k] = B;
+        ab[(int64_t)(k * L + k) * L2 + j * L + j] = B;
+        const int P = j * L + k - (j + 1) * (j + 2) / 2;
+        aa[(int64_t)P * np + P] = A;
+        bb[(int64_t)P * np + P] = A;
+    }
+}
+
+template <typename T>
+DevBuf<T> upload(const std::vector<T> &v, cudaStream_t s) {
+    DevBuf<T> d(std::max<size_t>(v.size(), 1));
+    if (!v.empty()) CIGPU_CUDA(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+}
+
+}  // namespace
 
 void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s) {
-    (void)c; (void)c_dev; (void)rdm1; (void)aa; (void)ab; (void)bb; (void)s;
-    throw std::invalid_argument("rdm not available");
+    const int L = c.L, np = L * (L - 1) / 2;
+    const int64_t L2 = (int64_t)L * L;
+    const int64_t n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;
+    DevBuf<double> out(n1 + 2 * n2 + n3);
+    double *o1 = out.p, *oaa = out.p + n1, *obb = out.p + n1 + n2, *oab = out.p + n1 + 2 * n2;
+    if (c.method == CIGPU_DOCI) {
+        if (L * L > 1024) throw std::invalid_argument("DOCI RDM needs L <= 32");
+        CIGPU_CUDA(cudaMemsetAsync(out.p, 0, sizeof(double) * out.n, s));
+        const int G = sm_count() * 4;
+        DevBuf<double> partial((size_t)G * 2 * L2);
+        const int th = ((L * L + 31) / 32) * 32;
+        k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial.p);
+        k_doci_rdm_finish<<<(int)((L2 + 255) / 256), 256, 0, s>>>(partial.p, G, L, np, o1, oaa, oab, obb);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch(2);
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+    } else {
+        if (L > 32) throw std::invalid_argument("FCI RDM needs L <= 32");
+        const SpinTables &ta = c.ta;
+        const SpinTables &tb = (c.ndown == c.nup) ? c.ta : c.tb;
+        Plan P;
+        P.L = L;
+        P.np = np;
+        P.Da = ta.D;
+        P.Db = tb.D;
+        P.off_ga = 0;
+        P.off_gb = L2;
+        P.off_g0 = 2 * L2;
+        P.off_g2 = P.off_g0 + n2;
+        P.off_g1 = P.off_g2 + n2;
+        P.nslots = P.off_g1 + n3;
+        // pair counts first (densities layout needs them)
+        auto count_pairs = [&](const SpinTables &t, size_t &npair, size_t &nz) {
+            size_t ns = 0, nd = 0;
+            for (int64_t I = 0; I < t.D; ++I) {
+                for (int q = 0; q < t.ns; ++q)
+                    if (t.s_target[(size_t)I * t.ns + q] > (uint32_t)I) ++ns;
+                for (int q = 0; q < t.nd; ++q)
+                    if (t.d_target[(size_t)I * t.nd + q] > (uint32_t)I) ++nd;
+            }
+            nz = (size_t)t.D + ns;
+            npair = nz + nd;
+        };
+        size_t npa, nza, npb, nzb;
+        count_pairs(ta, npa, nza);
+        count_pairs(tb, npb, nzb);
+        P.off_da0 = 0;
+        P.off_daz = npa;
+        P.off_db0 = P.off_daz + nza * L;
+        P.off_dbz = P.off_db0 + npb;
+        P.ndens = P.off_dbz + nzb * L;
+        P.terms.assign(P.nslots, {});
+        plan_spin(P, ta, true);
+        plan_spin(P, tb, false);
+        plan_ab(P, ta, tb);
+        if (P.a.I.size() != npa || P.b.I.size() != npb) throw std::runtime_error("rdm plan: pair count mismatch");
+        // CSR of the slot terms
+        std::vector<uint32_t> ptr(P.nslots + 1, 0), idx;
+        std::vector<int8_t> cf;
+        for (size_t q = 0; q < P.nslots; ++q) {
+            ptr[q + 1] = ptr[q] + (uint32_t)P.terms[q].size();
+            for (auto &e : P.terms[q]) {
+                idx.push_back(e.first);
+                cf.push_back(e.second);
+            }
+        }
+        // C^T for the beta densities
+        DevBuf<double> Ct((size_t)c.dim);
+        {
+            dim3 grid((unsigned)((tb.D + 31) / 32), (unsigned)((ta.D + 31) / 32));
+            k_transpose<<<grid, dim3(32, 8), 0, s>>>(c_dev, ta.D, tb.D, Ct.p);
+            count_launch();
+        }
+        DevBuf<uint64_t> sa = upload(ta.strings, s), sb = upload(tb.strings, s);
+        DevBuf<uint32_t> aI = upload(P.a.I, s), aJ = upload(P.a.J, s), bI = upload(P.b.I, s), bJ = upload(P.b.J, s);
+        DevBuf<double> dens(P.ndens);
+        const int G = sm_count() * 8;
+        k_pair_dens<<<G, kRdmThreads, 0, s>>>(c_dev, tb.D, aI.p, aJ.p, (int64_t)npa, (int64_t)nza, sb.p, L,
+                                              dens.p + P.off_da0, dens.p + P.off_daz);
+        k_pair_dens<<<G, kRdmThreads, 0, s>>>(Ct.p, ta.D, bI.p, bJ.p, (int64_t)npb, (int64_t)nzb, sa.p, L,
+                                              dens.p + P.off_db0, dens.p + P.off_dbz);
+        count_launch(2);
+        DevBuf<uint32_t> dptr = upload(ptr, s), didx = upload(idx, s);
+        DevBuf<int8_t> dcf = upload(cf, s);
+        DevBuf<double> acc(P.nslots);
+        k_slot_gather<<<G, kRdmThreads, 0, s>>>(dptr.p, didx.p, dcf.p, dens.p, (int64_t)P.nslots, acc.p);
+        count_launch();
+        // alpha-beta doubles
+        const int nsplit = 4;
+        DevBuf<uint32_t> app = upload(P.ap_ptr, s), bxp = upload(P.bx_ptr, s);
+        DevBuf<uint64_t> apd = upload(P.ap, s), bxd = upload(P.bx, s);
+        DevBuf<int8_t> aps = upload(P.ap_sign, s), bxs = upload(P.bx_sign, s);
+        DevBuf<double> slices((size_t)std::max(np, 1) * nsplit * L2);
+        if (np > 0) {
+            const size_t sm = sizeof(double) * 2 * (size_t)tb.D;
+            if (sm > 200 * 1024) throw std::invalid_argument("FCI RDM: beta string space too large");
+            if (sm > 48 * 1024)
+                CIGPU_CUDA(cudaFuncSetAttribute(k_ab_doubles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            const int th = std::min(1024, (int)((L2 + 31) / 32 * 32));
+            k_ab_doubles<<<np * nsplit, th, sm, s>>>(c_dev, tb.D, app.p, apd.p, aps.p, bxp.p, bxd.p,
+                                                                      bxs.p, L, nsplit, slices.p);
+            count_launch();
+        }
+        k_rdm_assemble<<<G, kRdmThreads, 0, s>>>(acc.p, slices.p, nsplit, L, np, P.off_ga, P.off_gb, P.off_g0, P.off_g1,
+                                                 P.off_g2, o1, oaa, oab, obb);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+    }
+    if (rdm1) CIGPU_CUDA(cudaMemcpyAsync(rdm1, o1, sizeof(double) * n1, cudaMemcpyDeviceToHost, s));
+    if (aa) CIGPU_CUDA(cudaMemcpyAsync(aa, oaa, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
+    if (bb) CIGPU_CUDA(cudaMemcpyAsync(bb, obb, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
+    if (ab) CIGPU_CUDA(cudaMemcpyAsync(ab, oab, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace cigpu

@@ -83,6 +83,27 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_warp(int64_t n, const int
     }
 }
 
+// FP64 product from split FP32 values: v = (double)hi + (double)lo.
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv_hilo(int64_t n, const int64_t *__restrict__ row_ptr,
+                                                            const uint32_t *__restrict__ col,
+                                                            const float *__restrict__ hi, const float *__restrict__ lo,
+                                                            const double *__restrict__ x, double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = wid; r < n; r += nw) {
+        const int64_t s = row_ptr[r], e = row_ptr[r + 1];
+        double acc = 0;
+        for (int64_t k = s + lane; k < e; k += 32) {
+            const double v = (double)__ldcs(hi + k) + (double)__ldcs(lo + k);
+            acc += v * __ldg(x + __ldcs(col + k));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) y[r] = acc;
+    }
+}
+
 }  // namespace
 
 int spmv_grid() { return sm_count_spmv() * kSpmvBlocksPerSM; }
@@ -107,6 +128,13 @@ void spmv_f64(int64_t n, const int64_t *row_ptr, const uint32_t *col, const doub
 void spmv_f32(int64_t n, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
               cudaStream_t s) {
     k_spmv_warp<float><<<spmv_grid(), kSpmvThreads, 0, s>>>(n, row_ptr, col, val, x, y);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void spmv_hilo(int64_t n, const int64_t *row_ptr, const uint32_t *col, const float *hi, const float *lo,
+               const double *x, double *y, cudaStream_t s) {
+    k_spmv_hilo<<<spmv_grid(), kSpmvThreads, 0, s>>>(n, row_ptr, col, hi, lo, x, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -99,6 +99,8 @@ CONFIGS = {
     "c1": dict(method="FCI", L=12, nup=6, ndown=6, nchol=16, seed=1),
     "c2": dict(method="DOCI", L=24, nup=12, ndown=12, nchol=24, seed=2),
     "c4": dict(method="FCI", L=10, nup=5, ndown=5, nchol=16, seed=4),
+    # profiling size: same construction, CRS of a few GB (x larger than L1, CRS larger than L2)
+    "p11": dict(method="FCI", L=11, nup=5, ndown=5, nchol=16, seed=11),
 }
 
 
