@@ -2,6 +2,7 @@
 // export, matvec and solve entry points.
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -37,10 +38,30 @@ void SpinDevStore::upload(const SpinTables &t, cudaStream_t s) {
     up(s_info, t.s_info);
     up(d_target, t.d_target);
     up(d_val, t.d_val);
+    up(d_hi, t.d_hi);
+    up(d_lo, t.d_lo);
     up(nb_full, t.nb_full);
     up(nb_sing, t.nb_sing);
     view = SpinDev{t.D, t.n, t.ns, t.nd, t.nfull, t.nsing, occ.p, diag.p, s_target.p, s_part.p,
-                   s_info.p, d_target.p, d_val.p, nb_full.p, nb_sing.p};
+                   s_info.p, d_target.p, d_val.p, d_hi.p, d_lo.p, nb_full.p, nb_sing.p};
+}
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+Trace::Trace(const char *sc, cudaStream_t st) : scope(sc), s(st) {
+    const char *e = std::getenv("CIGPU_TRACE");
+    on = e && e[0] == '1';
+    t0 = now_s();
+}
+
+void Trace::mark(const char *what) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    const double t = now_s();
+    std::fprintf(stderr, "[cigpu %s] %-24s %9.3f ms\n", scope, what, (t - t0) * 1e3);
+    t0 = t;
 }
 
 int status_from_exception() {
@@ -81,14 +102,17 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
 
 void build_crs(cigpu_crs &c, cudaStream_t s) {
     const auto t0 = std::chrono::steady_clock::now();
+    Trace tr("build", s);
     cigpu_ham &h = *c.ham;
     const int64_t dim = c.dim;
     c.diag.alloc(dim);
     DevBuf<uint32_t> count(dim);
     c.upper_off.alloc(dim);
     c.row_ptr.alloc(dim + 1);
+    tr.mark("alloc small");
     if (c.method == CIGPU_FCI) {
         build_spin_tables(c.L, c.nup, h.h.data(), h.eri.data(), c.ta);
+        tr.mark("host tables");
         c.da.upload(c.ta, s);
         if (c.ndown == c.nup) {
             c.db.view = c.da.view;
@@ -102,11 +126,15 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.a = c.da.view;
         p.b = c.db.view;
         p.eri = h.d_eri.p;
+        p.eri_hi = h.d_eri_hi.p;
+        p.eri_lo = h.d_eri_lo.p;
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
+        tr.mark("upload + diag");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         fci_launch(kCount, p, s);
+        tr.mark("count pass");
     } else {
         c.strings.alloc(dim);
         doci_strings_launch(c.L, c.nup, dim, c.strings.p, s);
@@ -124,6 +152,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         doci_launch(kCount, p, s);
+        tr.mark("strings + diag + count");
     }
     exclusive_scan_u32(count.p, c.row_ptr.p, dim, s);
     CIGPU_CUDA(cudaMemcpyAsync(&c.nnz_full, c.row_ptr.p + dim, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -136,6 +165,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         CIGPU_CUDA(cudaStreamSynchronize(s));
     }
     count.release();
+    tr.mark("scans");
     c.col.alloc(c.nnz_full);
     const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
     if (mode == kFill64)
@@ -144,6 +174,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         c.val32.alloc(c.nnz_full);
         c.val32lo.alloc(c.nnz_full);
     }
+    tr.mark("alloc matrix");
     if (c.method == CIGPU_FCI) {
         c.fp.row_ptr = c.row_ptr.p;
         c.fp.col = c.col.p;
@@ -159,13 +190,14 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         c.dp.val32lo = c.val32lo.p;
         doci_launch(mode, c.dp, s);
     }
+    tr.mark("fill pass");
     CIGPU_CUDA(cudaStreamSynchronize(s));
     c.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
 void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
     if (c.precision == CIGPU_FP64) {
-        spmv_f64(c.dim, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
+        spmv_f64(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
         return;
     }
     if (c.val32lo.p) {
@@ -189,7 +221,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
 
 void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
     if (c.precision != CIGPU_MIXED) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
-    spmv_f32(c.dim, c.row_ptr.p, c.col.p, c.val32.p, x, y, s);
+    spmv_f32(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, x, y, s);
 }
 
 }  // namespace cigpu
@@ -300,6 +332,14 @@ int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, 
     H->d_eri.alloc(L4);
     CIGPU_CUDA(cudaMemcpy(H->d_h.p, H->h.data(), L2 * sizeof(double), cudaMemcpyHostToDevice));
     CIGPU_CUDA(cudaMemcpy(H->d_eri.p, H->eri.data(), L4 * sizeof(double), cudaMemcpyHostToDevice));
+    {
+        std::vector<float> hi(L4), lo(L4);
+        for (size_t i = 0; i < L4; ++i) split_fp32(H->eri[i], hi[i], lo[i]);
+        H->d_eri_hi.alloc(L4);
+        H->d_eri_lo.alloc(L4);
+        CIGPU_CUDA(cudaMemcpy(H->d_eri_hi.p, hi.data(), L4 * sizeof(float), cudaMemcpyHostToDevice));
+        CIGPU_CUDA(cudaMemcpy(H->d_eri_lo.p, lo.data(), L4 * sizeof(float), cudaMemcpyHostToDevice));
+    }
     *out = H.release();
     return CIGPU_OK;
     CIGPU_CATCH

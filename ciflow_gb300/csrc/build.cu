@@ -54,13 +54,34 @@ __global__ void k_fci_diag(FciParams p, double *diag) {
     }
 }
 
+// |v| > 1e-14 on the bit pattern (integer compare; GB300's FP64 pipe is slow).
+__device__ __forceinline__ bool keep_bits(uint64_t b) {
+    return (b & 0x7FFFFFFFFFFFFFFFull) > 0x3D06849B86A12B9Bull;  // bits of 1e-14
+}
+__device__ __forceinline__ uint64_t flip_if(uint64_t b, uint32_t odd) { return b ^ ((uint64_t)odd << 63); }
+__device__ __forceinline__ float flipf_if(float f, uint32_t odd) {
+    return __uint_as_float(__float_as_uint(f) ^ (odd << 31));
+}
+
+// One FCI row per warp; the block owns one alpha string Ia and kFciRowsPerBlock
+// beta strings. Shared memory: the alpha neighbour list, group starts, the slot ->
+// group map, and the integral slices (ar ac|. .) of the alpha singles of Ia
+// (FP64 for COUNT/FILL64/MATVEC; FP32 hi/lo for FILL32, zeroed where |v| <= 1e-14).
 template <int MODE>
 __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nga = p.a.nfull;
+    const int L = p.L, L2 = L * L;
+    const int nsa = p.a.ns;
+    const int W = p.b.nfull + nsa * p.b.nsing + p.a.nd;
     uint64_t *nbA = reinterpret_cast<uint64_t *>(smem);
     uint32_t *gstart = reinterpret_cast<uint32_t *>(nbA + nga);
     uint16_t *gmap = reinterpret_cast<uint16_t *>(gstart + nga + 1);
+    unsigned char *after = reinterpret_cast<unsigned char *>(gmap + W);
+    after = reinterpret_cast<unsigned char *>(((uintptr_t)after + 15) & ~(uintptr_t)15);
+    uint64_t *sl64 = reinterpret_cast<uint64_t *>(after);  // [nsa][L2] FP64 bits
+    float *slhi = reinterpret_cast<float *>(after);       // [nsa][L2]
+    float *sllo = slhi + (size_t)nsa * L2;                // [nsa][L2]
 
     const int64_t nchunks = (p.Db + kFciRowsPerBlock - 1) / kFciRowsPerBlock;
     const int64_t ia = blockIdx.x / nchunks;
@@ -68,8 +89,21 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
 
-    // alpha neighbour list of Ia and the structural start of each group
     for (int g = tid; g < nga; g += blockDim.x) nbA[g] = p.a.nb_full[ia * nga + g];
+    if (p.staged) {
+        for (int i = tid; i < nsa * L2; i += blockDim.x) {
+            const int xa = i / L2, t = i - xa * L2;
+            const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
+            const int ar = (info >> 12) & 63, ac = (info >> 18) & 63;
+            const size_t at = ((size_t)ar * L + ac) * L2 + t;  // (ar ac|br bc)
+            if (MODE == kFill32) {
+                slhi[i] = __ldg(p.eri_hi + at);
+                sllo[i] = __ldg(p.eri_lo + at);
+            } else {
+                sl64[i] = __double_as_longlong(__ldg(p.eri + at));
+            }
+        }
+    }
     __syncthreads();
     if (warp == 0) {
         uint32_t run = 0;
@@ -96,9 +130,8 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
         for (uint32_t k = gstart[g]; k < gstart[g + 1]; ++k) gmap[k] = (uint16_t)g;
     __syncthreads();
 
-    const int W = (int)gstart[nga];
     const uint8_t *occA = p.a.occ + ia * p.a.n;
-    const size_t L1 = p.L, L2 = L1 * L1, L3 = L2 * L1;
+    const size_t L1 = L, L3 = (size_t)L2 * L;
 
     for (int rr = warp; rr < kFciRowsPerBlock; rr += nwarps) {
         const int64_t ib = chunk * kFciRowsPerBlock + rr;
@@ -113,9 +146,10 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
         double acc = 0;
         for (int k0 = 0; k0 < W; k0 += 32) {
             const int k = k0 + lane;
-            double v = 0;
+            uint64_t vb = 0;       // FP64 bits (COUNT / FILL64 / MATVEC, and computed elements)
+            float hi = 0, lo = 0;  // FILL32
+            bool keep = false, low = false, computed = false;
             uint32_t col = 0;
-            bool low = false;
             if (k < W) {
                 const int g = gmap[k];
                 const int q = k - (int)gstart[g];
@@ -131,21 +165,29 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     col = (uint32_t)(ia * p.Db + Jb);
                     low = Jb < (uint32_t)ib;
                     if (kindB == kSelf) {
-                        v = p.diag[r];
+                        vb = __double_as_longlong(p.diag[r]);
+                        computed = true;
                     } else if (kindB == kSingle) {
                         // one_diff_orbital(down1, down2, up1) (CIMethod.cpp:409-427)
                         const size_t at = ib * p.b.ns + xb;
-                        v = __ldg(p.b.s_part + at);
+                        double v = __ldg(p.b.s_part + at);
                         const uint32_t info = __ldg(p.b.s_info + at);
-                        const int lo = info & 63, hi = (info >> 6) & 63;
-                        const double *e = p.eri + lo * L3 + hi * L2;
+                        const int lo_ = info & 63, hi_ = (info >> 6) & 63;
+                        const double *e = p.eri + lo_ * L3 + hi_ * (size_t)L2;
                         for (int z = 0; z < p.a.n; ++z) {
                             const int o = occA[z];
                             v += __ldg(e + o * L1 + o);  // <lo z|hi z> = (lo hi|z z)
                         }
-                        if ((info >> 24) & 1) v = -v;
+                        vb = flip_if(__double_as_longlong(v), (info >> 24) & 1);
+                        computed = true;
                     } else {
-                        v = __ldg(p.b.d_val + ib * p.b.nd + xb);
+                        const size_t at = ib * p.b.nd + xb;
+                        if (MODE == kFill32) {
+                            hi = __ldg(p.b.d_hi + at);
+                            lo = __ldg(p.b.d_lo + at);
+                        } else {
+                            vb = __double_as_longlong(__ldg(p.b.d_val + at));
+                        }
                     }
                 } else if (kindA == kSingle) {
                     const uint64_t eb = __ldg(nbS + q);
@@ -154,37 +196,74 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     const uint32_t xb = (uint32_t)(eb >> 34);
                     col = (uint32_t)((int64_t)Ja * p.Db + Jb);
                     low = Ja < (uint32_t)ia;
-                    const size_t ata = ia * p.a.ns + xa;
+                    const size_t ata = ia * nsa + xa;
                     const uint32_t infoA = __ldg(p.a.s_info + ata);
                     if (kindB == kSelf) {
                         // one_diff_orbital(up1, up2, down1)
-                        v = __ldg(p.a.s_part + ata);
-                        const int lo = infoA & 63, hi = (infoA >> 6) & 63;
-                        const double *e = p.eri + lo * L3 + hi * L2;
+                        double v = __ldg(p.a.s_part + ata);
+                        const int lo_ = infoA & 63, hi_ = (infoA >> 6) & 63;
+                        const double *e = p.eri + lo_ * L3 + hi_ * (size_t)L2;
                         for (int z = 0; z < p.b.n; ++z) {
                             const int o = occB[z];
                             v += __ldg(e + o * L1 + o);
                         }
-                        if ((infoA >> 24) & 1) v = -v;
+                        vb = flip_if(__double_as_longlong(v), (infoA >> 24) & 1);
+                        computed = true;
                     } else {
                         // two_diff_orbitals(up1,up2,down1,down2) (CIMethod.cpp:444-457):
-                        // V(a_row, b_row, a_col, b_col) from the lower-ranked determinant.
+                        // V(a_row, b_row, a_col, b_col) = (ar ac|br bc); exact 8-fold symmetry
+                        // of the stored integrals makes it independent of which side is the row.
                         const uint32_t infoB = __ldg(p.b.s_info + ib * p.b.ns + xb);
-                        const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
                         const int br = (infoB >> 12) & 63, bc = (infoB >> 18) & 63;
-                        if (Ja > (uint32_t)ia)
-                            v = ld_eri(p.eri, p.L, ar, ac, br, bc);  // <ar br|ac bc> = (ar ac|br bc)
-                        else
-                            v = ld_eri(p.eri, p.L, ac, ar, bc, br);
-                        if (((infoA ^ infoB) >> 24) & 1) v = -v;
+                        const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
+                        const int t = br * L + bc;
+                        if (MODE == kFill32) {
+                            if (p.staged) {
+                                hi = slhi[xa * L2 + t];
+                                lo = sllo[xa * L2 + t];
+                            } else {
+                                const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
+                                const size_t at = ((size_t)ar * L + ac) * L2 + t;
+                                hi = __ldg(p.eri_hi + at);
+                                lo = __ldg(p.eri_lo + at);
+                            }
+                            hi = flipf_if(hi, odd);
+                            lo = flipf_if(lo, odd);
+                        } else {
+                            uint64_t b;
+                            if (p.staged) {
+                                b = sl64[xa * L2 + t];
+                            } else {
+                                const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
+                                b = __double_as_longlong(__ldg(p.eri + ((size_t)ar * L + ac) * L2 + t));
+                            }
+                            vb = flip_if(b, odd);
+                        }
                     }
                 } else {
                     col = (uint32_t)((int64_t)Ja * p.Db + ib);
                     low = Ja < (uint32_t)ia;
-                    v = __ldg(p.a.d_val + ia * p.a.nd + xa);
+                    const size_t at = ia * p.a.nd + xa;
+                    if (MODE == kFill32) {
+                        hi = __ldg(p.a.d_hi + at);
+                        lo = __ldg(p.a.d_lo + at);
+                    } else {
+                        vb = __double_as_longlong(__ldg(p.a.d_val + at));
+                    }
+                }
+                if (MODE == kFill32) {
+                    if (computed) {
+                        keep = keep_bits(vb);
+                        const double v = __longlong_as_double(vb);
+                        hi = (float)v;
+                        lo = (float)(v - (double)hi);
+                    } else {
+                        keep = (__float_as_uint(hi) & 0x7FFFFFFFu) != 0u;  // tables are zero where |v| <= 1e-14
+                    }
+                } else {
+                    keep = keep_bits(vb);
                 }
             }
-            const bool keep = (k < W) && (fabs(v) > kZero);
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (MODE == kCount) {
                 nlow += __popc(__ballot_sync(0xffffffffu, keep && low));
@@ -193,15 +272,14 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     const int64_t pos = base + running + __popc(mask & ((1u << lane) - 1u));
                     p.col[pos] = col;
                     if (MODE == kFill64) {
-                        p.val64[pos] = v;
+                        p.val64[pos] = __longlong_as_double(vb);
                     } else {
-                        const float hi = (float)v;
                         p.val32[pos] = hi;
-                        p.val32lo[pos] = (float)(v - (double)hi);
+                        p.val32lo[pos] = lo;
                     }
                 }
             } else {
-                if (keep) acc += v * __ldg(p.x + col);
+                if (keep) acc += __longlong_as_double(vb) * __ldg(p.x + col);
             }
             running += __popc(mask);
         }
@@ -312,7 +390,7 @@ __global__ void __launch_bounds__(kDociThreads) k_doci_rows(DociParams p) {
         if (MODE == kCount) {
             uint32_t cnt = 0, low = 0;
             for (int e = lane; e < W; e += 32) {
-                const bool keep = fabs(vals[e]) > kZero;
+                const bool keep = keep_bits(__double_as_longlong(vals[e]));
                 cnt += keep;
                 low += keep && keys[e] < (uint32_t)r;
             }
@@ -330,7 +408,7 @@ __global__ void __launch_bounds__(kDociThreads) k_doci_rows(DociParams p) {
         if (MODE == kMatvec64) {
             double acc = 0;
             for (int e = lane; e < W; e += 32)
-                if (fabs(vals[e]) > kZero) acc += vals[e] * __ldg(p.x + keys[e]);
+                if (keep_bits(__double_as_longlong(vals[e]))) acc += vals[e] * __ldg(p.x + keys[e]);
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) p.y[r] = acc;
             __syncwarp();
@@ -355,7 +433,7 @@ __global__ void __launch_bounds__(kDociThreads) k_doci_rows(DociParams p) {
                 v = vals[e];
                 col = keys[e];
             }
-            const bool keep = (k < W) && fabs(v) > kZero;
+            const bool keep = (k < W) && keep_bits(__double_as_longlong(v));
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const int64_t pos = base + running + __popc(mask & ((1u << lane) - 1u));
@@ -407,21 +485,32 @@ static int grid_for(int64_t work, int threads, int per_sm = 8) {
     return (int)(g < cap ? (g > 0 ? g : 1) : cap);
 }
 
-size_t fci_smem_bytes(const FciParams &p) {
+static size_t fci_base_smem(const FciParams &p) {
     const int W = p.b.nfull + p.a.ns * p.b.nsing + p.a.nd;
     size_t b = (size_t)p.a.nfull * 8 + ((size_t)p.a.nfull + 1) * 4 + (size_t)W * 2;
     return (b + 15) & ~(size_t)15;
 }
 
-void fci_launch(int mode, const FciParams &p, cudaStream_t s) {
+// Integral slices of the alpha singles: nsa * L^2 entries of 8 bytes (FP64, or FP32 hi + lo).
+static size_t fci_slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }
+
+size_t fci_smem_bytes(const FciParams &p) {
+    const size_t b = fci_base_smem(p), sl = fci_slice_smem(p);
+    return (b + sl <= kFciMaxSmem) ? b + sl : b;
+}
+
+void fci_launch(int mode, const FciParams &p0, cudaStream_t s) {
+    FciParams p = p0;
+    const size_t sm = fci_smem_bytes(p);
+    p.staged = (sm == fci_base_smem(p) + fci_slice_smem(p)) ? 1 : 0;
+    if (mode == kFill32 && (!p.eri_hi || !p.eri_lo)) throw CudaError{cudaErrorInvalidValue, "FP32 integral tables missing"};
     const int64_t nchunks = (p.Db + kFciRowsPerBlock - 1) / kFciRowsPerBlock;
     const int64_t blocks = p.a.D * nchunks;
-    const size_t sm = fci_smem_bytes(p);
     if (sm > 48 * 1024) {
-        cudaFuncSetAttribute(k_fci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_fci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_fci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_fci_rows<kMatvec64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_fci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
+        cudaFuncSetAttribute(k_fci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
+        cudaFuncSetAttribute(k_fci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
+        cudaFuncSetAttribute(k_fci_rows<kMatvec64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
     }
     switch (mode) {
         case kCount: k_fci_rows<kCount><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;

@@ -7,8 +7,9 @@ namespace cigpu {
 
 enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2, kMatvec64 = 3 };
 
-constexpr int kFciThreads = 128;
-constexpr int kFciRowsPerBlock = 32;
+constexpr int kFciThreads = 256;
+constexpr int kFciRowsPerBlock = 64;
+constexpr size_t kFciMaxSmem = 112 * 1024;  // two blocks per SM at most this size
 constexpr int kDociThreads = 128;
 
 struct FciParams {
@@ -16,6 +17,8 @@ struct FciParams {
     int64_t Db;
     SpinDev a, b;
     const double *eri;  // chemist (pq|rs), L^4
+    const float *eri_hi, *eri_lo;  // FP32 split of eri, zero where |v| <= 1e-14
+    int staged;         // alpha-single integral slices fit in shared memory
     const double *diag; // [dim] row diagonals
     // COUNT outputs
     uint32_t *row_count;

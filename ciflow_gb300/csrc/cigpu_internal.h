@@ -59,6 +59,17 @@ struct DevBuf {
 
 void *dev_alloc(size_t bytes);  // throws std::bad_alloc on failure
 
+// Phase timer: with CIGPU_TRACE=1 in the environment, mark() synchronises the
+// stream and prints the time since the previous mark to stderr.
+struct Trace {
+    const char *scope;
+    cudaStream_t s;
+    bool on;
+    double t0;
+    Trace(const char *sc, cudaStream_t st);
+    void mark(const char *what);
+};
+
 template <typename T>
 void DevBuf<T>::alloc(size_t count) {
     release();
@@ -71,6 +82,16 @@ void DevBuf<T>::alloc(size_t count) {
 // Per-spin string tables for FCI (host side, uploaded once per CRS).
 // Strings are ranked in colex order, the order of Permutator_Bit
 // (Permutator.cpp:113-153) and of determine_weight (CIMethod.cpp:689-747).
+// FP32 split (hi = fl32(v), lo = fl32(v - hi)); both zero when |v| <= 1e-14.
+inline void split_fp32(double v, float &hi, float &lo) {
+    if (!(v > kZero || v < -kZero)) {
+        hi = lo = 0.0f;
+        return;
+    }
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
 struct SpinTables {
     int L = 0, n = 0;
     int64_t D = 0;
@@ -86,6 +107,7 @@ struct SpinTables {
     std::vector<uint32_t> s_info;    // [D][ns] lo | hi<<6 | row<<12 | col<<18 | odd<<24
     std::vector<uint32_t> d_target;  // [D][nd]
     std::vector<double> d_val;       // [D][nd] signed element (min-rank perspective)
+    std::vector<float> d_hi, d_lo;   // [D][nd] FP32 split of d_val, zero where |v| <= 1e-14
     std::vector<uint64_t> nb_full;   // [D][nfull] sorted by target: target | kind<<32 | idx<<34
     std::vector<uint64_t> nb_sing;   // [D][nsing] sorted {self} + singles
 };
@@ -103,6 +125,7 @@ struct SpinDev {
     const uint32_t *s_info;
     const uint32_t *d_target;
     const double *d_val;
+    const float *d_hi, *d_lo;
     const uint64_t *nb_full;
     const uint64_t *nb_sing;
 };
@@ -110,6 +133,7 @@ struct SpinDev {
 struct SpinDevStore {
     DevBuf<uint8_t> occ;
     DevBuf<double> diag, s_part, d_val;
+    DevBuf<float> d_hi, d_lo;
     DevBuf<uint32_t> s_target, s_info, d_target;
     DevBuf<uint64_t> nb_full, nb_sing;
     SpinDev view{};
@@ -126,4 +150,5 @@ struct cigpu_ham {
     std::vector<double> eri;  // host copy, L^4 chemist
     cigpu::DevBuf<double> d_h;
     cigpu::DevBuf<double> d_eri;
+    cigpu::DevBuf<float> d_eri_hi, d_eri_lo;  // FP32 split, zero where |v| <= 1e-14
 };

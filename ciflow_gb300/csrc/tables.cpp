@@ -78,6 +78,8 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
     t.s_info.resize(D * (size_t)t.ns);
     t.d_target.resize(D * (size_t)t.nd);
     t.d_val.resize(D * (size_t)t.nd);
+    t.d_hi.resize(D * (size_t)t.nd);
+    t.d_lo.resize(D * (size_t)t.nd);
     t.nb_full.resize(D * (size_t)t.nfull);
     t.nb_sing.resize(D * (size_t)t.nsing);
 
@@ -162,6 +164,7 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
                         const size_t at = (size_t)I * t.nd + di;
                         t.d_target[at] = J;
                         t.d_val[at] = e;
+                        split_fp32(e, t.d_hi[at], t.d_lo[at]);
                         full.push_back((uint64_t)J | ((uint64_t)kDouble << 32) | ((uint64_t)di << 34));
                         ++di;
                     }
