@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "lanczos.cuh"
@@ -30,6 +31,14 @@ namespace cigpu {
 int sm_count();
 
 namespace {
+
+// Host-side time accounting of a solve (printed with CIGPU_TRACE=1).
+struct SolveClock {
+    double eigh = 0, wait = 0;
+    int64_t n_eigh = 0, n_wait = 0;
+};
+thread_local SolveClock g_clk;
+inline double wall() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
 
 constexpr int kVecThreads = 256;
 constexpr int kMaxBasis = 64;
@@ -338,7 +347,10 @@ struct VecOps {
     // fetch out[0..cnt) to the host (synchronises the stream)
     const double *fetch(int cnt) {
         CIGPU_CUDA(cudaMemcpyAsync(h_out, out.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
+        const double t0 = wall();
         CIGPU_CUDA(cudaStreamSynchronize(s));
+        g_clk.wait += wall() - t0;
+        ++g_clk.n_wait;
         return h_out;
     }
     double residual(const double *w, const double *c, double E, double *r, int64_t n) {
@@ -354,6 +366,10 @@ struct VecOps {
 
 // ---------------------------------------------------------------------------
 void small_eigh(int n, std::vector<double> &a, std::vector<double> &w, std::vector<double> &z) {
+    struct Acc {
+        double t0 = wall();
+        ~Acc() { g_clk.eigh += wall() - t0; ++g_clk.n_eigh; }
+    } acc_;
     z.assign((size_t)n * n, 0.0);
     for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
     double fro = 0;
@@ -590,7 +606,17 @@ struct Refine {
 
 }  // namespace
 
+static void trace_report(const char *what, const cigpu_solve_info &info, double t0) {
+    const char *e = std::getenv("CIGPU_TRACE");
+    if (!(e && e[0] == '1')) return;
+    std::fprintf(stderr, "[cigpu solve] %s: %.3f ms total, host eigensolves %lld (%.3f ms), waits %lld (%.3f ms), mv64 %lld mv32 %lld\n",
+                 what, (wall() - t0) * 1e3, (long long)g_clk.n_eigh, g_clk.eigh * 1e3, (long long)g_clk.n_wait,
+                 g_clk.wait * 1e3, (long long)info.matvecs_fp64, (long long)info.matvecs_fp32);
+}
+
 int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info) {
+    g_clk = SolveClock{};
+    const double tstart = wall();
     const int64_t n = P.n;
     const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
     const int m = (int)std::min<int64_t>(std::min(o.basis, kMaxBasis), std::max<int64_t>(n, 1));
@@ -627,6 +653,7 @@ int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool
     info.matvecs_fp64 = lz.matvecs + 1 + 0;
     info.restarts = lz.restarts;
     info.converged = er.second <= o.tol;
+    trace_report("fp64 lanczos", info, tstart);
     return info.converged ? CIGPU_OK : CIGPU_ENOCONV;
 }
 
@@ -644,6 +671,8 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     const int64_t n = P.n;
     const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
     cudaStream_t s = P.stream;
+    g_clk = SolveClock{};
+    const double tstart = wall();
     if (n <= 2 || !P.mv32 || !P.diag) {
         if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
         return solve_fp64(P, o, c_dev, true, info);
@@ -768,6 +797,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     info.restarts = 0;
     info.corrections = collapses;
     info.converged = rho <= o.tol;
+    trace_report("mixed davidson", info, tstart);
     return info.converged ? CIGPU_OK : CIGPU_ENOCONV;
 }
 

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstring>
 #include <stdexcept>
+#include <thread>
 
 #include "cigpu_internal.h"
 
@@ -32,14 +33,15 @@ int64_t binom(int n, int k) {
     return r;
 }
 
-// Colex rank = sum_m C(p_m, m) over set bits p_1 < p_2 < ... (CIMethod.cpp:732-747).
-uint32_t rank_of(uint64_t s) {
+// Colex rank = sum_m C(p_m, m) over set bits p_1 < p_2 < ... (CIMethod.cpp:732-747);
+// bt[p * 65 + m] = C(p, m).
+uint32_t rank_of(uint64_t s, const std::vector<int64_t> &bt) {
     int64_t r = 0;
     int m = 0;
     while (s) {
         int p = __builtin_ctzll(s);
         ++m;
-        r += binom(p, m);
+        r += bt[p * 65 + m];
         s &= s - 1;
     }
     return static_cast<uint32_t>(r);
@@ -55,6 +57,19 @@ int nstacked(int a, int b, uint64_t common) {
     int lo = a < b ? a : b, hi = a < b ? b : a;
     uint64_t mask = (hi > lo + 1) ? ((((uint64_t)1 << hi) - 1) & ~(((uint64_t)1 << (lo + 1)) - 1)) : 0;
     return __builtin_popcountll(common & mask);
+}
+
+// Stable LSD radix sort of packed entries by their low 32 bits (the target
+// rank, < 2^nbits), one byte per pass.
+void sort_by_target(std::vector<uint64_t> &a, std::vector<uint64_t> &tmp, int nbits) {
+    tmp.resize(a.size());
+    for (int shift = 0; shift < nbits; shift += 8) {
+        uint32_t cnt[257] = {0};
+        for (uint64_t x : a) ++cnt[(((uint32_t)x) >> shift & 255u) + 1];
+        for (int b = 0; b < 256; ++b) cnt[b + 1] += cnt[b];
+        for (uint64_t x : a) tmp[cnt[((uint32_t)x) >> shift & 255u]++] = x;
+        a.swap(tmp);
+    }
 }
 
 }  // namespace
@@ -89,12 +104,22 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
         if (n > 0 && I + 1 < D) s = next_comb(s);
     }
 
-    std::vector<uint64_t> full, sing;
-    for (int64_t I = 0; I < D; ++I) {
+    std::vector<int64_t> bt(65 * 65, 0);
+    for (int p = 0; p <= 64; ++p)
+        for (int m = 0; m <= 64 && m <= p; ++m) bt[p * 65 + m] = (p <= 62) ? binom(p, m) : 0;
+    auto work = [&](int64_t I0, int64_t I1) {
+    std::vector<uint64_t> full, sing, tmp;
+    int nbits = 1;
+    while (nbits < 32 && ((int64_t)1 << nbits) < D) ++nbits;
+    for (int64_t I = I0; I < I1; ++I) {
         const uint64_t si = t.strings[I];
-        int o[64], k = 0;
-        for (int b = 0; b < L; ++b)
-            if (si >> b & 1) o[k++] = b;
+        int o[64], k = 0, v[64], kv = 0;
+        for (int b = 0; b < L; ++b) {
+            if (si >> b & 1)
+                o[k++] = b;
+            else
+                v[kv++] = b;
+        }
         for (int a = 0; a < n; ++a) t.occ[I * n + a] = (uint8_t)o[a];
         // diagonal part of one string, reference order
         double d = 0;
@@ -109,18 +134,21 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
         sing.push_back((uint64_t)I | ((uint64_t)kSelf << 32));
         // singles: row orbital j (occupied) -> col orbital l (empty)
         int si_idx = 0;
-        for (int j = 0; j < L; ++j) {
-            if (!(si >> j & 1)) continue;
-            for (int l = 0; l < L; ++l) {
-                if (si >> l & 1) continue;
+        for (int ja = 0; ja < k; ++ja) {
+            const int j = o[ja];
+            for (int la = 0; la < kv; ++la) {
+                const int l = v[la];
                 const uint64_t sj = si ^ ((uint64_t)1 << j) ^ ((uint64_t)1 << l);
-                const uint32_t J = rank_of(sj);
+                const uint32_t J = rank_of(sj, bt);
                 const int lo = j < l ? j : l, hi = j < l ? l : j;
                 const uint64_t common = si & sj;
                 // one_diff_orbital: elemu = T(lo,hi) + sum_z (V(lo,z,hi,z) - V(lo,z,z,hi))
                 double e = h[lo * L + hi];
-                for (int z = 0; z < L; ++z)
-                    if (common >> z & 1) e += E.V(lo, z, hi, z) - E.V(lo, z, z, hi);
+                for (int za = 0; za < k; ++za) {  // common orbitals ascending: occupied minus j
+                    const int z = o[za];
+                    if (z == j) continue;
+                    e += E.V(lo, z, hi, z) - E.V(lo, z, z, hi);
+                }
                 const int odd = nstacked(lo, hi, common) & 1;
                 const size_t at = (size_t)I * t.ns + si_idx;
                 t.s_target[at] = J;
@@ -134,30 +162,31 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
         }
         // same-spin doubles j1<j2 occupied -> l1<l2 empty
         int di = 0;
-        for (int j1 = 0; j1 < L; ++j1) {
-            if (!(si >> j1 & 1)) continue;
-            for (int j2 = j1 + 1; j2 < L; ++j2) {
-                if (!(si >> j2 & 1)) continue;
-                for (int l1 = 0; l1 < L; ++l1) {
-                    if (si >> l1 & 1) continue;
-                    for (int l2 = l1 + 1; l2 < L; ++l2) {
-                        if (si >> l2 & 1) continue;
+        for (int a1 = 0; a1 < k; ++a1) {
+            const int j1 = o[a1];
+            for (int a2 = a1 + 1; a2 < k; ++a2) {
+                const int j2 = o[a2];
+                for (int b1 = 0; b1 < kv; ++b1) {
+                    const int l1 = v[b1];
+                    for (int b2 = b1 + 1; b2 < kv; ++b2) {
+                        const int l2 = v[b2];
                         const uint64_t sj =
                             si ^ ((uint64_t)1 << j1) ^ ((uint64_t)1 << j2) ^ ((uint64_t)1 << l1) ^ ((uint64_t)1 << l2);
-                        const uint32_t J = rank_of(sj);
+                        const uint32_t J = rank_of(sj, bt);
                         // the reference evaluates the upper element: row = the lower-ranked string
                         const uint64_t row = (J > (uint32_t)I) ? si : sj;
                         const uint64_t colS = (J > (uint32_t)I) ? sj : si;
                         const uint64_t common = si & sj;
                         int a[4], na = 0, nb = 2;
                         // arrange_order (CIMethod.cpp:353-380): row orbitals first, ascending
-                        for (int b = 0; b < L; ++b) {
-                            if (!((row ^ colS) >> b & 1)) continue;
+                        for (uint64_t x = row ^ colS; x; x &= x - 1) {
+                            const int b = __builtin_ctzll(x);
                             if (row >> b & 1)
                                 a[na++] = b;
                             else
                                 a[nb++] = b;
                         }
+                        (void)colS;
                         const int diff = nstacked(a[0], a[1], common) + nstacked(a[2], a[3], common);
                         double e = E.V(a[0], a[1], a[2], a[3]) - E.V(a[0], a[1], a[3], a[2]);
                         if (diff % 2 != 0) e *= -1;
@@ -171,11 +200,20 @@ void build_spin_tables(int L, int n, const double *h, const double *eri, SpinTab
                 }
             }
         }
-        auto by_target = [](uint64_t x, uint64_t y) { return (uint32_t)x < (uint32_t)y; };
-        std::sort(full.begin(), full.end(), by_target);
-        std::sort(sing.begin(), sing.end(), by_target);
+        sort_by_target(full, tmp, nbits);
+        sort_by_target(sing, tmp, nbits);
         std::memcpy(&t.nb_full[(size_t)I * t.nfull], full.data(), full.size() * sizeof(uint64_t));
         std::memcpy(&t.nb_sing[(size_t)I * t.nsing], sing.data(), sing.size() * sizeof(uint64_t));
+    }
+    };
+    // strings are independent: split them over host threads (disjoint output ranges)
+    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>((int64_t)std::thread::hardware_concurrency(), D / 64));
+    if (nt <= 1) {
+        work(0, D);
+    } else {
+        std::vector<std::thread> th;
+        for (int64_t q = 0; q < nt; ++q) th.emplace_back(work, D * q / nt, D * (q + 1) / nt);
+        for (auto &x : th) x.join();
     }
 }
 

@@ -4,7 +4,8 @@ named configuration (used for profiler captures and roofline timing).
     python -m ciflow_gb300.kernel_bench --config c4 --kernel spmv_f32 --reps 3
 
 Kernels: spmv_f32, spmv_f64 (CRS matvec), build_f64, build_f32 (CRS build:
-count + fill passes), matvec_regen (FP64 product with regenerated elements).
+count + fill passes), matvec_regen (FP64 product with regenerated elements),
+solve_mixed / solve_fp64 (one eigensolve on a prebuilt CRS).
 Prints one JSON line with the CUDA-event time per launch and the algorithmic
 bytes of the matvec.
 """
@@ -21,7 +22,9 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c4")
     ap.add_argument("--kernel", default="spmv_f32",
-                    choices=["spmv_f32", "spmv_f64", "build_f64", "build_f32", "matvec_regen"])
+                    choices=["spmv_f32", "spmv_f64", "build_f64", "build_f32", "matvec_regen", "solve_mixed",
+                             "solve_fp64"])
+    ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=1)
     args = ap.parse_args()
@@ -41,7 +44,7 @@ def main() -> None:
     A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri), ctypes.byref(ham)))
     stream = torch.cuda.Stream()
     sh = ctypes.c_void_p(stream.cuda_stream)
-    prec = A.MIXED if args.kernel in ("spmv_f32", "build_f32", "matvec_regen") else A.FP64
+    prec = A.MIXED if args.kernel in ("spmv_f32", "build_f32", "matvec_regen", "solve_mixed") else A.FP64
 
     def build():
         crs = ctypes.c_void_p()
@@ -50,7 +53,21 @@ def main() -> None:
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     out = {"config": args.config, "kernel": args.kernel, "reps": args.reps}
-    if args.kernel.startswith("build"):
+    if args.kernel.startswith("solve"):
+        crs = build()
+        info = A.SolveInfo()
+        for _ in range(args.warmup):
+            lib.cigpu_solve(crs, args.tol, 0, None, None, ctypes.byref(info))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.reps):
+            lib.cigpu_solve(crs, args.tol, 0, None, None, ctypes.byref(info))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["ms_per_solve"] = e0.elapsed_time(e1) / args.reps
+        out["info"] = info.as_dict()
+        lib.cigpu_crs_destroy(crs)
+    elif args.kernel.startswith("build"):
         for _ in range(args.warmup):
             lib.cigpu_crs_destroy(build())
         torch.cuda.synchronize()
