@@ -47,26 +47,30 @@ constexpr int kMaxKeep = 32;
 
 int vec_grid() { return sm_count() * 4; }
 
-template <typename VT, typename WT>
+// Per-block partial dots V_i . w (i < nvec, chunks of kDotChunk on blockIdx.y).
+// AT is the arithmetic type of the products and of the per-thread sums (float for
+// FP32 vectors: GB300 issues FP64 at 1/64 of the FP32 rate); block partials are
+// reduced in FP64.
+template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__ V, int64_t ld, int nvec,
                                                           const WT *__restrict__ w, int64_t n,
                                                           double *__restrict__ partial, int G) {
     const int v0 = blockIdx.y * kDotChunk;
     const int nv = min(kDotChunk, nvec - v0);
-    double acc[kDotChunk];
+    AT acc[kDotChunk];
 #pragma unroll
     for (int i = 0; i < kDotChunk; ++i) acc[i] = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        const double wr = (double)w[r];
+        const AT wr = (AT)w[r];
 #pragma unroll
         for (int i = 0; i < kDotChunk; ++i)
-            if (i < nv) acc[i] += (double)V[(int64_t)(v0 + i) * ld + r] * wr;
+            if (i < nv) acc[i] += (AT)V[(int64_t)(v0 + i) * ld + r] * wr;
     }
     __shared__ double sh[kDotChunk][kVecThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < kDotChunk; ++i) {
-        double a = acc[i];
+        double a = (double)acc[i];
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) sh[i][warp] = a;
     }
@@ -89,26 +93,27 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int G, int
     if (lane == 0) out[v] = s;
 }
 
-// w -= sum_{i<nvec} V_i coef_i (FP64 arithmetic); partial ||w||^2 per block when nrm != nullptr.
-template <typename VT, typename WT>
+// w -= sum_{i<nvec} V_i coef_i (arithmetic in AT); partial ||w||^2 per block when nrm != nullptr.
+template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
                                                         const double *__restrict__ coef, WT *__restrict__ w, int64_t n,
                                                         double *__restrict__ nrm) {
-    __shared__ double c[kMaxBasis + 1];
-    for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = coef[i];
+    __shared__ AT c[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = (AT)coef[i];
     __syncthreads();
-    double acc = 0;
+    AT acc = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        double x = (double)w[r];
-        for (int i = 0; i < nvec; ++i) x -= (double)V[(int64_t)i * ld + r] * c[i];
+        AT x = (AT)w[r];
+        for (int i = 0; i < nvec; ++i) x -= (AT)V[(int64_t)i * ld + r] * c[i];
         const WT xv = (WT)x;
         w[r] = xv;
-        acc += (double)xv * (double)xv;
+        acc += (AT)xv * (AT)xv;
     }
     if (nrm) {
         __shared__ double sh[kVecThreads / 32];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+        double a = (double)acc;
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
         __syncthreads();
         if (threadIdx.x == 0) {
             double s = 0;
@@ -159,6 +164,57 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual(const double *__re
         double s = 0;
         for (int q = 0; q < kVecThreads / 32; ++q) s += sh[q];
         nrm[blockIdx.x] = s;
+    }
+}
+
+// FP32 Davidson residual of u = a0 c + sum_i y_i v_i, written straight into the
+// next basis slot as the preconditioned direction:
+//   ru = a0 r + a0 (E - theta) c + sum_i y_i (HV_i - theta V_i)   (FP32 arithmetic;
+//        r = H c - E c is the exact FP64 anchor residual)
+//   t  = ru / (theta - H_ii)                                      (guarded)
+// and the partial ||ru||^2 (FP64 block sums).
+__global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const double *__restrict__ r64,
+                                                                const double *__restrict__ c64,
+                                                                const float *__restrict__ V, const float *__restrict__ HV,
+                                                                int64_t ld, int k, const double *__restrict__ y,
+                                                                double a0, double a0_de, double theta,
+                                                                const double *__restrict__ diag, float *__restrict__ t,
+                                                                int64_t n, double *__restrict__ nrm) {
+    __shared__ float ys[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = (float)y[i];
+    __syncthreads();
+    const float fa0 = (float)a0, fa0de = (float)a0_de, fth = (float)theta;
+    float acc = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        float ru = fa0 * (float)r64[r] + fa0de * (float)c64[r];
+        for (int i = 0; i < k; ++i) {
+            const int64_t o = (int64_t)(i + 1) * ld + r;  // corrections live in slots 1..k
+            ru += ys[i] * (HV[o] - fth * V[o]);
+        }
+        acc += ru * ru;
+        float d = (float)(theta - diag[r]);
+        if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
+        t[r] = ru / d;
+    }
+    __shared__ double sh[kVecThreads / 32];
+    double a = (double)acc;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0;
+        for (int q = 0; q < kVecThreads / 32; ++q) sum += sh[q];
+        nrm[blockIdx.x] = sum;
+    }
+}
+
+// t = r / (E - H_ii) in FP32 (first direction after an anchor update).
+__global__ void k_precond32(const double *__restrict__ r, const double *__restrict__ diag, double E,
+                            float *__restrict__ t, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float d = (float)(E - diag[i]);
+        if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
+        t[i] = (float)r[i] / d;
     }
 }
 
@@ -219,9 +275,9 @@ __global__ void k_unit_at_argmin(const double *__restrict__ pv, const int64_t *_
 
 template <typename VT>
 __global__ void k_scale(VT *__restrict__ w, int64_t n, const double *__restrict__ nrm2) {
-    const double inv = 1.0 / sqrt(*nrm2);
+    const VT inv = (VT)(1.0 / sqrt(*nrm2));
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
-        w[r] = (VT)((double)w[r] * inv);
+        w[r] = w[r] * inv;
 }
 
 // out_i = sum_{l<m} V_l Y[l + m*i], i < k (Y column-major on the device).
@@ -319,18 +375,19 @@ struct VecOps {
     ~VecOps() {
         if (h_out) cudaFreeHost(h_out);
     }
-    // out[dst .. dst+nvec) = V_i . w
-    template <typename VT, typename WT>
+    // out[dst .. dst+nvec) = V_i . w   (AT: arithmetic type of the products)
+    template <typename VT, typename WT, typename AT = double>
     void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst) {
         dim3 grid(G, (nvec + kDotChunk - 1) / kDotChunk);
-        k_multidot<VT, WT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, G);
+        k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, G);
         k_reduce_partials<<<(nvec + 7) / 8, 256, 0, s>>>(partial.p, G, nvec, out.p + dst);
         CIGPU_CUDA(cudaGetLastError());
         count_launch(2);
     }
-    template <typename VT, typename WT>
+    template <typename VT, typename WT, typename AT = double>
     void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at) {
-        k_update<VT, WT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n, nrm_at >= 0 ? partial.p : nullptr);
+        k_update<VT, WT, AT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n,
+                                                       nrm_at >= 0 ? partial.p : nullptr);
         count_launch();
         if (nrm_at >= 0) {
             k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p + nrm_at);
@@ -660,14 +717,16 @@ int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool
 int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info) {
     // Anchored mixed-precision Davidson.
     //   anchor c (FP64) with w = H c from an FP64 matvec, E = c.w, r = w - E c (exact);
-    //   corrections v_1..v_k stored in FP32 with H v_i from the FP32 CRS matvec;
+    //   corrections v_1..v_k stored in FP32 with H v_i from the FP32 CRS matvec; all
+    //   per-iteration vector arithmetic is FP32 with FP64 reductions;
     //   projected matrix over [c, v_i - eta_i c] (eta_i = c.v_i):
-    //       G = [[E, r.v_j], [r.v_i, v_i.H32 v_j]]   (FP64 accumulation)
+    //       G = [[E, r.v_j], [r.v_i, v_i.H32 v_j]]
     //   new direction t = ru / (theta - H_ii) (diagonal preconditioner) where ru is the
     //   Davidson residual assembled from FP32 vectors. The FP32 error in ru scales with
     //   the correction size |y_v|, so once ru approaches eps32 |H| |y_v| (or the basis is
     //   full) the correction is folded into the anchor and the residual is recomputed
     //   exactly with an FP64 matvec (residual-correction restart).
+    // Basis slots: 0 = fp32(c) (orthogonalisation only), 1..k = corrections, k+1 = new.
     const int64_t n = P.n;
     const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
     cudaStream_t s = P.stream;
@@ -679,7 +738,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     }
     VecOps ops(s);
     Refine ref(n, s, ops);
-    const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 1), n - 1);
+    const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 2), n - 2);
     if (!have_start) {
         DevBuf<double> pv(ops.G);
         DevBuf<int64_t> pi(ops.G);
@@ -687,92 +746,67 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         k_unit_at_argmin<<<ops.G, kVecThreads, 0, s>>>(pv.p, pi.p, ops.G, c_dev, n);
         CIGPU_CUDA(cudaGetLastError());
         count_launch(2);
-        CIGPU_CUDA(cudaStreamSynchronize(s));
     }
-    DevBuf<float> V((size_t)mmax * n), HV((size_t)mmax * n);
+    DevBuf<float> V((size_t)(mmax + 2) * n), HV((size_t)(mmax + 2) * n), cr32((size_t)2 * n);
     DevBuf<double> yd(kMaxBasis + 1);
     std::vector<double> A((size_t)kMaxBasis * kMaxBasis, 0.0), eta(kMaxBasis, 0.0), bvec(kMaxBasis, 0.0);
     int64_t mv32 = 0, mv64 = 0;
     int collapses = 0;
-    auto er = ref.eval(P, c_dev);
-    ++mv64;
-    double E = er.first, rho = er.second, gap = 0;
-    double last_rho = 1e300;
-    int k = 0;
-    double theta = E, a0 = 1.0;
+    double E = 0, rho = 0, gap = 0, last_rho = 1e300;
+    auto anchor = [&]() {  // exact FP64 anchor evaluation
+        const auto er = ref.eval(P, c_dev);
+        ++mv64;
+        E = er.first;
+        rho = er.second;
+        dev_convert(c_dev, V.p, n, s);          // slot 0
+        dev_convert(c_dev, cr32.p, n, s);       // c32, r32 for the couplings
+        dev_convert(ref.r.p, cr32.p + n, n, s);
+    };
+    anchor();
+    int k = 0;  // corrections in the basis
+    double theta = E, a0 = 1.0, yv = 0;
     std::vector<double> y(kMaxBasis + 1, 0.0);
-    bool fresh = true;  // next direction comes from the exact residual r
-    bool force_fold = false;
+    const int SLOT_R = 3 * (kMaxBasis + 1), SLOT_N = SLOT_R + 1;
     while (rho > o.tol && mv32 + mv64 < budget) {
-        // preconditioned direction
-        if (fresh) {
-            k_precond<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, ref.t.p, n);
+        float *vnew = V.p + (size_t)(k + 1) * n;
+        float *hvnew = HV.p + (size_t)(k + 1) * n;
+        // preconditioned direction into slot k+1 (and ||ru||^2 into SLOT_R)
+        if (k == 0) {
+            k_precond32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, vnew, n);
             count_launch();
         } else {
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
-            k_dav_residual<<<ops.G, kVecThreads, 0, s>>>(ref.w.p, c_dev, V.p, HV.p, n, k, yd.p, a0, theta, P.diag,
-                                                          ref.t.p, n, ops.partial.p);
-            k_reduce_partials<<<1, 32, 0, s>>>(ops.partial.p, ops.G, 1, ops.out.p);
+            k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, c_dev, V.p, HV.p, n, k, yd.p, a0, a0 * (E - theta),
+                                                            theta, P.diag, vnew, n, ops.partial.p);
+            k_reduce_partials<<<1, 32, 0, s>>>(ops.partial.p, ops.G, 1, ops.out.p + SLOT_R);
             count_launch(2);
-            CIGPU_CUDA(cudaGetLastError());
-            const double rho_u = std::sqrt(ops.fetch(1)[0]);
-            double yv = 0;
-            for (int i = 1; i <= k; ++i) yv += y[i] * y[i];
-            yv = std::sqrt(yv);
-            const double floor = 30.0 * 6e-8 * std::max(1.0, std::fabs(theta)) * yv;
-            if (rho_u <= std::max(0.5 * o.tol, floor) || k >= mmax || force_fold) {
-                force_fold = false;
-                // fold the correction into the anchor: c <- a0 c + sum_i y_i v_i (FP64)
-                CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
-                k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(V.p, n, k, yd.p, 1, ref.t.p, n, n);
-                k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
-                CIGPU_CUDA(cudaGetLastError());
-                count_launch(2);
-                er = ref.eval(P, c_dev);
-                ++mv64;
-                ++collapses;
-                E = er.first;
-                rho = er.second;
-                k = 0;
-                fresh = true;
-                if (rho > 0.7 * last_rho && collapses > 3) break;  // no progress between collapses
-                last_rho = rho;
-                continue;
-            }
         }
-        // orthonormalise t against c (FP64) and the FP32 corrections, twice
-        for (int pass = 0; pass < 2; ++pass) {
-            ops.dots(c_dev, n, 1, ref.t.p, n, 0);
-            ops.update(c_dev, n, 1, 0, ref.t.p, n, (k == 0 && pass == 1) ? 1 : -1);
-            if (k > 0) {
-                ops.dots(V.p, n, k, ref.t.p, n, 2);
-                ops.update(V.p, n, k, 2, ref.t.p, n, pass == 1 ? 1 : -1);
-            }
-        }
-        const double tn = std::sqrt(ops.fetch(2)[1]);
-        if (!(tn > 1e-14)) {
-            // the search space is invariant: nothing new to add
-            if (k == 0) break;
-            force_fold = true;  // fold the current correction on the next pass
-            continue;
-        }
-        k_scale_to<double, float><<<ops.G, kVecThreads, 0, s>>>(ref.t.p, n, ops.out.p + 1, V.p + (size_t)k * n);
-        CIGPU_CUDA(cudaGetLastError());
-        count_launch();
-        P.mv32(V.p + (size_t)k * n, HV.p + (size_t)k * n, s);
+        // orthonormalise against slots 0..k, twice (FP32 arithmetic, FP64 reductions)
+        ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0);
+        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, -1);
+        ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0);
+        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, SLOT_N);
+        ops.scale(vnew, n, SLOT_N);
+        P.mv32(vnew, hvnew, s);
         ++mv32;
-        // new column of the projection and the couplings of v_k to the anchor
-        ops.dots(V.p, n, k + 1, HV.p + (size_t)k * n, n, 0);
-        ops.dots(V.p + (size_t)k * n, n, 1, c_dev, n, k + 1);
-        ops.dots(V.p + (size_t)k * n, n, 1, ref.r.p, n, k + 2);
-        const double *h = ops.fetch(k + 3);
-        for (int i = 0; i <= k; ++i) {
-            A[(size_t)i * kMaxBasis + k] = h[i];
-            A[(size_t)k * kMaxBasis + i] = h[i];
+        // projection column and couplings: V[1..k+1].Hv_new, then c32.v_new, r32.v_new
+        ops.dots<float, float, float>(V.p + n, n, k + 1, hvnew, n, 0);
+        ops.dots<float, float, float>(cr32.p, n, 2, vnew, n, k + 1);
+        const double *h = ops.fetch(SLOT_N + 1);
+        const double tn2 = h[SLOT_N];
+        const double rho_u = (k > 0) ? std::sqrt(h[SLOT_R]) : 1e300;
+        if (!(tn2 > 1e-28)) {
+            // the search space is invariant: fold what we have and stop expanding
+            if (k == 0) break;
+        } else {
+            for (int i = 0; i <= k; ++i) {
+                A[(size_t)i * kMaxBasis + k] = h[i];
+                A[(size_t)k * kMaxBasis + i] = h[i];
+            }
+            eta[k] = h[k + 1];
+            bvec[k] = h[k + 2];
+            ++k;
         }
-        eta[k] = h[k + 1];
-        bvec[k] = h[k + 2];
-        ++k;
         // Rayleigh-Ritz over [c, v_1..v_k]
         const int q = k + 1;
         std::vector<double> G((size_t)q * q, 0.0), wv, zv;
@@ -782,11 +816,32 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
             for (int j = 0; j < k; ++j) G[(size_t)(i + 1) * q + (j + 1)] = A[(size_t)i * kMaxBasis + j];
         small_eigh(q, G, wv, zv);
         theta = wv[0];
-        gap = q > 1 ? wv[1] - wv[0] : gap;
+        if (q > 1) gap = wv[1] - wv[0];
         for (int i = 0; i < q; ++i) y[i] = zv[(size_t)i * q];
         a0 = y[0];
         for (int i = 1; i <= k; ++i) a0 -= y[i] * eta[i - 1];
-        fresh = false;
+        // fold when the previous approximate residual reached the FP32 floor of the
+        // correction (the new solution, with one more vector, is at least as good),
+        // when the basis is full, or on breakdown
+        const double floor = 30.0 * 6e-8 * std::max(1.0, std::fabs(theta)) * yv;
+        const bool fold = rho_u <= std::max(0.5 * o.tol, floor) || k >= mmax || !(tn2 > 1e-28);
+        yv = 0;
+        for (int i = 1; i <= k; ++i) yv += y[i] * y[i];
+        yv = std::sqrt(yv);
+        if (fold) {
+            // c <- a0 c + sum_i y_i v_i  (FP64)
+            CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+            k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(V.p + n, n, k, yd.p, 1, ref.t.p, n, n);
+            k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
+            CIGPU_CUDA(cudaGetLastError());
+            count_launch(2);
+            anchor();
+            ++collapses;
+            k = 0;
+            yv = 0;
+            if (rho > 0.7 * last_rho && collapses > 3) break;  // no progress between folds
+            last_rho = rho;
+        }
     }
     info.e0 = E;
     info.residual = rho;
