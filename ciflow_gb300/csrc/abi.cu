@@ -107,6 +107,8 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     const int64_t dim = c.dim;
     c.diag.alloc(dim);
     DevBuf<uint32_t> count(dim);
+    DevBuf<double> sgl64;                          // FCI row singles (build only)
+    DevBuf<float> sgl_hi, sgl_lo, diag_hi, diag_lo;  // their FP32 splits (MIXED build only)
     c.upper_off.alloc(dim);
     c.row_ptr.alloc(dim + 1);
     tr.mark("alloc small");
@@ -130,7 +132,21 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.eri_lo = h.d_eri_lo.p;
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
-        tr.mark("upload + diag");
+        const size_t nsr = (size_t)(c.da.view.ns + c.db.view.ns);
+        sgl64.alloc(std::max<size_t>((size_t)dim * nsr, 1));
+        if (c.precision == CIGPU_MIXED) {
+            sgl_hi.alloc(std::max<size_t>((size_t)dim * nsr, 1));
+            sgl_lo.alloc(std::max<size_t>((size_t)dim * nsr, 1));
+            diag_hi.alloc(dim);
+            diag_lo.alloc(dim);
+        }
+        fci_singles_launch(p, sgl64.p, sgl_hi.p, sgl_lo.p, diag_hi.p, diag_lo.p, s);
+        p.sgl64 = sgl64.p;
+        p.sgl_hi = sgl_hi.p;
+        p.sgl_lo = sgl_lo.p;
+        p.diag_hi = diag_hi.p;
+        p.diag_lo = diag_lo.p;
+        tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         fci_launch(kCount, p, s);
@@ -192,6 +208,9 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     }
     tr.mark("fill pass");
     CIGPU_CUDA(cudaStreamSynchronize(s));
+    // the per-row singles tables are only needed by the build passes
+    c.fp.sgl64 = nullptr;
+    c.fp.sgl_hi = c.fp.sgl_lo = c.fp.diag_hi = c.fp.diag_lo = nullptr;
     c.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -205,18 +224,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         spmv_hilo(c.dim, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
         return;
     }
-    // without the remainder array: regenerate the FP64 elements on the fly
-    if (c.method == CIGPU_FCI) {
-        FciParams p = c.fp;
-        p.x = x;
-        p.y = y;
-        fci_launch(kMatvec64, p, s);
-    } else {
-        DociParams p = c.dp;
-        p.x = x;
-        p.y = y;
-        doci_launch(kMatvec64, p, s);
-    }
+    throw std::invalid_argument("MIXED CRS without its FP32 remainder array");
 }
 
 void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {

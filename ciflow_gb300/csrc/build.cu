@@ -14,9 +14,8 @@
 //   DOCI row I: {I} plus every pair hop j -> k, sorted by rank in shared memory.
 // A warp owns one row; each lane evaluates one structural slot, and a ballot
 // keeps the elements with |v| > 1e-14 in order. Three passes use the same
-// generator: COUNT (row lengths), FILL (columns + values), and MATVEC (an FP64
-// product with regenerated elements, used for the residual corrections of the
-// mixed-precision solver).
+// generator: COUNT (row lengths) and FILL (columns + values; FP64, or FP32 hi
+// and lo parts for the mixed method).
 //
 // Values are bit-identical to the reference: every element is a chain of FP64
 // additions in the reference order (no multiplications, so no FMA contraction),
@@ -67,6 +66,51 @@ __device__ __forceinline__ float flipf_if(float f, uint32_t odd) {
 // beta strings. Shared memory: the alpha neighbour list, group starts, the slot ->
 // group map, and the integral slices (ar ac|. .) of the alpha singles of Ia
 // (FP64 for COUNT/FILL64/MATVEC; FP32 hi/lo for FILL32, zeroed where |v| <= 1e-14).
+// Single-excitation elements of every row, one thread per (row, single):
+// one_diff_orbital (CIMethod.cpp:409-427) = same-spin part (host, s_part) + the
+// opposite-spin terms added in ascending orbital order, then the phase. Done
+// here without divergence so the row generator only loads them.
+__global__ void k_fci_singles(FciParams p, double *__restrict__ sgl64, float *__restrict__ sgl_hi,
+                              float *__restrict__ sgl_lo, float *__restrict__ diag_hi, float *__restrict__ diag_lo) {
+    const int ns = p.a.ns + p.b.ns;
+    const int64_t dim = p.a.D * p.Db;
+    const int64_t total = dim * ns;
+    const size_t L1 = p.L, L2 = L1 * L1, L3 = L2 * L1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / ns;
+        const int q = (int)(i - r * ns);
+        const int64_t ia = r / p.Db, ib = r - ia * p.Db;
+        double v;
+        uint32_t info;
+        if (q < p.a.ns) {  // alpha single, beta spectators
+            const size_t at = ia * p.a.ns + q;
+            v = p.a.s_part[at];
+            info = p.a.s_info[at];
+            const double *e = p.eri + (info & 63) * L3 + ((info >> 6) & 63) * L2;
+            const uint8_t *occ = p.b.occ + ib * p.b.n;
+            for (int z = 0; z < p.b.n; ++z) v += __ldg(e + occ[z] * (L1 + 1));  // (lo hi|z z)
+        } else {  // beta single, alpha spectators
+            const size_t at = ib * p.b.ns + (q - p.a.ns);
+            v = p.b.s_part[at];
+            info = p.b.s_info[at];
+            const double *e = p.eri + (info & 63) * L3 + ((info >> 6) & 63) * L2;
+            const uint8_t *occ = p.a.occ + ia * p.a.n;
+            for (int z = 0; z < p.a.n; ++z) v += __ldg(e + occ[z] * (L1 + 1));
+        }
+        if ((info >> 24) & 1) v = -v;
+        sgl64[i] = v;
+        if (sgl_hi) {
+            float hi, lo;
+            split_fp32(v, hi, lo);
+            sgl_hi[i] = hi;
+            sgl_lo[i] = lo;
+        }
+    }
+    if (diag_hi)
+        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+            split_fp32(p.diag[r], diag_hi[r], diag_lo[r]);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -130,25 +174,20 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
         for (uint32_t k = gstart[g]; k < gstart[g + 1]; ++k) gmap[k] = (uint16_t)g;
     __syncthreads();
 
-    const uint8_t *occA = p.a.occ + ia * p.a.n;
-    const size_t L1 = L, L3 = (size_t)L2 * L;
-
     for (int rr = warp; rr < kFciRowsPerBlock; rr += nwarps) {
         const int64_t ib = chunk * kFciRowsPerBlock + rr;
         if (ib >= p.Db) break;
         const int64_t r = ia * p.Db + ib;
         const uint64_t *nbF = p.b.nb_full + ib * p.b.nfull;
         const uint64_t *nbS = p.b.nb_sing + ib * p.b.nsing;
-        const uint8_t *occB = p.b.occ + ib * p.b.n;
         int64_t base = 0;
         if (MODE == kFill64 || MODE == kFill32) base = p.row_ptr[r];
         uint32_t running = 0, nlow = 0;
-        double acc = 0;
         for (int k0 = 0; k0 < W; k0 += 32) {
             const int k = k0 + lane;
             uint64_t vb = 0;       // FP64 bits (COUNT / FILL64 / MATVEC, and computed elements)
             float hi = 0, lo = 0;  // FILL32
-            bool keep = false, low = false, computed = false;
+            bool keep = false, low = false;
             uint32_t col = 0;
             if (k < W) {
                 const int g = gmap[k];
@@ -165,21 +204,21 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     col = (uint32_t)(ia * p.Db + Jb);
                     low = Jb < (uint32_t)ib;
                     if (kindB == kSelf) {
-                        vb = __double_as_longlong(p.diag[r]);
-                        computed = true;
-                    } else if (kindB == kSingle) {
-                        // one_diff_orbital(down1, down2, up1) (CIMethod.cpp:409-427)
-                        const size_t at = ib * p.b.ns + xb;
-                        double v = __ldg(p.b.s_part + at);
-                        const uint32_t info = __ldg(p.b.s_info + at);
-                        const int lo_ = info & 63, hi_ = (info >> 6) & 63;
-                        const double *e = p.eri + lo_ * L3 + hi_ * (size_t)L2;
-                        for (int z = 0; z < p.a.n; ++z) {
-                            const int o = occA[z];
-                            v += __ldg(e + o * L1 + o);  // <lo z|hi z> = (lo hi|z z)
+                        if (MODE == kFill32) {
+                            hi = p.diag_hi[r];
+                            lo = p.diag_lo[r];
+                        } else {
+                            vb = __double_as_longlong(p.diag[r]);
                         }
-                        vb = flip_if(__double_as_longlong(v), (info >> 24) & 1);
-                        computed = true;
+                    } else if (kindB == kSingle) {
+                        // beta single (one_diff_orbital(down1, down2, up1)), precomputed per row
+                        const size_t at = (size_t)r * (nsa + p.b.ns) + nsa + xb;
+                        if (MODE == kFill32) {
+                            hi = __ldg(p.sgl_hi + at);
+                            lo = __ldg(p.sgl_lo + at);
+                        } else {
+                            vb = __double_as_longlong(__ldg(p.sgl64 + at));
+                        }
                     } else {
                         const size_t at = ib * p.b.nd + xb;
                         if (MODE == kFill32) {
@@ -196,19 +235,16 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     const uint32_t xb = (uint32_t)(eb >> 34);
                     col = (uint32_t)((int64_t)Ja * p.Db + Jb);
                     low = Ja < (uint32_t)ia;
-                    const size_t ata = ia * nsa + xa;
-                    const uint32_t infoA = __ldg(p.a.s_info + ata);
+                    const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
                     if (kindB == kSelf) {
-                        // one_diff_orbital(up1, up2, down1)
-                        double v = __ldg(p.a.s_part + ata);
-                        const int lo_ = infoA & 63, hi_ = (infoA >> 6) & 63;
-                        const double *e = p.eri + lo_ * L3 + hi_ * (size_t)L2;
-                        for (int z = 0; z < p.b.n; ++z) {
-                            const int o = occB[z];
-                            v += __ldg(e + o * L1 + o);
+                        // alpha single (one_diff_orbital(up1, up2, down1)), precomputed per row
+                        const size_t at = (size_t)r * (nsa + p.b.ns) + xa;
+                        if (MODE == kFill32) {
+                            hi = __ldg(p.sgl_hi + at);
+                            lo = __ldg(p.sgl_lo + at);
+                        } else {
+                            vb = __double_as_longlong(__ldg(p.sgl64 + at));
                         }
-                        vb = flip_if(__double_as_longlong(v), (infoA >> 24) & 1);
-                        computed = true;
                     } else {
                         // two_diff_orbitals(up1,up2,down1,down2) (CIMethod.cpp:444-457):
                         // V(a_row, b_row, a_col, b_col) = (ar ac|br bc); exact 8-fold symmetry
@@ -251,18 +287,10 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                         vb = __double_as_longlong(__ldg(p.a.d_val + at));
                     }
                 }
-                if (MODE == kFill32) {
-                    if (computed) {
-                        keep = keep_bits(vb);
-                        const double v = __longlong_as_double(vb);
-                        hi = (float)v;
-                        lo = (float)(v - (double)hi);
-                    } else {
-                        keep = (__float_as_uint(hi) & 0x7FFFFFFFu) != 0u;  // tables are zero where |v| <= 1e-14
-                    }
-                } else {
+                if (MODE == kFill32)
+                    keep = (__float_as_uint(hi) & 0x7FFFFFFFu) != 0u;  // splits are zero where |v| <= 1e-14
+                else
                     keep = keep_bits(vb);
-                }
             }
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (MODE == kCount) {
@@ -278,8 +306,6 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                         p.val32lo[pos] = lo;
                     }
                 }
-            } else {
-                if (keep) acc += __longlong_as_double(vb) * __ldg(p.x + col);
             }
             running += __popc(mask);
         }
@@ -288,10 +314,6 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                 p.row_count[r] = running;
                 p.upper_off[r] = nlow;
             }
-        } else if (MODE == kMatvec64) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) p.y[r] = acc;
         }
     }
 }
@@ -405,15 +427,6 @@ __global__ void __launch_bounds__(kDociThreads) k_doci_rows(DociParams p) {
             __syncwarp();
             continue;
         }
-        if (MODE == kMatvec64) {
-            double acc = 0;
-            for (int e = lane; e < W; e += 32)
-                if (keep_bits(__double_as_longlong(vals[e]))) acc += vals[e] * __ldg(p.x + keys[e]);
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) p.y[r] = acc;
-            __syncwarp();
-            continue;
-        }
         // sorted position = number of smaller ranks (ranks are distinct)
         for (int e = lane; e < W; e += 32) {
             const uint32_t key = keys[e];
@@ -510,14 +523,21 @@ void fci_launch(int mode, const FciParams &p0, cudaStream_t s) {
         cudaFuncSetAttribute(k_fci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
-        cudaFuncSetAttribute(k_fci_rows<kMatvec64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
     }
     switch (mode) {
         case kCount: k_fci_rows<kCount><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
         case kFill64: k_fci_rows<kFill64><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
-        case kFill32: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
-        default: k_fci_rows<kMatvec64><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
+        default: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
     }
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void fci_singles_launch(const FciParams &p, double *sgl64, float *sgl_hi, float *sgl_lo, float *diag_hi,
+                        float *diag_lo, cudaStream_t s) {
+    const int64_t total = p.a.D * p.Db * (int64_t)(p.a.ns + p.b.ns);
+    k_fci_singles<<<grid_for(std::max<int64_t>(total, 1), 256, 16), 256, 0, s>>>(p, sgl64, sgl_hi, sgl_lo, diag_hi,
+                                                                                 diag_lo);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -553,15 +573,13 @@ void doci_launch(int mode, const DociParams &p, cudaStream_t s) {
         cudaFuncSetAttribute(k_doci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_doci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_doci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_doci_rows<kMatvec64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     const int blocks = grid_for(p.D * 32, kDociThreads, 16);
     switch (mode) {
         case kCount: k_doci_rows<kCount><<<blocks, kDociThreads, sm, s>>>(p); break;
         case kFill64: k_doci_rows<kFill64><<<blocks, kDociThreads, sm, s>>>(p); break;
-        case kFill32: k_doci_rows<kFill32><<<blocks, kDociThreads, sm, s>>>(p); break;
-        default: k_doci_rows<kMatvec64><<<blocks, kDociThreads, sm, s>>>(p); break;
+        default: k_doci_rows<kFill32><<<blocks, kDociThreads, sm, s>>>(p); break;
     }
     CIGPU_CUDA(cudaGetLastError());
     count_launch();

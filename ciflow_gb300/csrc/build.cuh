@@ -5,7 +5,7 @@
 
 namespace cigpu {
 
-enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2, kMatvec64 = 3 };
+enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2 };
 
 constexpr int kFciThreads = 256;
 constexpr int kFciRowsPerBlock = 64;
@@ -20,6 +20,11 @@ struct FciParams {
     const float *eri_hi, *eri_lo;  // FP32 split of eri, zero where |v| <= 1e-14
     int staged;         // alpha-single integral slices fit in shared memory
     const double *diag; // [dim] row diagonals
+    const float *diag_hi, *diag_lo;  // FP32 split of diag (MIXED)
+    // single-excitation elements per row: [dim][ns_a + ns_b], alpha singles first
+    // (FP64, and the FP32 split zeroed where |v| <= 1e-14 for MIXED)
+    const double *sgl64;
+    const float *sgl_hi, *sgl_lo;
     // COUNT outputs
     uint32_t *row_count;
     uint32_t *upper_off;
@@ -29,9 +34,6 @@ struct FciParams {
     double *val64;
     float *val32;
     float *val32lo;  // v - (double)hi, rounded to FP32 (FP32 fill only)
-    // MATVEC
-    const double *x;
-    double *y;
 };
 
 struct DociParams {
@@ -49,8 +51,6 @@ struct DociParams {
     double *val64;
     float *val32;
     float *val32lo;
-    const double *x;
-    double *y;
 };
 
 __host__ __device__ inline int64_t d_binom(int n, int k) {
@@ -70,6 +70,9 @@ __device__ __forceinline__ int nth_set(uint64_t x, int a) {
 size_t fci_smem_bytes(const FciParams &p);
 void fci_launch(int mode, const FciParams &p, cudaStream_t s);
 void fci_diag_launch(const FciParams &p, double *diag, cudaStream_t s);
+// Row singles table (and FP32 splits of it and of diag when hi/lo are non-null).
+void fci_singles_launch(const FciParams &p, double *sgl64, float *sgl_hi, float *sgl_lo, float *diag_hi,
+                        float *diag_lo, cudaStream_t s);
 size_t doci_smem_bytes(int W, int warps);
 void doci_strings_launch(int L, int n, int64_t D, uint64_t *strings, cudaStream_t s);
 void doci_diag_launch(const DociParams &p, double *diag, cudaStream_t s);

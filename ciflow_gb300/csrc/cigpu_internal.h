@@ -83,7 +83,7 @@ void DevBuf<T>::alloc(size_t count) {
 // Strings are ranked in colex order, the order of Permutator_Bit
 // (Permutator.cpp:113-153) and of determine_weight (CIMethod.cpp:689-747).
 // FP32 split (hi = fl32(v), lo = fl32(v - hi)); both zero when |v| <= 1e-14.
-inline void split_fp32(double v, float &hi, float &lo) {
+__host__ __device__ inline void split_fp32(double v, float &hi, float &lo) {
     if (!(v > kZero || v < -kZero)) {
         hi = lo = 0.0f;
         return;

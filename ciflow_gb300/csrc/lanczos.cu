@@ -528,19 +528,28 @@ struct TRLanczos {
         j = 0;
     }
 
-    // One Lanczos step: expand V[j] -> V[j+1]. Returns the new beta.
-    double step() {
+    // One Lanczos step, split in two so the next step can run on the device while
+    // the host analyses the projected matrix: enqueue() expands V[j] -> V[j+1] and
+    // queues the copy of the coefficients; finish() waits and records them.
+    static constexpr int H1 = 0, H2 = kMaxBasis + 1, NR = 2 * (kMaxBasis + 1);
+    void enqueue() {
         VT *w = vec(j + 1);
         mv(vec(j), w, s);
         ++matvecs;
         const int nv = j + 1;
-        const int H1 = 0, H2 = kMaxBasis + 1, NR = 2 * (kMaxBasis + 1);
         ops.dots(V.p, n, nv, w, n, H1);
         ops.update(V.p, n, nv, H1, w, n, -1);
         ops.dots(V.p, n, nv, w, n, H2);
         ops.update(V.p, n, nv, H2, w, n, NR);
         ops.scale(w, n, NR);
-        const double *h = ops.fetch(NR + 1);
+        CIGPU_CUDA(cudaMemcpyAsync(ops.h_out, ops.out.p, sizeof(double) * (NR + 1), cudaMemcpyDeviceToHost, s));
+    }
+    double finish() {
+        const double t0 = wall();
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+        g_clk.wait += wall() - t0;
+        ++g_clk.n_wait;
+        const double *h = ops.h_out;
         for (int i = 0; i <= j; ++i) {
             const double v = h[H1 + i] + h[H2 + i];
             t(i, j) = v;
@@ -551,6 +560,10 @@ struct TRLanczos {
         t(j, j + 1) = beta;
         ++j;
         return beta;
+    }
+    double step() {
+        enqueue();
+        return finish();
     }
 
     // Ritz analysis of T[0..j); updates theta0/theta1/y0/resid_est.
@@ -603,39 +616,51 @@ struct TRLanczos {
 
     // Iterate until resid_est <= max(abs_target, rel_target * max(1, |theta0|)), the
     // matvec budget is spent, breakdown, or stagnation (no 10% gain in 3 cycles).
-    // Returns true when the target was met.
+    // The step after the current one is already running on the device while the host
+    // diagonalises T; when the target is met that speculative step is discarded
+    // (V[0..j) and T are untouched by it). Returns true when the target was met.
     bool run(double abs_target, double rel_target, int64_t budget) {
-        using clk = std::chrono::steady_clock;
-        int check_every = 1, since = 0;
         double best = 1e300;
         int64_t best_at = matvecs;
         auto target = [&] { return std::max(abs_target, rel_target * std::max(1.0, std::fabs(theta0))); };
-        while (matvecs < budget) {
-            const auto t0 = clk::now();
-            const double beta = step();
-            const auto t1 = clk::now();
-            ++since;
-            const bool full = (j == m) || (j >= n);
+        bool inflight = false;
+        if (matvecs < budget && j < m && j < n) {
+            enqueue();
+            inflight = true;
+        }
+        while (inflight) {
+            const double beta = finish();
+            inflight = false;
             const bool breakdown = beta <= 1e-13 * std::max(1.0, std::fabs(theta0));
-            if (since >= check_every || full || breakdown) {
-                analyse();
-                const auto t2 = clk::now();
-                since = 0;
-                // keep the host eigensolve under ~10% of the device step time
-                const double ts = std::chrono::duration<double>(t1 - t0).count();
-                const double te = std::chrono::duration<double>(t2 - t1).count();
-                check_every = std::max(1, std::min(8, (int)(te / std::max(ts * 0.1, 1e-9))));
-                if (breakdown) resid_est = 0.0;
-                if (resid_est <= target()) return true;
+            if (!breakdown && j < m && j < n && matvecs < budget) {
+                enqueue();  // overlaps with the analysis below
+                inflight = true;
+            }
+            analyse();
+            if (breakdown) resid_est = 0.0;
+            bool stop = resid_est <= target();
+            if (!stop) {
                 if (resid_est < 0.9 * best) {
                     best = resid_est;
                     best_at = matvecs;
                 } else if (matvecs - best_at > 3 * m) {
-                    return false;  // stagnated (e.g. at the FP32 accuracy floor)
+                    stop = true;  // stagnated
                 }
             }
-            if (j >= n) return true;  // the whole space is spanned
-            if (j == m) restart();
+            if (stop || j >= n || breakdown) {
+                if (inflight) {  // discard the speculative step
+                    CIGPU_CUDA(cudaStreamSynchronize(s));
+                    inflight = false;
+                }
+                return resid_est <= target() || j >= n;
+            }
+            if (!inflight && j == m) {
+                restart();
+                if (matvecs < budget) {
+                    enqueue();
+                    inflight = true;
+                }
+            }
         }
         analyse();
         return resid_est <= target();
