@@ -61,6 +61,7 @@ SIGNATURES = {
     "cigpu_mvprod_device": (_I, [_P, _P, _P, _I, _P]),
     "cigpu_solve": (_I, [_P, _D, _I64, _P, _P, _P]),
     "cigpu_rdm": (_I, [_P, _P, _P, _P, _P, _P]),
+    "cigpu_rdm_doci_noalloc": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "cigpu_server_create": (_I, [_I, ctypes.c_size_t, _I, _I, _P]),
     "cigpu_server_submit": (_I, [_P, _P, _P]),
     "cigpu_server_poll": (_I, [_P, ctypes.c_uint64, _I, _P, _P, _P]),

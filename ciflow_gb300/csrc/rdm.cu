@@ -28,6 +28,7 @@
 // Storage follows CIDens: the 1-RDM and each 2-RDM block are symmetric pair
 // matrices (Vector2d, matrix.cpp:674-690), accumulated on (min, max) and mirrored.
 #include <algorithm>
+#include <mutex>
 #include <stdexcept>
 
 #include "crs.cuh"
@@ -566,3 +567,83 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
 }
 
 }  // namespace cigpu
+
+// ---------------------------------------------------------------------------
+// DOCI RDMs without any device allocation (cigpu_rdm_doci_noalloc).
+//
+// Some callers cannot allocate device memory at the point where they need the
+// RDMs: a host framework that hands out all device memory from its own fixed
+// pool and forbids cudaMalloc on its request path, or a latency-bound loop where
+// the implicit device synchronisation of cudaMalloc/cudaFree would stall work
+// queued by others. For them the per-block partial sums of the DOCI RDM kernel
+// live in a fixed array inside this library instead of in allocated scratch.
+//
+// The array below is file-scope device memory: every GPU that loads the library
+// holds it (4 MiB) until the process exits. Host code must not take its name as
+// a device address; the address is looked up once per device with
+// cudaGetSymbolAddress (on the first call on that device, which should therefore
+// come before any stream capture). Every call shares the array and leaves its
+// contents behind: calls that overlap on the GPU race on it.
+namespace cigpu {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;  // 4 MiB
+constexpr int kNoAllocMaxBlocks = 256;
+
+static __device__ __align__(256) double g_doci_rdm_scratch[kNoAllocScratchBytes / sizeof(double)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double *g_scratch_addr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set up once per device).
+cudaError_t scratch_address(double **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_doci_rdm_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace cigpu
+
+extern "C" int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa,
+                                      double *rdm2_ab, double *rdm2_bb, cigpu_stream stream) {
+    using namespace cigpu;
+    if (!crs || !c || !rdm1 || !rdm2_aa || !rdm2_ab || !rdm2_bb) return CIGPU_EINVAL;
+    if (crs->method != CIGPU_DOCI) return CIGPU_EINVAL;
+    const int L = crs->L, np = L * (L - 1) / 2;
+    const int64_t L2 = (int64_t)L * L;
+    // one thread per orbital pair (j, k) and 2 L^2 partial sums per block must fit
+    if (L2 > 1024) return CIGPU_ENOTSUP;
+    const int G = (int)std::min<int64_t>(kNoAllocMaxBlocks, kNoAllocScratchBytes / (sizeof(double) * 2 * L2));
+    if (G < 1) return CIGPU_ENOTSUP;
+    double *scratch = nullptr;
+    cudaError_t e = scratch_address(&scratch);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "cigpu: scratch address lookup failed: %s\n", cudaGetErrorString(e));
+        return CIGPU_ECUDA;
+    }
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : crs->stream;
+    // the finishing kernel only writes the nonzero DOCI entries: clear the outputs
+    if (cudaMemsetAsync(rdm1, 0, sizeof(double) * 2 * L2, s) != cudaSuccess ||
+        cudaMemsetAsync(rdm2_aa, 0, sizeof(double) * np * np, s) != cudaSuccess ||
+        cudaMemsetAsync(rdm2_bb, 0, sizeof(double) * np * np, s) != cudaSuccess ||
+        cudaMemsetAsync(rdm2_ab, 0, sizeof(double) * L2 * L2, s) != cudaSuccess)
+        return CIGPU_ECUDA;
+    const int th = (int)((L2 + 31) / 32 * 32);
+    k_doci_rdm<<<G, th, 0, s>>>(c, crs->strings.p, crs->dim, L, crs->nup, scratch);
+    k_doci_rdm_finish<<<(int)((L2 + 255) / 256), 256, 0, s>>>(scratch, G, L, np, rdm1, rdm2_aa, rdm2_ab, rdm2_bb);
+    if (cudaGetLastError() != cudaSuccess) return CIGPU_ECUDA;
+    count_launch(2);
+    return CIGPU_OK;
+}

@@ -130,6 +130,20 @@ int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0
  *   rdm2_ab [L*L][L*L]     = get_two_rdm(1, p, q, r, s) at (p*L+q, r*L+s) ---- */
 int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa, double *rdm2_ab, double *rdm2_bb);
 
+/* ---- DOCI RDMs without device allocation. No counterpart in the reference.
+ * For callers that cannot allocate device memory on their request path (a host
+ * framework that owns all device memory through its own fixed pool, or a
+ * latency-bound loop that cannot afford the device synchronisation cudaMalloc
+ * implies): the block partial sums live in a fixed 4 MiB array inside the
+ * library, so this call allocates nothing. crs must be a DOCI CRS with L <= 32
+ * (CIGPU_ENOTSUP otherwise). c (dim) and the outputs, laid out as in cigpu_rdm,
+ * are DEVICE buffers; the work is queued on `stream` (NULL: the CRS stream) and
+ * the call returns without waiting. The first call on a device looks up the
+ * array's device address; make it before any stream capture. Calls share the
+ * array: calls that overlap on the GPU race, so serialise them. ---- */
+int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa, double *rdm2_ab,
+                           double *rdm2_bb, cigpu_stream stream);
+
 /* ---- serving: continuous batching of independent solves (the served analogue of
  * the set_ham -> solve loop of the orbital optimisers, SimulatedAnnealing.cpp:72-86,
  * 130-134; CIMethod::set_ham CIMethod.cpp:117-126). Requests are admitted as
