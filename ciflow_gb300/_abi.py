@@ -115,3 +115,10 @@ def device_count() -> int:
     n = ctypes.c_int(0)
     lib().cigpu_device_count(ctypes.byref(n))
     return n.value
+
+
+def estimate_bytes(L: int, nup: int, ndown: int, method: int, precision: int) -> int:
+    """Device bytes a solve of this shape needs (the server's admission estimate)."""
+    b = ctypes.c_size_t()
+    check(lib().cigpu_estimate_bytes(L, nup, ndown, method, precision, ctypes.byref(b)), "cigpu_estimate_bytes")
+    return b.value

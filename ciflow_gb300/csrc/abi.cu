@@ -2,6 +2,8 @@
 // export, matvec and solve entry points.
 #include <chrono>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -15,13 +17,80 @@ namespace cigpu {
 
 std::atomic<int64_t> g_launches{0};
 
-void *dev_alloc(size_t bytes) {
-    void *p = nullptr;
-    if (cudaMalloc(&p, bytes) != cudaSuccess) {
-        cudaGetLastError();  // clear the sticky-free allocation error
-        throw std::bad_alloc();
+// ---- caching device allocator ----
+// Blocks are rounded up to 2 MiB (small requests to a power of two of at least
+// 256 bytes) and kept per rounded size after release. A failed cudaMalloc
+// returns every cached block to the driver and retries once.
+namespace {
+std::mutex g_alloc_mutex;
+std::multimap<size_t, void *> g_free_blocks;  // rounded size -> block (current device)
+std::map<void *, size_t> g_block_size;        // every live or cached block -> rounded size
+size_t g_cached_bytes = 0, g_live_bytes = 0;
+constexpr size_t kMaxCachedBytes = size_t(96) << 30;
+
+size_t round_block(size_t bytes) {
+    if (bytes >= (size_t(2) << 20)) return (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+    size_t r = 256;
+    while (r < bytes) r <<= 1;
+    return r;
+}
+
+void release_cache_locked() {
+    for (auto &kv : g_free_blocks) {
+        cudaFree(kv.second);
+        g_block_size.erase(kv.second);
     }
+    g_free_blocks.clear();
+    g_cached_bytes = 0;
+}
+}  // namespace
+
+void *dev_alloc(size_t bytes) {
+    const size_t rb = round_block(bytes);
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    // best fit among cached blocks, wasting at most a quarter
+    auto it = g_free_blocks.lower_bound(rb);
+    if (it != g_free_blocks.end() && it->first <= rb + rb / 4) {
+        void *p = it->second;
+        const size_t got = it->first;
+        g_free_blocks.erase(it);
+        g_cached_bytes -= got;
+        g_live_bytes += got;
+        return p;
+    }
+    void *p = nullptr;
+    if (cudaMalloc(&p, rb) != cudaSuccess) {
+        cudaGetLastError();
+        release_cache_locked();
+        if (cudaMalloc(&p, rb) != cudaSuccess) {
+            cudaGetLastError();  // clear the allocation error
+            throw std::bad_alloc();
+        }
+    }
+    g_block_size[p] = rb;
+    g_live_bytes += rb;
     return p;
+}
+
+void dev_free(void *p, size_t) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    auto it = g_block_size.find(p);
+    if (it == g_block_size.end()) return;
+    const size_t rb = it->second;
+    g_live_bytes -= rb;
+    if (g_cached_bytes + rb > kMaxCachedBytes) {
+        cudaFree(p);
+        g_block_size.erase(it);
+        return;
+    }
+    g_free_blocks.emplace(rb, p);
+    g_cached_bytes += rb;
+}
+
+size_t dev_bytes_in_use() {
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    return g_live_bytes;
 }
 
 void SpinDevStore::upload(const SpinTables &t, cudaStream_t s) {
@@ -232,6 +301,40 @@ void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
     spmv_f32(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, x, y, s);
 }
 
+// Host validation of integrals: finite, h symmetric, eri 8-fold symmetric to 1e-10
+// relative. *exact reports whether eri is exactly symmetric already.
+int validate_integrals(int L, const double *h, const double *eri, bool *exact_out) {
+    const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
+    double hmax = 0, emax = 0;
+    for (size_t i = 0; i < L2; ++i) {
+        if (!std::isfinite(h[i])) return CIGPU_EINVAL;
+        hmax = std::max(hmax, std::fabs(h[i]));
+    }
+    for (size_t i = 0; i < L4; ++i) {
+        if (!std::isfinite(eri[i])) return CIGPU_EINVAL;
+        emax = std::max(emax, std::fabs(eri[i]));
+    }
+    const double htol = 1e-10 * std::max(1.0, hmax), etol = 1e-10 * std::max(1.0, emax);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j)
+            if (std::fabs(h[i * L1 + j] - h[j * L1 + i]) > htol) return CIGPU_EINVAL;
+    bool exact = true;
+    for (int p = 0; p < L; ++p)
+        for (int q = 0; q < L; ++q)
+            for (int r = 0; r < L; ++r)
+                for (int s = 0; s < L; ++s) {
+                    const double v = eri[p * L3 + q * L2 + r * L1 + s];
+                    const double a = eri[q * L3 + p * L2 + r * L1 + s];
+                    const double b = eri[r * L3 + s * L2 + p * L1 + q];
+                    const double c = eri[p * L3 + q * L2 + s * L1 + r];
+                    if (std::fabs(v - a) > etol || std::fabs(v - b) > etol || std::fabs(v - c) > etol)
+                        return CIGPU_EINVAL;
+                    exact = exact && v == a && v == b && v == c;
+                }
+    if (exact_out) *exact_out = exact;
+    return CIGPU_OK;
+}
+
 }  // namespace cigpu
 
 using namespace cigpu;
@@ -279,33 +382,8 @@ int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, 
     if (L < 1 || L > kMaxL || nup < 0 || ndown < 0 || nup > L || ndown > L) return CIGPU_EINVAL;
     if (!std::isfinite(econst)) return CIGPU_EINVAL;
     const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
-    // host validation: finite, h symmetric, eri 8-fold symmetric (relative 1e-10)
-    double hmax = 0, emax = 0;
-    for (size_t i = 0; i < L2; ++i) {
-        if (!std::isfinite(h[i])) return CIGPU_EINVAL;
-        hmax = std::max(hmax, std::fabs(h[i]));
-    }
-    for (size_t i = 0; i < L4; ++i) {
-        if (!std::isfinite(eri[i])) return CIGPU_EINVAL;
-        emax = std::max(emax, std::fabs(eri[i]));
-    }
-    const double htol = 1e-10 * std::max(1.0, hmax), etol = 1e-10 * std::max(1.0, emax);
-    for (int i = 0; i < L; ++i)
-        for (int j = 0; j < L; ++j)
-            if (std::fabs(h[i * L1 + j] - h[j * L1 + i]) > htol) return CIGPU_EINVAL;
     bool exact = true;
-    for (int p = 0; p < L; ++p)
-        for (int q = 0; q < L; ++q)
-            for (int r = 0; r < L; ++r)
-                for (int s = 0; s < L; ++s) {
-                    const double v = eri[p * L3 + q * L2 + r * L1 + s];
-                    const double a = eri[q * L3 + p * L2 + r * L1 + s];
-                    const double b = eri[r * L3 + s * L2 + p * L1 + q];
-                    const double c = eri[p * L3 + q * L2 + s * L1 + r];
-                    if (std::fabs(v - a) > etol || std::fabs(v - b) > etol || std::fabs(v - c) > etol)
-                        return CIGPU_EINVAL;
-                    exact = exact && v == a && v == b && v == c;
-                }
+    if (validate_integrals(L, h, eri, &exact) != CIGPU_OK) return CIGPU_EINVAL;
     CIGPU_TRY
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

@@ -568,13 +568,13 @@ void doci_diag_launch(const DociParams &p, double *diag, cudaStream_t s) {
 void doci_launch(int mode, const DociParams &p, cudaStream_t s) {
     const int warps = kDociThreads / 32;
     const size_t sm = doci_smem_bytes(p.W, warps);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_doci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_doci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(k_doci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
+        return true;
+    }();
+    (void)attr_set;
     const int blocks = grid_for(p.D * 32, kDociThreads, 16);
     switch (mode) {
         case kCount: k_doci_rows<kCount><<<blocks, kDociThreads, sm, s>>>(p); break;
@@ -694,12 +694,12 @@ void exclusive_scan_u32(const uint32_t *in, int64_t *out, int64_t n, cudaStream_
 }
 
 int sm_count() {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {  // thread-safe one-time init
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
-    }
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        return n;
+    }();
     return sms;
 }
 

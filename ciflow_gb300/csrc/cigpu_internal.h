@@ -33,7 +33,16 @@ struct CudaError {
         if (e_ != cudaSuccess) throw ::cigpu::CudaError{e_, #call};            \
     } while (0)
 
-// Device buffer with RAII; allocation failure throws std::bad_alloc.
+void *dev_alloc(size_t bytes);          // throws std::bad_alloc on failure
+void dev_free(void *p, size_t bytes);   // returns the block to the cache
+// Bytes currently held by live DevBufs (not counting the cache).
+size_t dev_bytes_in_use();
+
+// Device buffer with RAII; allocation failure throws std::bad_alloc. Blocks come
+// from a caching allocator: cudaFree synchronises the whole device, which would
+// serialise concurrent solves on different streams. Every release in this
+// library happens after the stream that used the block has synchronised, so a
+// cached block can be handed out again at once.
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -50,14 +59,12 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void alloc(size_t count);
     void release() {
-        if (p) cudaFree(p);
+        if (p) dev_free(p, n * sizeof(T));
         p = nullptr;
         n = 0;
     }
     size_t bytes() const { return n * sizeof(T); }
 };
-
-void *dev_alloc(size_t bytes);  // throws std::bad_alloc on failure
 
 // Phase timer: with CIGPU_TRACE=1 in the environment, mark() synchronises the
 // stream and prints the time since the previous mark to stderr.

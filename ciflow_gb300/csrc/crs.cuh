@@ -44,4 +44,6 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision);
 // RDMs of device vector c (normalised); host outputs as in cigpu_rdm.
 void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s);
 int status_from_exception();
+// CIGPU_EINVAL unless h is symmetric and eri 8-fold symmetric (1e-10 relative) and all finite.
+int validate_integrals(int L, const double *h, const double *eri, bool *exact);
 }  // namespace cigpu

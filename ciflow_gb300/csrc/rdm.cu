@@ -546,8 +546,10 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
         if (np > 0) {
             const size_t sm = sizeof(double) * 2 * (size_t)tb.D;
             if (sm > 200 * 1024) throw std::invalid_argument("FCI RDM: beta string space too large");
-            if (sm > 48 * 1024)
-                CIGPU_CUDA(cudaFuncSetAttribute(k_ab_doubles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            // one fixed limit, set once: concurrent callers (server workers) must never lower it
+            static const cudaError_t attr =
+                cudaFuncSetAttribute(k_ab_doubles, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            CIGPU_CUDA(attr);
             const int th = std::min(1024, (int)((L2 + 31) / 32 * 32));
             k_ab_doubles<<<np * nsplit, th, sm, s>>>(c_dev, tb.D, app.p, apd.p, aps.p, bxp.p, bxd.p,
                                                                       bxs.p, L, nsplit, slices.p);

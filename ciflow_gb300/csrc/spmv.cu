@@ -123,12 +123,12 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_hilo(int64_t n, const int
 int spmv_grid() { return sm_count_spmv() * kSpmvBlocksPerSM; }
 
 int sm_count_spmv() {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {  // thread-safe one-time init
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
-    }
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        return n;
+    }();
     return sms;
 }
 

@@ -1,0 +1,141 @@
+"""Served solve stream: open-loop Poisson arrivals into the continuous-batching server.
+
+The stream is the L=10 5a5b FCI problem (63,504 determinants) under random
+orbital rotations U = exp(kappa) of one seeded base integral set, as in an
+orbital-optimisation sweep (CIFlow SimulatedAnnealing.cpp:72-86, 130-134), mixed
+with uneven problems of the batched-solve shape (L uniform in 6..12, FCI with
+1..L/2 electrons per spin or DOCI with 2..L/2 pairs) and a few L=12 6a6b
+requests. The same request list runs through the mixed FP32/FP64 form and the
+plain FP64 form; every mixed result carries |dE0| against the plain FP64 result
+of the same request, solved to a tighter tolerance.
+
+    python -m ciflow_gb300.serve_bench --rate 1000 --requests 300
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import threading
+import time
+
+import numpy as np
+
+from . import _abi as A
+from .server import Server
+from .synthetic import make_integrals, rotate_integrals
+
+
+def make_stream(n: int, seed: int = 4, frac_other: float = 0.15, every_big: int = 100):
+    """Request list [(kind, ints, method)], deterministic in `seed`."""
+    rng = np.random.default_rng(seed + 17)
+    base = make_integrals(10, 5, 5, nchol=16, seed=seed)
+    big = None
+    out = []
+    for i in range(n):
+        if every_big and i % every_big == every_big // 2:
+            if big is None:
+                big = make_integrals(12, 6, 6, nchol=16, seed=1)
+            out.append(("c1", big, A.FCI))
+        elif rng.random() < frac_other:
+            L = int(rng.integers(6, 13))
+            if rng.random() < 0.5:
+                ne = int(rng.integers(1, L // 2 + 1))
+                out.append(("c3", make_integrals(L, ne, ne, nchol=16, seed=1000 + i), A.FCI))
+            else:
+                p = int(rng.integers(2, L // 2 + 1))
+                out.append(("c3", make_integrals(L, p, p, nchol=16, seed=1000 + i), A.DOCI))
+        else:
+            out.append(("c4", rotate_integrals(base, 0.05, seed=10**6 + i), A.FCI))
+    return out
+
+
+def pct(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def run_stream(stream, precision: int, rate: float, tol: float, max_inflight: int, seed: int = 0):
+    """Submits `stream` at Poisson arrival times; returns per-request results and the wall time."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(stream)) if rate > 0 else np.zeros(len(stream))
+    with Server(max_inflight=max_inflight, max_queue=1 << 16) as srv:
+        # warm-up: one request of each kind builds the allocator cache and kernel state
+        seen = set()
+        for kind, ints, m in stream:
+            if kind not in seen:
+                seen.add(kind)
+                srv.wait(srv.submit(ints, method=m, precision=precision, tol=tol))
+        ids = [None] * len(stream)
+        results = [None] * len(stream)
+        t0 = time.perf_counter()
+
+        def submitter():
+            t = t0
+            for i, (kind, ints, m) in enumerate(stream):
+                t += gaps[i]
+                d = t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                ids[i] = srv.submit(ints, method=m, precision=precision, tol=tol)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        for i, rid in enumerate(ids):
+            results[i] = srv.wait(rid)
+        wall = time.perf_counter() - t0
+    return results, wall
+
+
+def summarise(stream, results, wall):
+    lat = {"all": [r["latency_s"] for r in results]}
+    for k in ("c4", "c3", "c1"):
+        lat[k] = [r["latency_s"] for (kind, _, _), r in zip(stream, results) if kind == k]
+    ok = sum(r["status"] == A.OK for r in results)
+    return {
+        "solves_per_s": len(results) / wall,
+        "wall_s": wall,
+        "ok": ok,
+        "p50_ms": {k: (pct(v, 50) * 1e3 if v else None) for k, v in lat.items()},
+        "p99_ms": {k: (pct(v, 99) * 1e3 if v else None) for k, v in lat.items()},
+        "counts": {k: len(v) for k, v in lat.items()},
+        "matvecs_fp32": int(sum(r["matvecs_fp32"] for r in results)),
+        "matvecs_fp64": int(sum(r["matvecs_fp64"] for r in results)),
+    }
+
+
+def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed: float = 1e-5,
+           tol_fp64: float = 1e-5, tol_ref: float = 1e-8, every_big: int = 100, seed: int = 4,
+           ref_results=None):
+    """Both forms over the same stream; the tighter FP64 pass gives each request's E0."""
+    stream = make_stream(n, seed=seed, every_big=every_big)
+    res_m, wall_m = run_stream(stream, A.MIXED, rate, tol_mixed, max_inflight, seed=seed)
+    res_p, wall_p = run_stream(stream, A.FP64, rate, tol_fp64, max_inflight, seed=seed)
+    if ref_results is None:
+        ref_results, _ = run_stream(stream, A.FP64, 0.0, tol_ref, max_inflight, seed=seed)
+    e_ref = np.array([r["e0"] for r in ref_results])
+    dm = np.abs(np.array([r["e0"] for r in res_m]) - e_ref)
+    dp = np.abs(np.array([r["e0"] for r in res_p]) - e_ref)
+    out = {
+        "requests": n, "arrival_rate_per_s": rate, "max_inflight": max_inflight,
+        "mix": {k: sum(1 for s in stream if s[0] == k) for k in ("c4", "c3", "c1")},
+        "dims": {"min": min(r["dim"] for r in res_m), "max": max(r["dim"] for r in res_m)},
+        "mixed": summarise(stream, res_m, wall_m) | {"max_abs_dE0": float(dm.max()), "tol": tol_mixed},
+        "plain_fp64": summarise(stream, res_p, wall_p) | {"max_abs_dE0": float(dp.max()), "tol": tol_fp64},
+    }
+    out["mixed_over_plain_solves_per_s"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=300)
+    ap.add_argument("--rate", type=float, default=1000.0)
+    ap.add_argument("--inflight", type=int, default=8)
+    ap.add_argument("--tol", type=float, default=1e-5)
+    ap.add_argument("--every-big", type=int, default=100)
+    a = ap.parse_args()
+    print(json.dumps(served(a.requests, a.rate, a.inflight, a.tol, a.tol, every_big=a.every_big)))
+
+
+if __name__ == "__main__":
+    main()

@@ -66,3 +66,16 @@ def test_estimate_bytes(lib):
     lib.cigpu_estimate_bytes(12, 6, 6, A.FCI, A.MIXED, ctypes.byref(b32))
     assert b32.value < b.value
     assert lib.cigpu_estimate_bytes(12, 6, 6, 7, A.FP64, ctypes.byref(b)) == A.EINVAL
+
+
+def test_server_arguments_checked_on_host(lib):
+    out = ctypes.c_void_p()
+    assert lib.cigpu_server_create(0, 0, 0, 16, ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_server_create(0, 0, 4, 0, ctypes.byref(out)) == A.EINVAL
+    assert lib.cigpu_server_create(-1, 0, 4, 16, ctypes.byref(out)) in (A.ECUDA, A.EINVAL)
+    assert lib.cigpu_server_submit(None, None, None) == A.EINVAL
+    assert lib.cigpu_server_poll(None, 1, 0, None, None, None) == A.EINVAL
+    assert lib.cigpu_server_cancel(None, 1) == A.EINVAL
+    assert lib.cigpu_server_destroy(None) == A.OK
+    if A.device_count() == 0:  # no GPU: refused, never a crash
+        assert lib.cigpu_server_create(0, 0, 4, 16, ctypes.byref(out)) == A.ECUDA

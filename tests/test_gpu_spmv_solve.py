@@ -11,6 +11,7 @@ import pytest
 import oracle as O
 from ciflow_gb300 import _abi as A
 from ciflow_gb300.ciflow import DOCI, FCI, Hamiltonian
+from ciflow_gb300.synthetic import make_integrals
 from tests.helpers import beh2_integrals, integrals, load_golden
 
 pytestmark = pytest.mark.gpu
@@ -117,3 +118,22 @@ def test_matvec_limit_reports_no_convergence():
     cim.solve(tol=1e-12, max_matvec=5)
     assert cim.info["status"] == A.ENOCONV
     assert not cim.info["converged"]
+
+
+# uneven shapes of the batched/served mix, down to spaces smaller than the Krylov basis
+SMALL_SHAPES = [(O.FCI, 4, 0, 0), (O.FCI, 3, 1, 1), (O.DOCI, 6, 2, 2), (O.FCI, 6, 1, 1), (O.FCI, 5, 2, 1),
+                (O.DOCI, 8, 3, 3), (O.FCI, 6, 3, 2), (O.FCI, 7, 2, 2)]
+
+
+@pytest.mark.parametrize("shape", SMALL_SHAPES, ids=lambda s: "%s-L%d-%d-%d" % (("FCI", "DOCI")[s[0]], *s[1:]))
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_small_spaces_match_dense_eigensolve(shape, precision):
+    method, L, na, nb = shape
+    ints = make_integrals(L, na, nb, nchol=16, seed=100 + L * 10 + na)
+    ref = O.build_upper(method, ints)
+    e_ref = np.linalg.eigvalsh(ref.full_csr().toarray())[0]
+    cim = build(DOCI if method == O.DOCI else FCI, ints, precision)
+    cim.solve(tol=1e-9)
+    tol = 1e-8 if precision == A.FP64 else 1e-6
+    assert abs(cim.get_ci_energy() - ints.econst - e_ref) <= tol
+    assert cim.info["converged"]
