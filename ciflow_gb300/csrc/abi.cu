@@ -9,6 +9,7 @@
 #include <memory>
 #include <new>
 #include <stdexcept>
+#include <vector>
 
 #include "crs.cuh"
 #include "spmv.cuh"
@@ -19,14 +20,26 @@ std::atomic<int64_t> g_launches{0};
 
 // ---- caching device allocator ----
 // Blocks are rounded up to 2 MiB (small requests to a power of two of at least
-// 256 bytes) and kept per rounded size after release. A failed cudaMalloc
-// returns every cached block to the driver and retries once.
+// 256 bytes) and kept per rounded size after release. A released block carries
+// an event recorded on the releasing thread's stream (StreamScope); it is handed
+// out again at once on that same stream, and to any other stream only once the
+// event has completed, so concurrent solves on different streams never share a
+// block that pending work still touches. A failed cudaMalloc returns every cached
+// block to the driver and retries once.
 namespace {
+struct Cached {
+    void *p;
+    cudaEvent_t ev;   // completes when the releasing stream's work on the block is done
+    cudaStream_t st;  // the releasing stream
+};
 std::mutex g_alloc_mutex;
-std::multimap<size_t, void *> g_free_blocks;  // rounded size -> block (current device)
+std::multimap<size_t, Cached> g_free_blocks;  // rounded size -> block (current device)
 std::map<void *, size_t> g_block_size;        // every live or cached block -> rounded size
+std::vector<cudaEvent_t> g_event_pool;
 size_t g_cached_bytes = 0, g_live_bytes = 0;
 constexpr size_t kMaxCachedBytes = size_t(96) << 30;
+thread_local cudaStream_t tls_stream = nullptr;
+thread_local bool tls_stream_set = false;
 
 size_t round_block(size_t bytes) {
     if (bytes >= (size_t(2) << 20)) return (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
@@ -35,24 +48,49 @@ size_t round_block(size_t bytes) {
     return r;
 }
 
+void recycle_event_locked(cudaEvent_t ev) {
+    if (ev) g_event_pool.push_back(ev);
+}
+
+bool reusable(const Cached &c) {
+    if (!c.ev) return true;
+    if (tls_stream_set && c.st == tls_stream) return true;  // stream order covers it
+    const cudaError_t q = cudaEventQuery(c.ev);
+    if (q == cudaSuccess) return true;
+    if (cudaPeekAtLastError() == q) cudaGetLastError();  // "not ready" is not an error here
+    return false;
+}
+
 void release_cache_locked() {
     for (auto &kv : g_free_blocks) {
-        cudaFree(kv.second);
-        g_block_size.erase(kv.second);
+        cudaFree(kv.second.p);  // synchronises the device: pending users are done
+        g_block_size.erase(kv.second.p);
+        recycle_event_locked(kv.second.ev);
     }
     g_free_blocks.clear();
     g_cached_bytes = 0;
 }
 }  // namespace
 
+StreamScope::StreamScope(cudaStream_t s, bool set) : prev(tls_stream), prev_set(tls_stream_set) {
+    tls_stream = s;
+    tls_stream_set = set;
+}
+
+StreamScope::~StreamScope() {
+    tls_stream = prev;
+    tls_stream_set = prev_set;
+}
+
 void *dev_alloc(size_t bytes) {
     const size_t rb = round_block(bytes);
     std::lock_guard<std::mutex> lock(g_alloc_mutex);
     // best fit among cached blocks, wasting at most a quarter
-    auto it = g_free_blocks.lower_bound(rb);
-    if (it != g_free_blocks.end() && it->first <= rb + rb / 4) {
-        void *p = it->second;
+    for (auto it = g_free_blocks.lower_bound(rb); it != g_free_blocks.end() && it->first <= rb + rb / 4; ++it) {
+        if (!reusable(it->second)) continue;
+        void *p = it->second.p;
         const size_t got = it->first;
+        recycle_event_locked(it->second.ev);
         g_free_blocks.erase(it);
         g_cached_bytes -= got;
         g_live_bytes += got;
@@ -84,7 +122,26 @@ void dev_free(void *p, size_t) {
         g_block_size.erase(it);
         return;
     }
-    g_free_blocks.emplace(rb, p);
+    Cached c{p, nullptr, nullptr};
+    if (tls_stream_set) {
+        if (!g_event_pool.empty()) {
+            c.ev = g_event_pool.back();
+            g_event_pool.pop_back();
+        } else if (cudaEventCreateWithFlags(&c.ev, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            c.ev = nullptr;
+        }
+        if (c.ev && cudaEventRecord(c.ev, tls_stream) != cudaSuccess) {
+            cudaGetLastError();
+            recycle_event_locked(c.ev);
+            c.ev = nullptr;
+        }
+        c.st = tls_stream;
+        if (!c.ev) cudaStreamSynchronize(tls_stream);
+    } else {
+        cudaDeviceSynchronize();  // unknown stream: wait as cudaFree would
+    }
+    g_free_blocks.emplace(rb, c);
     g_cached_bytes += rb;
 }
 
@@ -288,8 +345,9 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         spmv_f64(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
         return;
     }
-    if (c.val32lo.p) {
-        // MIXED CRS: FP64 product with values hi + lo (|v - hi - lo| <= 2^-48 |v|)
+    if (c.val32lo.p || c.nnz_full == 0) {
+        // MIXED CRS: FP64 product with values hi + lo (|v - hi - lo| <= 2^-48 |v|);
+        // an all-zero matrix (e.g. no electrons) has no value arrays at all
         spmv_hilo(c.dim, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
         return;
     }
@@ -385,6 +443,7 @@ int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, 
     bool exact = true;
     if (validate_integrals(L, h, eri, &exact) != CIGPU_OK) return CIGPU_EINVAL;
     CIGPU_TRY
+    StreamScope scope(nullptr, false);  // synchronous copies below: reuse only completed blocks
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -468,6 +527,7 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
         CIGPU_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         c->own_stream = true;
     }
+    StreamScope scope(c->stream);
     build_crs(*c, c->stream);
     *out = c.release();
     return CIGPU_OK;
@@ -475,8 +535,16 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
 }
 
 int cigpu_crs_destroy(cigpu_crs *crs) {
-    if (crs && crs->stream) cudaStreamSynchronize(crs->stream);
-    delete crs;
+    if (!crs) return CIGPU_OK;
+    if (crs->stream) cudaStreamSynchronize(crs->stream);
+    {
+        StreamScope scope(crs->stream);  // blocks return to the cache ordered on this stream
+        const bool own = crs->own_stream;
+        cudaStream_t st = crs->stream;
+        crs->own_stream = false;
+        delete crs;
+        if (own) cudaStreamDestroy(st);
+    }
     return CIGPU_OK;
 }
 
@@ -493,6 +561,7 @@ int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double 
     if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
+    StreamScope scope(s);
     const int64_t dim = crs->dim;
     DevBuf<uint32_t> ucnt(dim);
     DevBuf<int64_t> urow(dim + 1);
@@ -516,6 +585,7 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
+    StreamScope scope(s);
     CIGPU_CUDA(cudaMemcpyAsync(row, crs->row_ptr.p, sizeof(int64_t) * (crs->dim + 1), cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaMemcpyAsync(col, crs->col.p, sizeof(uint32_t) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
     if (crs->precision == CIGPU_FP64) {
@@ -535,6 +605,7 @@ int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y) {
     if (!crs || !x || !y) return CIGPU_EINVAL;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
+    StreamScope scope(s);
     DevBuf<double> dx(crs->dim), dy(crs->dim);
     CIGPU_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
     crs_mv64(*crs, dx.p, dy.p, s);
@@ -549,6 +620,7 @@ int cigpu_mvprod_device(cigpu_crs *crs, const void *x, void *y, int dtype, cigpu
     if (dtype == 1 && crs->precision != CIGPU_MIXED) return CIGPU_EINVAL;
     CIGPU_TRY
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : crs->stream;
+    StreamScope scope(s);
     if (dtype == 0)
         crs_mv64(*crs, static_cast<const double *>(x), static_cast<double *>(y), s);
     else
@@ -563,6 +635,7 @@ int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0
     CIGPU_TRY
     const auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = crs->stream;
+    StreamScope scope(s);
     DevBuf<double> c(crs->dim);
     if (c0) CIGPU_CUDA(cudaMemcpyAsync(c.p, c0, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
     SolveProblem P;
@@ -591,6 +664,7 @@ int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *aa, double 
     if (!crs || !c) return CIGPU_EINVAL;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
+    StreamScope scope(s);
     DevBuf<double> dc(crs->dim);
     CIGPU_CUDA(cudaMemcpyAsync(dc.p, c, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
     crs_rdm(*crs, dc.p, rdm1, aa, ab, bb, s);

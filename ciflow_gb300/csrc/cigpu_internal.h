@@ -38,11 +38,22 @@ void dev_free(void *p, size_t bytes);   // returns the block to the cache
 // Bytes currently held by live DevBufs (not counting the cache).
 size_t dev_bytes_in_use();
 
+// The stream the calling thread's library work is ordered on. Entry points set it
+// for their duration; a block released while it is set is handed to another
+// stream only after an event recorded on it has completed (stream-ordered reuse).
+// A block released with no stream set waits for the whole device first, as
+// cudaFree would.
+struct StreamScope {
+    cudaStream_t prev;
+    bool prev_set;
+    // set = false: no stream (e.g. synchronous legacy-stream copies follow)
+    explicit StreamScope(cudaStream_t s, bool set = true);
+    ~StreamScope();
+};
+
 // Device buffer with RAII; allocation failure throws std::bad_alloc. Blocks come
 // from a caching allocator: cudaFree synchronises the whole device, which would
-// serialise concurrent solves on different streams. Every release in this
-// library happens after the stream that used the block has synchronised, so a
-// cached block can be handed out again at once.
+// serialise concurrent solves on different streams.
 template <typename T>
 struct DevBuf {
     T *p = nullptr;

@@ -110,6 +110,7 @@ struct cigpu_server {
                 return;
             }
         }
+        cigpu::StreamScope scope(s);  // released blocks are ordered on this worker's stream
         cigpu_ham *ham = nullptr;
         cigpu_crs *crs = nullptr;
         int st = cigpu_ham_create(q.r.L, q.r.nup, q.r.ndown, q.r.econst, q.h.data(), q.eri.data(), &ham);
