@@ -300,14 +300,12 @@ def run_cigpu(args, rank: int, world: int, dist):
         e1.record(stream)
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / 1000.0 / reps
-        sv = 4 if tag == "fp32" else 8
-        n = dim.value
-        bytes_alg = nf.value * (sv + 4) + 8 * (n + 1) + n * sv + n * sv
+        bytes_alg, layout = A.matvec_bytes(crs, tag == "fp32")
         ach = bytes_alg / t / 1e9
         roof[tag] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{args.config}"),
-                     "algorithmic_bytes": bytes_alg, "ms_per_launch": t * 1000, "nnz_full": nf.value,
-                     "peak_source": peaks["source"]}
+                     "algorithmic_bytes": bytes_alg, "layout": layout, "ms_per_launch": t * 1000,
+                     "nnz_full": nf.value, "peak_source": peaks["source"]}
         lib.cigpu_crs_destroy(crs)
 
     # e2e through the C ABI with host buffers, H2D of the integrals and D2H of c inside the region

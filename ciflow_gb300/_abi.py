@@ -16,6 +16,7 @@ OK, EINVAL, ENOMEM, EAGAIN, ECANCELED, ETIMEDOUT, ENOTSUP, ENOCONV, ECUDA, ENOTF
     0, 22, 12, 11, 125, 110, 95, 200, 201, 202)
 FCI, DOCI = 0, 1
 FP64, MIXED = 0, 1
+LAYOUT_CRS, LAYOUT_SLOTS = 0, 1
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -55,6 +56,7 @@ SIGNATURES = {
     "cigpu_build": (_I, [_P, _I, _I, _P, _P]),
     "cigpu_crs_destroy": (_I, [_P]),
     "cigpu_crs_dims": (_I, [_P, _P, _P, _P]),
+    "cigpu_crs_layout": (_I, [_P, _P, _P]),
     "cigpu_crs_export_upper": (_I, [_P, _P, _P, _P]),
     "cigpu_crs_export_full": (_I, [_P, _P, _P, _P]),
     "cigpu_mvprod": (_I, [_P, _P, _P]),
@@ -122,3 +124,20 @@ def estimate_bytes(L: int, nup: int, ndown: int, method: int, precision: int) ->
     b = ctypes.c_size_t()
     check(lib().cigpu_estimate_bytes(L, nup, ndown, method, precision, ctypes.byref(b)), "cigpu_estimate_bytes")
     return b.value
+
+
+def matvec_bytes(handle, fp32: bool) -> tuple[int, str]:
+    """Algorithmic bytes of one matvec for the stored layout: one read of the stored
+    matrix and of x, one write of y. FP32: FP32 values/x/y; FP64: FP64 x/y with FP64
+    values (plain CRS) or the split hi + lo values (MIXED)."""
+    dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    check(lib().cigpu_crs_dims(handle, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf)))
+    lay, stored = ctypes.c_int(), ctypes.c_int64()
+    check(lib().cigpu_crs_layout(handle, ctypes.byref(lay), ctypes.byref(stored)))
+    n, m = dim.value, stored.value
+    sx = 4 if fp32 else 8
+    if lay.value == LAYOUT_SLOTS:
+        sv = 4 if fp32 else 8
+        return m * sv + 2 * n * sx, "slots-fp32" if fp32 else "slots-hilo"
+    sv = 4 if fp32 else 8
+    return m * (sv + 4) + 8 * (n + 1) + 2 * n * sx, "crs-fp32" if fp32 else "crs-fp64"

@@ -218,13 +218,57 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
         W = 1 + sa + sb + sa * sb + binom64(nup, 2) * binom64(L - nup, 2) + binom64(ndown, 2) * binom64(L - ndown, 2);
     }
     const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
-    size_t b = (size_t)dim * W * 12;              // col + values (FP64, or FP32 hi + lo)
+    // col + values (FP64, or FP32 hi + lo); the mixed FCI layout stores values only
+    size_t b = (size_t)dim * W * 12;
+    if (method == CIGPU_FCI && precision == CIGPU_MIXED) b = (size_t)dim * ((W + 3) & ~(int64_t)3) * 8;
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
     b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
     b += (size_t)dim * 8 * 5;                    // c, refinement vectors
     b += (size_t)L * L * L * L * 8 + (64u << 20);  // integrals + tables/slack
     return b;
 }
+
+// Per-row single-excitation tables of an FCI CRS (FP64, plus the FP32 splits of
+// them and of the diagonal for MIXED); only the fill passes read them.
+struct RowSingles {
+    DevBuf<double> sgl64;
+    DevBuf<float> sgl_hi, sgl_lo, diag_hi, diag_lo;
+    void make(cigpu_crs &c, FciParams &p, cudaStream_t s) {
+        const size_t nsr = (size_t)(c.da.view.ns + c.db.view.ns);
+        sgl64.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
+        if (c.precision == CIGPU_MIXED) {
+            sgl_hi.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
+            sgl_lo.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
+            diag_hi.alloc(c.dim);
+            diag_lo.alloc(c.dim);
+        }
+        fci_singles_launch(p, sgl64.p, sgl_hi.p, sgl_lo.p, diag_hi.p, diag_lo.p, s);
+        p.sgl64 = sgl64.p;
+        p.sgl_hi = sgl_hi.p;
+        p.sgl_lo = sgl_lo.p;
+        p.diag_hi = diag_hi.p;
+        p.diag_lo = diag_lo.p;
+    }
+};
+
+// Explicit FP32 CRS (columns + hi values) of a values-only CRS, for export.
+struct ExplicitFp32 {
+    DevBuf<uint32_t> col;
+    DevBuf<float> hi, lo;
+    void make(cigpu_crs &c, cudaStream_t s) {
+        FciParams q = c.fp;
+        RowSingles rs;
+        rs.make(c, q, s);
+        col.alloc(std::max<int64_t>(c.nnz_full, 1));
+        hi.alloc(std::max<int64_t>(c.nnz_full, 1));
+        lo.alloc(std::max<int64_t>(c.nnz_full, 1));
+        q.row_ptr = c.row_ptr.p;
+        q.col = col.p;
+        q.val32 = hi.p;
+        q.val32lo = lo.p;
+        fci_launch(kFill32, q, s);
+    }
+};
 
 void build_crs(cigpu_crs &c, cudaStream_t s) {
     const auto t0 = std::chrono::steady_clock::now();
@@ -233,8 +277,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     const int64_t dim = c.dim;
     c.diag.alloc(dim);
     DevBuf<uint32_t> count(dim);
-    DevBuf<double> sgl64;                          // FCI row singles (build only)
-    DevBuf<float> sgl_hi, sgl_lo, diag_hi, diag_lo;  // their FP32 splits (MIXED build only)
+    RowSingles singles;  // FCI row singles (build only)
     c.upper_off.alloc(dim);
     c.row_ptr.alloc(dim + 1);
     tr.mark("alloc small");
@@ -258,20 +301,9 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.eri_lo = h.d_eri_lo.p;
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
-        const size_t nsr = (size_t)(c.da.view.ns + c.db.view.ns);
-        sgl64.alloc(std::max<size_t>((size_t)dim * nsr, 1));
-        if (c.precision == CIGPU_MIXED) {
-            sgl_hi.alloc(std::max<size_t>((size_t)dim * nsr, 1));
-            sgl_lo.alloc(std::max<size_t>((size_t)dim * nsr, 1));
-            diag_hi.alloc(dim);
-            diag_lo.alloc(dim);
-        }
-        fci_singles_launch(p, sgl64.p, sgl_hi.p, sgl_lo.p, diag_hi.p, diag_lo.p, s);
-        p.sgl64 = sgl64.p;
-        p.sgl_hi = sgl_hi.p;
-        p.sgl_lo = sgl_lo.p;
-        p.diag_hi = diag_hi.p;
-        p.diag_lo = diag_lo.p;
+        singles.make(c, p, s);
+        p.Wp = slots_stride(p);
+        c.slots = c.precision == CIGPU_MIXED && slots_supported(p);
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
@@ -308,11 +340,15 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     }
     count.release();
     tr.mark("scans");
-    c.col.alloc(c.nnz_full);
-    const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
-    if (mode == kFill64)
+    const int mode = c.slots ? kFillSlots : (c.precision == CIGPU_MIXED ? kFill32 : kFill64);
+    if (c.slots) {
+        c.val32.alloc((size_t)dim * c.fp.Wp);
+        c.val32lo.alloc((size_t)dim * c.fp.Wp);
+    } else if (mode == kFill64) {
+        c.col.alloc(c.nnz_full);
         c.val64.alloc(c.nnz_full);
-    else {
+    } else {
+        c.col.alloc(c.nnz_full);
         c.val32.alloc(c.nnz_full);
         c.val32lo.alloc(c.nnz_full);
     }
@@ -341,6 +377,10 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
 }
 
 void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
+    if (c.slots) {
+        spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, y, s);
+        return;
+    }
     if (c.precision == CIGPU_FP64) {
         spmv_f64(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
         return;
@@ -348,7 +388,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
     if (c.val32lo.p || c.nnz_full == 0) {
         // MIXED CRS: FP64 product with values hi + lo (|v - hi - lo| <= 2^-48 |v|);
         // an all-zero matrix (e.g. no electrons) has no value arrays at all
-        spmv_hilo(c.dim, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
+        spmv_hilo(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
         return;
     }
     throw std::invalid_argument("MIXED CRS without its FP32 remainder array");
@@ -356,6 +396,10 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
 
 void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
     if (c.precision != CIGPU_MIXED) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
+    if (c.slots) {
+        spmv_slots_f32(c.fp, c.val32.p, x, y, s);
+        return;
+    }
     spmv_f32(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, x, y, s);
 }
 
@@ -556,6 +600,13 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
     return CIGPU_OK;
 }
 
+int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
+    if (!crs) return CIGPU_EINVAL;
+    if (layout) *layout = crs->slots ? CIGPU_LAYOUT_SLOTS : CIGPU_LAYOUT_CRS;
+    if (stored) *stored = crs->slots ? crs->dim * crs->fp.Wp : crs->nnz_full;
+    return CIGPU_OK;
+}
+
 int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val) {
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
     if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
@@ -569,8 +620,10 @@ int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double 
     exclusive_scan_u32(ucnt.p, urow.p, dim, s);
     DevBuf<uint32_t> ucol(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
     DevBuf<double> uval(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
-    extract_upper_launch(dim, crs->row_ptr.p, crs->upper_off.p, crs->col.p, crs->val64.p, crs->val32.p, urow.p,
-                         ucol.p, uval.p, s);
+    ExplicitFp32 ex;
+    if (crs->slots) ex.make(*crs, s);
+    extract_upper_launch(dim, crs->row_ptr.p, crs->upper_off.p, crs->slots ? ex.col.p : crs->col.p, crs->val64.p,
+                         crs->slots ? ex.hi.p : crs->val32.p, urow.p, ucol.p, uval.p, s);
     std::vector<int64_t> hr(dim + 1);
     CIGPU_CUDA(cudaMemcpyAsync(hr.data(), urow.p, sizeof(int64_t) * (dim + 1), cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaMemcpyAsync(col, ucol.p, sizeof(uint32_t) * crs->nnz_upper, cudaMemcpyDeviceToHost, s));
@@ -586,14 +639,18 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
     CIGPU_TRY
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
+    ExplicitFp32 ex;
+    if (crs->slots) ex.make(*crs, s);
     CIGPU_CUDA(cudaMemcpyAsync(row, crs->row_ptr.p, sizeof(int64_t) * (crs->dim + 1), cudaMemcpyDeviceToHost, s));
-    CIGPU_CUDA(cudaMemcpyAsync(col, crs->col.p, sizeof(uint32_t) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+    CIGPU_CUDA(cudaMemcpyAsync(col, crs->slots ? ex.col.p : crs->col.p, sizeof(uint32_t) * crs->nnz_full,
+                               cudaMemcpyDeviceToHost, s));
     if (crs->precision == CIGPU_FP64) {
         CIGPU_CUDA(cudaMemcpyAsync(val, crs->val64.p, sizeof(double) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaStreamSynchronize(s));
     } else {
         std::vector<float> tmp(crs->nnz_full);
-        CIGPU_CUDA(cudaMemcpyAsync(tmp.data(), crs->val32.p, sizeof(float) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(tmp.data(), crs->slots ? ex.hi.p : crs->val32.p, sizeof(float) * crs->nnz_full,
+                                   cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaStreamSynchronize(s));
         for (int64_t i = 0; i < crs->nnz_full; ++i) val[i] = tmp[i];
     }

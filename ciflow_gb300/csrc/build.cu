@@ -118,6 +118,8 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
     const int L = p.L, L2 = L * L;
     const int nsa = p.a.ns;
     const int W = p.b.nfull + nsa * p.b.nsing + p.a.nd;
+    constexpr bool F32 = (MODE == kFill32 || MODE == kFillSlots);
+    const int Wloop = MODE == kFillSlots ? (int)p.Wp : W;  // slots also write the zero padding
     uint64_t *nbA = reinterpret_cast<uint64_t *>(smem);
     uint32_t *gstart = reinterpret_cast<uint32_t *>(nbA + nga);
     uint16_t *gmap = reinterpret_cast<uint16_t *>(gstart + nga + 1);
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
             const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
             const int ar = (info >> 12) & 63, ac = (info >> 18) & 63;
             const size_t at = ((size_t)ar * L + ac) * L2 + t;  // (ar ac|br bc)
-            if (MODE == kFill32) {
+            if (F32) {
                 slhi[i] = __ldg(p.eri_hi + at);
                 sllo[i] = __ldg(p.eri_lo + at);
             } else {
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
         int64_t base = 0;
         if (MODE == kFill64 || MODE == kFill32) base = p.row_ptr[r];
         uint32_t running = 0, nlow = 0;
-        for (int k0 = 0; k0 < W; k0 += 32) {
+        for (int k0 = 0; k0 < Wloop; k0 += 32) {
             const int k = k0 + lane;
             uint64_t vb = 0;       // FP64 bits (COUNT / FILL64 / MATVEC, and computed elements)
             float hi = 0, lo = 0;  // FILL32
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     col = (uint32_t)(ia * p.Db + Jb);
                     low = Jb < (uint32_t)ib;
                     if (kindB == kSelf) {
-                        if (MODE == kFill32) {
+                        if (F32) {
                             hi = p.diag_hi[r];
                             lo = p.diag_lo[r];
                         } else {
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     } else if (kindB == kSingle) {
                         // beta single (one_diff_orbital(down1, down2, up1)), precomputed per row
                         const size_t at = (size_t)r * (nsa + p.b.ns) + nsa + xb;
-                        if (MODE == kFill32) {
+                        if (F32) {
                             hi = __ldg(p.sgl_hi + at);
                             lo = __ldg(p.sgl_lo + at);
                         } else {
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                         }
                     } else {
                         const size_t at = ib * p.b.nd + xb;
-                        if (MODE == kFill32) {
+                        if (F32) {
                             hi = __ldg(p.b.d_hi + at);
                             lo = __ldg(p.b.d_lo + at);
                         } else {
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     if (kindB == kSelf) {
                         // alpha single (one_diff_orbital(up1, up2, down1)), precomputed per row
                         const size_t at = (size_t)r * (nsa + p.b.ns) + xa;
-                        if (MODE == kFill32) {
+                        if (F32) {
                             hi = __ldg(p.sgl_hi + at);
                             lo = __ldg(p.sgl_lo + at);
                         } else {
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                         const int br = (infoB >> 12) & 63, bc = (infoB >> 18) & 63;
                         const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
                         const int t = br * L + bc;
-                        if (MODE == kFill32) {
+                        if (F32) {
                             if (p.staged) {
                                 hi = slhi[xa * L2 + t];
                                 lo = sllo[xa * L2 + t];
@@ -280,17 +282,25 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     col = (uint32_t)((int64_t)Ja * p.Db + ib);
                     low = Ja < (uint32_t)ia;
                     const size_t at = ia * p.a.nd + xa;
-                    if (MODE == kFill32) {
+                    if (F32) {
                         hi = __ldg(p.a.d_hi + at);
                         lo = __ldg(p.a.d_lo + at);
                     } else {
                         vb = __double_as_longlong(__ldg(p.a.d_val + at));
                     }
                 }
-                if (MODE == kFill32)
+                if (F32)
                     keep = (__float_as_uint(hi) & 0x7FFFFFFFu) != 0u;  // splits are zero where |v| <= 1e-14
                 else
                     keep = keep_bits(vb);
+            }
+            if (MODE == kFillSlots) {
+                if (k < Wloop) {
+                    const int64_t at = r * p.Wp + k;
+                    p.val32[at] = keep ? hi : 0.0f;
+                    p.val32lo[at] = keep ? lo : 0.0f;
+                }
+                continue;
             }
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (MODE == kCount) {
@@ -516,18 +526,23 @@ void fci_launch(int mode, const FciParams &p0, cudaStream_t s) {
     FciParams p = p0;
     const size_t sm = fci_smem_bytes(p);
     p.staged = (sm == fci_base_smem(p) + fci_slice_smem(p)) ? 1 : 0;
-    if (mode == kFill32 && (!p.eri_hi || !p.eri_lo)) throw CudaError{cudaErrorInvalidValue, "FP32 integral tables missing"};
     const int64_t nchunks = (p.Db + kFciRowsPerBlock - 1) / kFciRowsPerBlock;
     const int64_t blocks = p.a.D * nchunks;
-    if (sm > 48 * 1024) {
+    if ((mode == kFill32 || mode == kFillSlots) && (!p.eri_hi || !p.eri_lo))
+        throw CudaError{cudaErrorInvalidValue, "FP32 integral tables missing"};
+    static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
-    }
+        cudaFuncSetAttribute(k_fci_rows<kFillSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
+        return true;
+    }();
+    (void)attr_set;
     switch (mode) {
         case kCount: k_fci_rows<kCount><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
         case kFill64: k_fci_rows<kFill64><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
-        default: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
+        case kFill32: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
+        default: k_fci_rows<kFillSlots><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
     }
     CIGPU_CUDA(cudaGetLastError());
     count_launch();

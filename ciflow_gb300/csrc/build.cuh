@@ -5,7 +5,11 @@
 
 namespace cigpu {
 
-enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2 };
+// kFillSlots: the mixed method's values-only FCI layout. Every structural slot of
+// a row (W of them, the same count for every row) is written at r * Wp + k with no
+// column index; dropped elements (|v| <= 1e-14) are stored as zero. The columns are
+// regenerated from the string tables by the matvec (k_spmv_slots).
+enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2, kFillSlots = 3 };
 
 constexpr int kFciThreads = 256;
 constexpr int kFciRowsPerBlock = 64;
@@ -34,6 +38,7 @@ struct FciParams {
     double *val64;
     float *val32;
     float *val32lo;  // v - (double)hi, rounded to FP32 (FP32 fill only)
+    int64_t Wp;      // slot stride of the values-only layout (W rounded up to 4)
 };
 
 struct DociParams {
@@ -68,6 +73,8 @@ __device__ __forceinline__ int nth_set(uint64_t x, int a) {
 }
 
 size_t fci_smem_bytes(const FciParams &p);
+// structural slots per FCI row: nfull_b + ns_a * nsing_b + nd_a
+__host__ __device__ inline int fci_row_width(const FciParams &p) { return p.b.nfull + p.a.ns * p.b.nsing + p.a.nd; }
 void fci_launch(int mode, const FciParams &p, cudaStream_t s);
 void fci_diag_launch(const FciParams &p, double *diag, cudaStream_t s);
 // Row singles table (and FP32 splits of it and of diag when hi/lo are non-null).

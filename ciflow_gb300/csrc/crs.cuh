@@ -3,6 +3,7 @@
 
 #include "build.cuh"
 #include "lanczos.cuh"
+#include "slots.cuh"
 
 struct cigpu_crs {
     cigpu_ham *ham = nullptr;
@@ -23,6 +24,9 @@ struct cigpu_crs {
     cigpu::DevBuf<double> val64;
     cigpu::DevBuf<float> val32;
     cigpu::DevBuf<float> val32lo;  // MIXED: FP32 rounding remainder of each value
+    // MIXED FCI: values-only layout (val32/val32lo hold dim x Wp slots, no col);
+    // row_ptr/upper_off/nnz still describe the explicit matrix for export
+    bool slots = false;
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};
     double build_seconds = 0;

@@ -23,6 +23,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
+#include <mutex>
 
 #include "lanczos.cuh"
 
@@ -44,8 +46,37 @@ constexpr int kVecThreads = 256;
 constexpr int kMaxBasis = 64;
 constexpr int kDotChunk = 8;
 constexpr int kMaxKeep = 32;
+constexpr int kStartSteps = 4;  // FP32 Lanczos steps of the mixed solver's Krylov start
 
 int vec_grid() { return sm_count() * 4; }
+// blocks for an n-element vector kernel: about 4 elements per thread, at most vec_grid()
+int vec_grid_for(int64_t n) {
+    const int64_t b = (n + kVecThreads * 4 - 1) / (kVecThreads * 4);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(vec_grid(), b));
+}
+
+// Ends a kernel that wrote per-block partial sums partial[v*G + b] (G = gridDim.x):
+// the last block to finish reduces them into out[v], v < nvec, one warp per entry in
+// a fixed order (run-to-run reproducible), and resets the ticket for the next kernel
+// on the stream. Saves a separate reduction launch per dot product.
+__device__ __forceinline__ void reduce_in_last_block(const double *partial, int nvec, double *out,
+                                                     unsigned *ticket) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x * gridDim.y - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int G = gridDim.x, lane = threadIdx.x & 31;
+    for (int v = threadIdx.x >> 5; v < nvec; v += blockDim.x >> 5) {
+        double s = 0;
+        for (int b = lane; b < G; b += 32) s += __ldcg(partial + (int64_t)v * G + b);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[v] = s;
+    }
+    if (threadIdx.x == 0) *ticket = 0;
+}
 
 // Per-block partial dots V_i . w (i < nvec, chunks of kDotChunk on blockIdx.y).
 // AT is the arithmetic type of the products and of the per-thread sums (float for
@@ -54,7 +85,9 @@ int vec_grid() { return sm_count() * 4; }
 template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__ V, int64_t ld, int nvec,
                                                           const WT *__restrict__ w, int64_t n,
-                                                          double *__restrict__ partial, int G) {
+                                                          double *__restrict__ partial, double *__restrict__ out,
+                                                          unsigned *__restrict__ ticket) {
+    const int G = gridDim.x;
     const int v0 = blockIdx.y * kDotChunk;
     const int nv = min(kDotChunk, nvec - v0);
     AT acc[kDotChunk];
@@ -80,24 +113,15 @@ __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__
         for (int k = 0; k < kVecThreads / 32; ++k) s += sh[threadIdx.x][k];
         partial[(int64_t)(v0 + threadIdx.x) * G + blockIdx.x] = s;
     }
-}
-
-// out[v] = sum_b partial[v*G + b], one warp per entry, fixed order.
-__global__ void k_reduce_partials(const double *__restrict__ partial, int G, int nvec, double *__restrict__ out) {
-    const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (v >= nvec) return;
-    double s = 0;
-    for (int b = lane; b < G; b += 32) s += partial[(int64_t)v * G + b];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) out[v] = s;
+    reduce_in_last_block(partial, nvec, out, ticket);
 }
 
 // w -= sum_{i<nvec} V_i coef_i (arithmetic in AT); partial ||w||^2 per block when nrm != nullptr.
 template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
                                                         const double *__restrict__ coef, WT *__restrict__ w, int64_t n,
-                                                        double *__restrict__ nrm) {
+                                                        double *__restrict__ nrm, double *__restrict__ nrm_out,
+                                                        unsigned *__restrict__ ticket) {
     __shared__ AT c[kMaxBasis + 1];
     for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = (AT)coef[i];
     __syncthreads();
@@ -120,6 +144,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
             for (int k = 0; k < kVecThreads / 32; ++k) s += sh[k];
             nrm[blockIdx.x] = s;
         }
+        reduce_in_last_block(nrm, 1, nrm_out, ticket);
     }
 }
 
@@ -129,42 +154,6 @@ __global__ void k_scale_to(const IT *__restrict__ t, int64_t n, const double *__
     const double inv = 1.0 / sqrt(*nrm2);
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
         out[r] = (OT)((double)t[r] * inv);
-}
-
-// Davidson residual of u = a0 c + sum_i y_i v_i with H u ~ a0 w + sum_i y_i (H v_i):
-//   ru = a0 (w - theta c) + sum_i y_i (HV_i - theta V_i)      (FP64 arithmetic)
-//   t  = ru / (theta - H_ii)   (diagonal preconditioner, guarded)
-// and partial ||ru||^2.
-__global__ void __launch_bounds__(kVecThreads) k_dav_residual(const double *__restrict__ w, const double *__restrict__ c,
-                                                              const float *__restrict__ V, const float *__restrict__ HV,
-                                                              int64_t ld, int k, const double *__restrict__ y,
-                                                              double a0, double theta, const double *__restrict__ diag,
-                                                              double *__restrict__ t, int64_t n,
-                                                              double *__restrict__ nrm) {
-    __shared__ double ys[kMaxBasis + 1];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = y[i];
-    __syncthreads();
-    double acc = 0;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        double ru = a0 * (w[r] - theta * c[r]);
-        for (int i = 0; i < k; ++i) {
-            const int64_t o = (int64_t)i * ld + r;
-            ru += ys[i] * ((double)HV[o] - theta * (double)V[o]);
-        }
-        acc += ru * ru;
-        double d = theta - diag[r];
-        if (fabs(d) < 1e-2) d = d < 0 ? -1e-2 : 1e-2;
-        t[r] = ru / d;
-    }
-    __shared__ double sh[kVecThreads / 32];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int q = 0; q < kVecThreads / 32; ++q) s += sh[q];
-        nrm[blockIdx.x] = s;
-    }
 }
 
 // FP32 Davidson residual of u = a0 c + sum_i y_i v_i, written straight into the
@@ -179,7 +168,8 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const double *__
                                                                 int64_t ld, int k, const double *__restrict__ y,
                                                                 double a0, double a0_de, double theta,
                                                                 const double *__restrict__ diag, float *__restrict__ t,
-                                                                int64_t n, double *__restrict__ nrm) {
+                                                                int64_t n, double *__restrict__ nrm,
+                                                                double *__restrict__ nrm_out, unsigned *__restrict__ ticket) {
     __shared__ float ys[kMaxBasis + 1];
     for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = (float)y[i];
     __syncthreads();
@@ -206,6 +196,7 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const double *__
         for (int q = 0; q < kVecThreads / 32; ++q) sum += sh[q];
         nrm[blockIdx.x] = sum;
     }
+    reduce_in_last_block(nrm, 1, nrm_out, ticket);
 }
 
 // t = r / (E - H_ii) in FP32 (first direction after an anchor update).
@@ -254,23 +245,32 @@ __global__ void k_argmin_partial(const double *__restrict__ d, int64_t n, double
     }
 }
 
-// v = e_{argmin}: zero everywhere except 1 at the lowest diagonal element.
-__global__ void k_unit_at_argmin(const double *__restrict__ pv, const int64_t *__restrict__ pi, int G,
-                                 double *__restrict__ v, int64_t n) {
-    __shared__ int64_t at;
-    if (threadIdx.x == 0) {
-        double best = 1e308;
-        int64_t bi = 0;
-        for (int b = 0; b < G; ++b)
-            if (pv[b] < best || (pv[b] == best && pi[b] < bi)) {
-                best = pv[b];
-                bi = pi[b];
-            }
-        at = bi;
+// One warp: the (value, index) minimum over the G block partials, ties to the lower
+// index; the index goes to pi[0].
+__global__ void k_argmin_final(const double *__restrict__ pv, int64_t *__restrict__ pi, int G) {
+    double best = 1e308;
+    int64_t bi = INT64_MAX;
+    for (int b = threadIdx.x; b < G; b += 32)
+        if (pv[b] < best || (pv[b] == best && pi[b] < bi)) {
+            best = pv[b];
+            bi = pi[b];
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob < best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+        }
     }
-    __syncthreads();
+    if (threadIdx.x == 0) pi[0] = bi;
+}
+
+// v = e_at + keep * v with at = *pi (v holds a random vector on entry).
+__global__ void k_add_unit_at(const int64_t *__restrict__ pi, double keep, double *__restrict__ v, int64_t n) {
+    const int64_t at = *pi;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
-        v[r] = (r == at) ? 1.0 : 0.0;
+        v[r] = keep * v[r] + ((r == at) ? 1.0 : 0.0);
 }
 
 template <typename VT>
@@ -281,25 +281,27 @@ __global__ void k_scale(VT *__restrict__ w, int64_t n, const double *__restrict_
 }
 
 // out_i = sum_{l<m} V_l Y[l + m*i], i < k (Y column-major on the device).
-template <typename VT, typename OT>
+// KMAX bounds k at compile time: the single-vector form (a Ritz vector) keeps one
+// accumulator instead of kMaxKeep.
+template <typename VT, typename OT, int KMAX = kMaxKeep>
 __global__ void __launch_bounds__(kVecThreads) k_combine(const VT *__restrict__ V, int64_t ld, int m,
                                                          const double *__restrict__ Y, int k, OT *__restrict__ out,
                                                          int64_t ldo, int64_t n) {
-    __shared__ double y[kMaxBasis * kMaxKeep];
+    __shared__ double y[kMaxBasis * KMAX];
     for (int i = threadIdx.x; i < m * k; i += blockDim.x) y[i] = Y[i];
     __syncthreads();
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        double acc[kMaxKeep];
+        double acc[KMAX];
 #pragma unroll
-        for (int i = 0; i < kMaxKeep; ++i) acc[i] = 0;
+        for (int i = 0; i < KMAX; ++i) acc[i] = 0;
         for (int l = 0; l < m; ++l) {
             const double v = (double)V[(int64_t)l * ld + r];
 #pragma unroll
-            for (int i = 0; i < kMaxKeep; ++i)
+            for (int i = 0; i < KMAX; ++i)
                 if (i < k) acc[i] += v * y[l + m * i];
         }
 #pragma unroll
-        for (int i = 0; i < kMaxKeep; ++i)
+        for (int i = 0; i < KMAX; ++i)
             if (i < k) out[(int64_t)i * ldo + r] = (OT)acc[i];
     }
 }
@@ -307,7 +309,8 @@ __global__ void __launch_bounds__(kVecThreads) k_combine(const VT *__restrict__ 
 // r = w - E c; partial ||r||^2.
 __global__ void __launch_bounds__(kVecThreads) k_residual(const double *__restrict__ w, const double *__restrict__ c,
                                                           double E, double *__restrict__ r, int64_t n,
-                                                          double *__restrict__ nrm) {
+                                                          double *__restrict__ nrm, double *__restrict__ nrm_out,
+                                                          unsigned *__restrict__ ticket) {
     double acc = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double x = w[i] - E * c[i];
@@ -323,6 +326,7 @@ __global__ void __launch_bounds__(kVecThreads) k_residual(const double *__restri
         for (int k = 0; k < kVecThreads / 32; ++k) s += sh[k];
         nrm[blockIdx.x] = s;
     }
+    reduce_in_last_block(nrm, 1, nrm_out, ticket);
 }
 
 // Davidson-type diagonal preconditioner t = r / (E - H_ii), guarded away from 0.
@@ -362,37 +366,65 @@ __global__ void k_convert(const S *__restrict__ s, D *__restrict__ d, int64_t n)
 
 // ---------------------------------------------------------------------------
 // Host-side helpers around the kernels.
+
+// Pinned result buffers are pooled for the life of the process: cudaFreeHost
+// synchronises the whole device, which would stall every concurrent solve.
+constexpr size_t kPinnedDoubles = 4 * (kMaxBasis + 2);
+std::mutex g_pinned_mutex;
+std::vector<double *> g_pinned_pool;
+
+double *pinned_get() {
+    {
+        std::lock_guard<std::mutex> lock(g_pinned_mutex);
+        if (!g_pinned_pool.empty()) {
+            double *p = g_pinned_pool.back();
+            g_pinned_pool.pop_back();
+            return p;
+        }
+    }
+    double *p = nullptr;
+    CIGPU_CUDA(cudaMallocHost(&p, sizeof(double) * kPinnedDoubles));
+    return p;
+}
+
+void pinned_put(double *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mutex);
+    g_pinned_pool.push_back(p);
+}
+
 struct VecOps {
     cudaStream_t s;
-    int G;
-    DevBuf<double> partial;  // [(kMaxBasis+1) * G]
-    DevBuf<double> out;      // [4 * (kMaxBasis+1)]
+    int G;                   // blocks of every vector kernel: sized to n, at most vec_grid()
+    DevBuf<double> partial;  // [(kMaxBasis+2) * G]
+    DevBuf<double> out;      // [4 * (kMaxBasis+2)]
+    DevBuf<unsigned> ticket; // last-block counter of the fused reductions
     double *h_out = nullptr; // pinned
-    explicit VecOps(cudaStream_t st) : s(st), G(vec_grid()), partial((size_t)(kMaxBasis + 2) * vec_grid()),
-                                       out(4 * (kMaxBasis + 2)) {
-        CIGPU_CUDA(cudaMallocHost(&h_out, sizeof(double) * 4 * (kMaxBasis + 2)));
+    VecOps(cudaStream_t st, int64_t n)
+        : s(st), G(vec_grid_for(n)), partial((size_t)(kMaxBasis + 2) * vec_grid_for(n)), out(4 * (kMaxBasis + 2)),
+          ticket(1) {
+        CIGPU_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
+        h_out = pinned_get();
     }
     ~VecOps() {
-        if (h_out) cudaFreeHost(h_out);
+        // normally every copy into h_out has been waited for; on an error path wait here
+        if (std::uncaught_exceptions() > 0) cudaStreamSynchronize(s);
+        pinned_put(h_out);
     }
     // out[dst .. dst+nvec) = V_i . w   (AT: arithmetic type of the products)
     template <typename VT, typename WT, typename AT = double>
     void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst) {
         dim3 grid(G, (nvec + kDotChunk - 1) / kDotChunk);
-        k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, G);
-        k_reduce_partials<<<(nvec + 7) / 8, 256, 0, s>>>(partial.p, G, nvec, out.p + dst);
+        k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, out.p + dst, ticket.p);
         CIGPU_CUDA(cudaGetLastError());
-        count_launch(2);
+        count_launch();
     }
     template <typename VT, typename WT, typename AT = double>
     void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at) {
         k_update<VT, WT, AT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n,
-                                                       nrm_at >= 0 ? partial.p : nullptr);
+                                                       nrm_at >= 0 ? partial.p : nullptr,
+                                                       nrm_at >= 0 ? out.p + nrm_at : nullptr, ticket.p);
         count_launch();
-        if (nrm_at >= 0) {
-            k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p + nrm_at);
-            count_launch();
-        }
         CIGPU_CUDA(cudaGetLastError());
     }
     template <typename VT>
@@ -411,10 +443,9 @@ struct VecOps {
         return h_out;
     }
     double residual(const double *w, const double *c, double E, double *r, int64_t n) {
-        k_residual<<<G, kVecThreads, 0, s>>>(w, c, E, r, n, partial.p);
-        k_reduce_partials<<<1, 32, 0, s>>>(partial.p, G, 1, out.p);
+        k_residual<<<G, kVecThreads, 0, s>>>(w, c, E, r, n, partial.p, out.p, ticket.p);
         CIGPU_CUDA(cudaGetLastError());
-        count_launch(2);
+        count_launch();
         return std::sqrt(fetch(1)[0]);
     }
 };
@@ -608,7 +639,7 @@ struct TRLanczos {
     // c = V[0..j) y0 (FP64 output)
     void ritz_vector(double *c_dev) {
         CIGPU_CUDA(cudaMemcpyAsync(Yd.p, y0.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
-        k_combine<VT, double><<<ops.G, kVecThreads, 0, s>>>(V.p, n, j, Yd.p, 1, c_dev, n, n);
+        k_combine<VT, double, 1><<<ops.G, kVecThreads, 0, s>>>(V.p, n, j, Yd.p, 1, c_dev, n, n);
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
         CIGPU_CUDA(cudaStreamSynchronize(s));
@@ -704,7 +735,7 @@ int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool
     const int m = (int)std::min<int64_t>(std::min(o.basis, kMaxBasis), std::max<int64_t>(n, 1));
     const int keep = std::max(1, std::min({o.keep, m - 1, kMaxKeep}));
     cudaStream_t s = P.stream;
-    VecOps ops(s);
+    VecOps ops(s, n);
     if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
     Refine ref(n, s, ops);
     if (n == 1) {
@@ -761,21 +792,64 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         if (!have_start) dev_fill_random(c_dev, n, o.seed, s);
         return solve_fp64(P, o, c_dev, true, info);
     }
-    VecOps ops(s);
+    VecOps ops(s, n);
     Refine ref(n, s, ops);
     const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 2), n - 2);
-    if (!have_start) {
-        DevBuf<double> pv(ops.G);
-        DevBuf<int64_t> pi(ops.G);
-        k_argmin_partial<<<ops.G, kVecThreads, 0, s>>>(P.diag, n, pv.p, pi.p);
-        k_unit_at_argmin<<<ops.G, kVecThreads, 0, s>>>(pv.p, pi.p, ops.G, c_dev, n);
-        CIGPU_CUDA(cudaGetLastError());
-        count_launch(2);
-    }
     DevBuf<float> V((size_t)(mmax + 2) * n), HV((size_t)(mmax + 2) * n), cr32((size_t)2 * n);
     DevBuf<double> yd(kMaxBasis + 1);
-    std::vector<double> A((size_t)kMaxBasis * kMaxBasis, 0.0), eta(kMaxBasis, 0.0), bvec(kMaxBasis, 0.0);
     int64_t mv32 = 0, mv64 = 0;
+    if (!have_start) {
+        // Krylov start. Davidson from the lowest-diagonal determinant alone can settle
+        // on an excited state when that determinant overlaps the ground state weakly
+        // (few electrons in many orbitals, strong two-electron terms). Instead take
+        // q0 = e_argmin + g (g uniform random, |g| ~ 1), run kStartSteps FP32 Lanczos
+        // steps with full reorthogonalisation, and start from the lowest Ritz vector.
+        DevBuf<double> pv(ops.G);
+        DevBuf<int64_t> pi(ops.G);
+        dev_fill_random(c_dev, n, o.seed, s);
+        k_argmin_partial<<<ops.G, kVecThreads, 0, s>>>(P.diag, n, pv.p, pi.p);
+        k_argmin_final<<<1, 32, 0, s>>>(pv.p, pi.p, ops.G);
+        k_add_unit_at<<<ops.G, kVecThreads, 0, s>>>(pi.p, std::sqrt(3.0 / (double)n), c_dev, n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch(3);
+        const int m0 = (int)std::min<int64_t>(kStartSteps, std::min<int64_t>(n - 1, mmax + 1));
+        constexpr int kCol = 44, kNrm = 100;  // out[] slots: T columns, norms (coefficients at 0)
+        dev_convert(c_dev, V.p, n, s);
+        ops.dots<float, float, float>(V.p, n, 1, V.p, n, kNrm);
+        ops.scale(V.p, n, kNrm);
+        for (int j = 0; j < m0; ++j) {
+            float *w = V.p + (size_t)(j + 1) * n;
+            P.mv32(V.p + (size_t)j * n, w, s);
+            ++mv32;
+            ops.dots<float, float, float>(V.p, n, j + 1, w, n, kCol + 8 * j);  // column j of T
+            if (j + 1 == m0) break;
+            ops.update<float, float, float>(V.p, n, j + 1, kCol + 8 * j, w, n, -1);
+            ops.dots<float, float, float>(V.p, n, j + 1, w, n, 0);
+            ops.update<float, float, float>(V.p, n, j + 1, 0, w, n, kNrm + 1 + j);
+            ops.scale(w, n, kNrm + 1 + j);
+        }
+        const double *h = ops.fetch(kNrm + 1 + m0);
+        // an invariant Krylov space ends the start early (later slots hold no basis vectors)
+        int m = m0;
+        for (int j = 0; j + 1 < m0; ++j) {
+            const double d = h[kCol + 8 * j + j];
+            if (!(h[kNrm + 1 + j] > 1e-24 * (1.0 + d * d))) {
+                m = j + 1;
+                break;
+            }
+        }
+        std::vector<double> T((size_t)m * m), tw, tz;
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i <= j; ++i) T[(size_t)i * m + j] = T[(size_t)j * m + i] = h[kCol + 8 * j + i];
+        small_eigh(m, T, tw, tz);
+        std::vector<double> y0(m);
+        for (int i = 0; i < m; ++i) y0[i] = tz[(size_t)i * m];
+        CIGPU_CUDA(cudaMemcpyAsync(yd.p, y0.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
+        k_combine<float, double, 1><<<ops.G, kVecThreads, 0, s>>>(V.p, n, m, yd.p, 1, c_dev, n, n);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+    }
+    std::vector<double> A((size_t)kMaxBasis * kMaxBasis, 0.0), eta(kMaxBasis, 0.0), bvec(kMaxBasis, 0.0);
     int collapses = 0;
     double E = 0, rho = 0, gap = 0, last_rho = 1e300;
     auto anchor = [&]() {  // exact FP64 anchor evaluation
@@ -802,9 +876,9 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         } else {
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
             k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, c_dev, V.p, HV.p, n, k, yd.p, a0, a0 * (E - theta),
-                                                            theta, P.diag, vnew, n, ops.partial.p);
-            k_reduce_partials<<<1, 32, 0, s>>>(ops.partial.p, ops.G, 1, ops.out.p + SLOT_R);
-            count_launch(2);
+                                                            theta, P.diag, vnew, n, ops.partial.p,
+                                                            ops.out.p + SLOT_R, ops.ticket.p);
+            count_launch();
         }
         // orthonormalise against slots 0..k, twice (FP32 arithmetic, FP64 reductions)
         ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0);
@@ -856,7 +930,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         if (fold) {
             // c <- a0 c + sum_i y_i v_i  (FP64)
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
-            k_combine<float, double><<<ops.G, kVecThreads, 0, s>>>(V.p + n, n, k, yd.p, 1, ref.t.p, n, n);
+            k_combine<float, double, 1><<<ops.G, kVecThreads, 0, s>>>(V.p + n, n, k, yd.p, 1, ref.t.p, n, n);
             k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
             CIGPU_CUDA(cudaGetLastError());
             count_launch(2);

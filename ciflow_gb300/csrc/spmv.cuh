@@ -15,7 +15,7 @@ void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *co
 void spmv_f32(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
               cudaStream_t s);
 
-void spmv_hilo(int64_t n, const int64_t *row_ptr, const uint32_t *col, const float *hi, const float *lo,
+void spmv_hilo(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *hi, const float *lo,
                const double *x, double *y, cudaStream_t s);
 
 }  // namespace cigpu

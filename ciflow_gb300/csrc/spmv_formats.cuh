@@ -1,0 +1,101 @@
+// Value formats shared by the CRS matvec (spmv.cu) and the values-only FCI
+// matvec (slots.cu).
+#pragma once
+
+#include "cigpu_internal.h"
+
+namespace cigpu {
+
+// Value formats. A format loads 4 values with 16-byte loads (load4) or one value
+// (load1) and accumulates value * x into its accumulator.
+//   Plain<VT>: VT values, VT x/y, VT accumulation (FP64 method, FP32 matvec).
+//   HiLo: FP64 product from split FP32 values v = hi + lo (|v - hi - lo| <= 2^-48 |v|):
+//     hi * x accumulates in FP64 (one DFMA per element); lo * x is at most 2^-24 of
+//     the term, so FP32 arithmetic for it adds below 2^-48 relative error while
+//     halving the FP64 instructions (GB300 issues FP64 at 1/64 of the FP32 rate).
+template <typename VT>
+struct Plain {
+    using X = VT;
+    const VT *__restrict__ val;
+    struct Acc {
+        VT s = 0;
+    };
+    struct Chunk {
+        VT v[4];
+    };
+    __device__ __forceinline__ void load4(int64_t at, Chunk &c) const;
+    __device__ __forceinline__ void zero(Chunk &c) const { c.v[0] = c.v[1] = c.v[2] = c.v[3] = 0; }
+    __device__ __forceinline__ void fma(const Chunk &c, int j, X xv, Acc &a) const { a.s += c.v[j] * xv; }
+    __device__ __forceinline__ void fma1(int64_t at, X xv, Acc &a) const { a.s += __ldcs(val + at) * xv; }
+    __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const { a.s += __shfl_xor_sync(mask, a.s, o); }
+    __device__ __forceinline__ X result(const Acc &a) const { return a.s; }
+};
+template <>
+__device__ __forceinline__ void Plain<double>::load4(int64_t at, Chunk &c) const {
+    const double2 a = __ldcs(reinterpret_cast<const double2 *>(val + at));
+    const double2 b = __ldcs(reinterpret_cast<const double2 *>(val + at) + 1);
+    c.v[0] = a.x; c.v[1] = a.y; c.v[2] = b.x; c.v[3] = b.y;
+}
+template <>
+__device__ __forceinline__ void Plain<float>::load4(int64_t at, Chunk &c) const {
+    const float4 a = __ldcs(reinterpret_cast<const float4 *>(val + at));
+    c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
+}
+
+// Format conversions assembled from the IEEE-754 bit fields on the integer pipe
+// (GB300 runs float<->double conversions on its FP64 pipe, 1/64 of the FP32 rate).
+// float -> double, exact for zero and normal floats (the split values are 0 or
+// normal: |v| > 1e-14); Inf/NaN keep their class.
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    const uint64_t ed = e == 0 ? 0 : (e == 0xFFu ? 0x7FFull : (uint64_t)e + 896u);
+    const uint64_t m = e == 0 ? 0 : (uint64_t)(u & 0x7FFFFFu) << 29;
+    return __longlong_as_double((long long)(sign | (ed << 52) | m));
+}
+// double -> float by truncation (relative error below 2^-23); magnitudes below
+// 2^-126 flush to zero, above the float range become Inf.
+__device__ __forceinline__ float d2f_trunc(double d) {
+    const uint64_t u = (uint64_t)__double_as_longlong(d);
+    const int e = (int)((u >> 52) & 0x7FF) - 896;
+    const uint32_t sign = (uint32_t)(u >> 63) << 31;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((uint32_t)e << 23) | (uint32_t)((u >> 29) & 0x7FFFFFu));
+}
+
+struct HiLo {
+    using X = double;
+    const float *__restrict__ hi;
+    const float *__restrict__ lo;
+    struct Acc {
+        double d = 0;
+        float f = 0;
+    };
+    struct Chunk {
+        float4 h, l;
+    };
+    __device__ __forceinline__ void load4(int64_t at, Chunk &c) const {
+        c.h = __ldcs(reinterpret_cast<const float4 *>(hi + at));
+        c.l = __ldcs(reinterpret_cast<const float4 *>(lo + at));
+    }
+    __device__ __forceinline__ void zero(Chunk &c) const { c.h = c.l = make_float4(0, 0, 0, 0); }
+    __device__ __forceinline__ void fma(const Chunk &c, int j, X xv, Acc &a) const {
+        const float h = j == 0 ? c.h.x : j == 1 ? c.h.y : j == 2 ? c.h.z : c.h.w;
+        const float l = j == 0 ? c.l.x : j == 1 ? c.l.y : j == 2 ? c.l.z : c.l.w;
+        a.d = ::fma(f2d_bits(h), xv, a.d);
+        a.f = fmaf(l, d2f_trunc(xv), a.f);
+    }
+    __device__ __forceinline__ void fma1(int64_t at, X xv, Acc &a) const {
+        a.d = ::fma(f2d_bits(__ldcs(hi + at)), xv, a.d);
+        a.f = fmaf(__ldcs(lo + at), d2f_trunc(xv), a.f);
+    }
+    __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const {
+        a.d += __shfl_xor_sync(mask, a.d, o);
+        a.f += __shfl_xor_sync(mask, a.f, o);
+    }
+    __device__ __forceinline__ X result(const Acc &a) const { return a.d + f2d_bits(a.f); }
+};
+
+}  // namespace cigpu

@@ -95,10 +95,9 @@ def main() -> None:
         e1.record(stream)
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / args.reps
-        sv = 4 if f32 else 8
         n = dim.value
-        alg = nf.value * (sv + 4) + 8 * (n + 1) + 2 * n * sv if args.kernel != "matvec_hilo" else nf.value * 12 + 8 * (n + 1) + 16 * n
-        out.update({"dim": n, "nnz_full": nf.value, "ms_per_launch": t, "algorithmic_bytes": alg,
+        alg, layout = A.matvec_bytes(crs, f32)
+        out.update({"dim": n, "nnz_full": nf.value, "layout": layout, "ms_per_launch": t, "algorithmic_bytes": alg,
                     "achieved_gbs": alg / (t / 1000) / 1e9})
         lib.cigpu_crs_destroy(crs)
     lib.cigpu_ham_destroy(ham)

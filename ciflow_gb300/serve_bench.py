@@ -115,8 +115,14 @@ def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed:
     e_ref = np.array([r["e0"] for r in ref_results])
     dm = np.abs(np.array([r["e0"] for r in res_m]) - e_ref)
     dp = np.abs(np.array([r["e0"] for r in res_p]) - e_ref)
+    def failures(res, de, tol_e=1e-6):
+        return [{"i": i, "kind": stream[i][0], "dim": r["dim"], "status": r["status"], "dE0": float(de[i]),
+                 "residual": r["residual"], "mv32": r["matvecs_fp32"], "mv64": r["matvecs_fp64"]}
+                for i, r in enumerate(res) if r["status"] != A.OK or de[i] > tol_e][:10]
+
     out = {
         "requests": n, "arrival_rate_per_s": rate, "max_inflight": max_inflight,
+        "failures": {"mixed": failures(res_m, dm), "plain_fp64": failures(res_p, dp)},
         "mix": {k: sum(1 for s in stream if s[0] == k) for k in ("c4", "c3", "c1")},
         "dims": {"min": min(r["dim"] for r in res_m), "max": max(r["dim"] for r in res_m)},
         "mixed": summarise(stream, res_m, wall_m) | {"max_abs_dE0": float(dm.max()), "tol": tol_mixed},

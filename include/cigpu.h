@@ -96,6 +96,13 @@ int cigpu_ham_destroy(cigpu_ham *ham);
 int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, cigpu_crs **out);
 int cigpu_crs_destroy(cigpu_crs *crs);
 int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full);
+/* Device storage of the matrix (no reference counterpart; reported with matvec
+ * measurements). CIGPU_LAYOUT_CRS: full symmetric CRS, stored = nnz_full values
+ * with a 4-byte column each. CIGPU_LAYOUT_SLOTS (MIXED FCI): values only, every
+ * structural slot of a row at a fixed stride, stored = dim * stride; columns are
+ * regenerated from the string tables. */
+enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1 };
+int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored);
 /* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
  * SparseMatrix_CRS.h:107-111): row[dim+1], col[nnz_upper], val[nnz_upper]. Host buffers. */
 int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val);
@@ -105,7 +112,8 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
 /* ---- matvec: replaces SparseMatrix_CRS_Sym::mvprod(const double*, double*)
  * (SparseMatrix_CRS.cpp:700-723; virtual at SparseMatrix_CRS.h:126).
  * Host buffers x, y of length dim; FP64 arithmetic (for a MIXED CRS the FP64
- * product regenerates the elements on the fly). ---- */
+ * product uses the stored FP32 split of each value, v = hi + lo, exact to
+ * 2^-48 relative). ---- */
 int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y);
 /* Device-buffer form on the given stream. dtype 0: FP64 x/y (FP64 matvec);
  * dtype 1: FP32 x/y (FP32 values, FP32 accumulation; MIXED CRS only). */

@@ -31,7 +31,7 @@ def test_mvprod_matches_reference_matvec(name, precision):
     y_ref = O.sym_mvprod(ref, x, threaded=True)
     y = m.mvprod(x)
     scale = np.abs(y_ref).max()
-    # FP64 product (regenerated elements for the mixed CRS): summation order only
+    # FP64 product (from the split FP32 values hi + lo for the mixed CRS): summation order only
     assert np.abs(y - y_ref).max() <= 1e-12 * scale
 
 
@@ -137,3 +137,21 @@ def test_small_spaces_match_dense_eigensolve(shape, precision):
     tol = 1e-8 if precision == A.FP64 else 1e-6
     assert abs(cim.get_ci_energy() - ints.econst - e_ref) <= tol
     assert cim.info["converged"]
+
+
+# (L, electrons per spin, seed): spaces where the lowest-diagonal determinant overlaps
+# the ground state weakly, so a Davidson started from it alone settles on an excited state
+HARD_STARTS = [(7, 1, 1123), (11, 1, 1109), (7, 1, 1234), (10, 4, 1237)]
+
+
+@pytest.mark.parametrize("case", HARD_STARTS, ids=lambda c: "L%d-%d-s%d" % c)
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_solver_finds_the_ground_state(case, precision):
+    import scipy.sparse.linalg as sla
+    L, ne, seed = case
+    ints = make_integrals(L, ne, ne, nchol=16, seed=seed)
+    H = O.build_upper(O.FCI, ints).full_csr()
+    e_ref = sla.eigsh(H, k=1, which="SA", tol=1e-12)[0][0] if H.shape[0] > 2000 else np.linalg.eigvalsh(H.toarray())[0]
+    cim = build(FCI, ints, precision)
+    cim.solve(tol=1e-6)
+    assert abs(cim.get_ci_energy() - ints.econst - e_ref) <= 1e-6
