@@ -220,7 +220,8 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
     // col + values (FP64, or FP32 hi + lo); the mixed FCI layout stores values only
     size_t b = (size_t)dim * W * 12;
-    if (method == CIGPU_FCI && precision == CIGPU_MIXED) b = (size_t)dim * ((W + 3) & ~(int64_t)3) * 8;
+    if (method == CIGPU_FCI && precision == CIGPU_MIXED)  // slot tiles of 64 beta strings, hi + lo
+        b = (size_t)binom64(L, nup) * ((binom64(L, ndown) + 63) / 64 * 64) * W * 8;
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
     b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
     b += (size_t)dim * 8 * 5;                    // c, refinement vectors
@@ -302,7 +303,6 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
         singles.make(c, p, s);
-        p.Wp = slots_stride(p);
         c.slots = c.precision == CIGPU_MIXED && slots_supported(p);
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
@@ -340,10 +340,10 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     }
     count.release();
     tr.mark("scans");
-    const int mode = c.slots ? kFillSlots : (c.precision == CIGPU_MIXED ? kFill32 : kFill64);
+    const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
     if (c.slots) {
-        c.val32.alloc((size_t)dim * c.fp.Wp);
-        c.val32lo.alloc((size_t)dim * c.fp.Wp);
+        c.val32.alloc(slots_count(c.fp));
+        c.val32lo.alloc(slots_count(c.fp));
     } else if (mode == kFill64) {
         c.col.alloc(c.nnz_full);
         c.val64.alloc(c.nnz_full);
@@ -359,7 +359,10 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         c.fp.val64 = c.val64.p;
         c.fp.val32 = c.val32.p;
         c.fp.val32lo = c.val32lo.p;
-        fci_launch(mode, c.fp, s);
+        if (c.slots)
+            fill_slots_launch(c.fp, c.val32.p, c.val32lo.p, s);
+        else
+            fci_launch(mode, c.fp, s);
     } else {
         c.dp.row_ptr = c.row_ptr.p;
         c.dp.col = c.col.p;
@@ -603,7 +606,7 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
     if (!crs) return CIGPU_EINVAL;
     if (layout) *layout = crs->slots ? CIGPU_LAYOUT_SLOTS : CIGPU_LAYOUT_CRS;
-    if (stored) *stored = crs->slots ? crs->dim * crs->fp.Wp : crs->nnz_full;
+    if (stored) *stored = crs->slots ? slots_count(crs->fp) : crs->nnz_full;
     return CIGPU_OK;
 }
 

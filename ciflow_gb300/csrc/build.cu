@@ -118,8 +118,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
     const int L = p.L, L2 = L * L;
     const int nsa = p.a.ns;
     const int W = p.b.nfull + nsa * p.b.nsing + p.a.nd;
-    constexpr bool F32 = (MODE == kFill32 || MODE == kFillSlots);
-    const int Wloop = MODE == kFillSlots ? (int)p.Wp : W;  // slots also write the zero padding
+    constexpr bool F32 = MODE == kFill32;
     uint64_t *nbA = reinterpret_cast<uint64_t *>(smem);
     uint32_t *gstart = reinterpret_cast<uint32_t *>(nbA + nga);
     uint16_t *gmap = reinterpret_cast<uint16_t *>(gstart + nga + 1);
@@ -185,7 +184,7 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
         int64_t base = 0;
         if (MODE == kFill64 || MODE == kFill32) base = p.row_ptr[r];
         uint32_t running = 0, nlow = 0;
-        for (int k0 = 0; k0 < Wloop; k0 += 32) {
+        for (int k0 = 0; k0 < W; k0 += 32) {
             const int k = k0 + lane;
             uint64_t vb = 0;       // FP64 bits (COUNT / FILL64 / MATVEC, and computed elements)
             float hi = 0, lo = 0;  // FILL32
@@ -293,14 +292,6 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
                     keep = (__float_as_uint(hi) & 0x7FFFFFFFu) != 0u;  // splits are zero where |v| <= 1e-14
                 else
                     keep = keep_bits(vb);
-            }
-            if (MODE == kFillSlots) {
-                if (k < Wloop) {
-                    const int64_t at = r * p.Wp + k;
-                    p.val32[at] = keep ? hi : 0.0f;
-                    p.val32lo[at] = keep ? lo : 0.0f;
-                }
-                continue;
             }
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (MODE == kCount) {
@@ -528,21 +519,19 @@ void fci_launch(int mode, const FciParams &p0, cudaStream_t s) {
     p.staged = (sm == fci_base_smem(p) + fci_slice_smem(p)) ? 1 : 0;
     const int64_t nchunks = (p.Db + kFciRowsPerBlock - 1) / kFciRowsPerBlock;
     const int64_t blocks = p.a.D * nchunks;
-    if ((mode == kFill32 || mode == kFillSlots) && (!p.eri_hi || !p.eri_lo))
+    if (mode == kFill32 && (!p.eri_hi || !p.eri_lo))
         throw CudaError{cudaErrorInvalidValue, "FP32 integral tables missing"};
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fci_rows<kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         cudaFuncSetAttribute(k_fci_rows<kFill32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
-        cudaFuncSetAttribute(k_fci_rows<kFillSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFciMaxSmem);
         return true;
     }();
     (void)attr_set;
     switch (mode) {
         case kCount: k_fci_rows<kCount><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
         case kFill64: k_fci_rows<kFill64><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
-        case kFill32: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
-        default: k_fci_rows<kFillSlots><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
+        default: k_fci_rows<kFill32><<<(unsigned)blocks, kFciThreads, sm, s>>>(p); break;
     }
     CIGPU_CUDA(cudaGetLastError());
     count_launch();

@@ -5,11 +5,7 @@
 
 namespace cigpu {
 
-// kFillSlots: the mixed method's values-only FCI layout. Every structural slot of
-// a row (W of them, the same count for every row) is written at r * Wp + k with no
-// column index; dropped elements (|v| <= 1e-14) are stored as zero. The columns are
-// regenerated from the string tables by the matvec (k_spmv_slots).
-enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2, kFillSlots = 3 };
+enum BuildMode { kCount = 0, kFill64 = 1, kFill32 = 2 };
 
 constexpr int kFciThreads = 256;
 constexpr int kFciRowsPerBlock = 64;
@@ -38,7 +34,6 @@ struct FciParams {
     double *val64;
     float *val32;
     float *val32lo;  // v - (double)hi, rounded to FP32 (FP32 fill only)
-    int64_t Wp;      // slot stride of the values-only layout (W rounded up to 4)
 };
 
 struct DociParams {

@@ -24,8 +24,8 @@ struct cigpu_crs {
     cigpu::DevBuf<double> val64;
     cigpu::DevBuf<float> val32;
     cigpu::DevBuf<float> val32lo;  // MIXED: FP32 rounding remainder of each value
-    // MIXED FCI: values-only layout (val32/val32lo hold dim x Wp slots, no col);
-    // row_ptr/upper_off/nnz still describe the explicit matrix for export
+    // MIXED FCI: values-only slot tiles (val32/val32lo hold slots_count(fp) values,
+    // no col); row_ptr/upper_off/nnz still describe the explicit matrix for export
     bool slots = false;
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};

@@ -1,16 +1,19 @@
-// Values-only FCI matvec of the mixed method (slots.cu).
+// Values-only FCI layout of the mixed method ("slot tiles", slots.cu).
 #pragma once
 
 #include "build.cuh"
 
 namespace cigpu {
 
-constexpr size_t kSlotsMaxSmem = 96 * 1024;  // slot descriptors of one row (8 bytes per slot)
+constexpr int kTileRows = 64;                // beta strings per tile (rows of one alpha string)
+constexpr size_t kSlotsMaxSmem = 96 * 1024;  // per-block shared memory of the slot kernels
 
-// Whether the slot descriptors of a row fit in shared memory (W up to ~12,000).
+// Whether the layout applies (its shared-memory tables fit; indices fit 32 bits).
 bool slots_supported(const FciParams &p);
-// Slot stride Wp: the row width rounded up to a multiple of 4.
-int64_t slots_stride(const FciParams &p);
+// Stored values (FP32 each, hi and lo arrays): tiles x W x kTileRows.
+int64_t slots_count(const FciParams &p);
+// Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p).
+void fill_slots_launch(const FciParams &p, float *hi, float *lo, cudaStream_t s);
 // y = H x from FP32 slot values, FP32 x/y and accumulation.
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s);
 // FP64 y = H x from the split slot values hi + lo.

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int
     const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
     for (int64_t r = gid; r < n; r += ng) {
         const int64_t s = row_ptr[r], e = row_ptr[r + 1];
-        typename F::Acc acc;
+        typename F::Acc acc{};
         // scalar head up to a 16-byte boundary of both arrays (4 elements)
         const int64_t s4 = (s + 3) & ~(int64_t)3;
         const int64_t head_end = s4 < e ? s4 : e;

@@ -17,8 +17,8 @@ template <typename VT>
 struct Plain {
     using X = VT;
     const VT *__restrict__ val;
-    struct Acc {
-        VT s = 0;
+    struct Acc {  // value-initialise (Acc a{}) to zero
+        VT s;
     };
     struct Chunk {
         VT v[4];
@@ -28,6 +28,7 @@ struct Plain {
     __device__ __forceinline__ void fma(const Chunk &c, int j, X xv, Acc &a) const { a.s += c.v[j] * xv; }
     __device__ __forceinline__ void fma1(int64_t at, X xv, Acc &a) const { a.s += __ldcs(val + at) * xv; }
     __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const { a.s += __shfl_xor_sync(mask, a.s, o); }
+    __device__ __forceinline__ void add(Acc &a, const Acc &b) const { a.s += b.s; }
     __device__ __forceinline__ X result(const Acc &a) const { return a.s; }
 };
 template <>
@@ -69,9 +70,9 @@ struct HiLo {
     using X = double;
     const float *__restrict__ hi;
     const float *__restrict__ lo;
-    struct Acc {
-        double d = 0;
-        float f = 0;
+    struct Acc {  // value-initialise (Acc a{}) to zero
+        double d;
+        float f;
     };
     struct Chunk {
         float4 h, l;
@@ -94,6 +95,10 @@ struct HiLo {
     __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const {
         a.d += __shfl_xor_sync(mask, a.d, o);
         a.f += __shfl_xor_sync(mask, a.f, o);
+    }
+    __device__ __forceinline__ void add(Acc &a, const Acc &b) const {
+        a.d += b.d;
+        a.f += b.f;
     }
     __device__ __forceinline__ X result(const Acc &a) const { return a.d + f2d_bits(a.f); }
 };

@@ -99,8 +99,9 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
 /* Device storage of the matrix (no reference counterpart; reported with matvec
  * measurements). CIGPU_LAYOUT_CRS: full symmetric CRS, stored = nnz_full values
  * with a 4-byte column each. CIGPU_LAYOUT_SLOTS (MIXED FCI): values only, every
- * structural slot of a row at a fixed stride, stored = dim * stride; columns are
- * regenerated from the string tables. */
+ * structural slot of every row (zeros included, rows padded to tiles of 64 beta
+ * strings), stored = that slot count; columns are regenerated from the string
+ * tables. */
 enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1 };
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored);
 /* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
