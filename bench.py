@@ -42,6 +42,10 @@ def parse_args():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--tol", type=float, default=1e-5, help="FP64 residual target (|dE0| ~ tol^2/gap)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--served-requests", type=int, default=200,
+                    help="served-stream requests per form (0 skips the served stream)")
+    ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
+    ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
     return ap.parse_args()
 
 
@@ -346,6 +350,20 @@ def run_cigpu(args, rank: int, world: int, dist):
            "h2d_bytes_per_step": int(h.nbytes + eri.nbytes), "d2h_bytes_per_step": int(c_host.nbytes),
            "path": "cigpu_ham_create + cigpu_build(MIXED) + cigpu_solve(c_out host), pageable host buffers"}
 
+    # served stream: L=10 5a5b FCI under random orbital rotations mixed with uneven
+    # problems, Poisson arrivals into the continuous-batching server, both forms
+    served = None
+    if args.served_requests > 0:
+        from ciflow_gb300.serve_bench import served as run_served
+        barrier()
+        served = run_served(args.served_requests, args.served_rate, args.served_inflight, tol_mixed=args.tol,
+                            tol_fp64=args.tol, seed=4 + rank)
+        if dist is not None:
+            t = torch.tensor([served["mixed"]["solves_per_s"], served["plain_fp64"]["solves_per_s"]], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+            served["mixed"]["solves_per_s_all_ranks"] = float(t[0].item())
+            served["plain_fp64"]["solves_per_s_all_ranks"] = float(t[1].item())
+
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
@@ -370,6 +388,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "e2e": e2e, "gpu_launches": launches_mixed,
         "gpu_launches_plain": launches_plain,
         "clocks": clk.summary(),
+        "served": served,
         "cpu_baseline": cpu,
     }
     print(json.dumps(out), flush=True)

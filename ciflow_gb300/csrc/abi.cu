@@ -380,8 +380,12 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
 }
 
 void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
+    if (c.precision == CIGPU_MIXED) {
+        if (!c.x32.p) c.x32.alloc(std::max<int64_t>(c.dim, 1));
+        dev_convert(x, c.x32.p, c.dim, s);
+    }
     if (c.slots) {
-        spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, y, s);
+        spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
         return;
     }
     if (c.precision == CIGPU_FP64) {
@@ -391,7 +395,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
     if (c.val32lo.p || c.nnz_full == 0) {
         // MIXED CRS: FP64 product with values hi + lo (|v - hi - lo| <= 2^-48 |v|);
         // an all-zero matrix (e.g. no electrons) has no value arrays at all
-        spmv_hilo(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, y, s);
+        spmv_hilo(c.dim, c.nnz_full, c.row_ptr.p, c.col.p, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
         return;
     }
     throw std::invalid_argument("MIXED CRS without its FP32 remainder array");

@@ -72,7 +72,6 @@ template <typename F>
 struct MatvecRun {
     const FciParams &p;
     const F &f;
-    const typename F::X *__restrict__ x;
     const uint32_t *st;  // [nsb][kTileRows] beta single targets of the tile rows (shared)
     int64_t ia, ib, vbase;
     int rr;
@@ -84,29 +83,28 @@ struct MatvecRun {
             // alpha doubles: one slot per xa, beta self
             for (int xd = xb0; xd < xb1; ++xd, ++k) {
                 const int64_t J = __ldg(p.a.d_target + ia * p.a.nd + xa + (xd - xb0));
-                f.fma1(vbase + (int64_t)k * kTileRows, __ldg(x + J * p.Db + ib), acc);
+                f.term1(vbase + (int64_t)k * kTileRows, J * p.Db + ib, acc);
             }
             return;
         }
-        const typename F::X *pan = x + Ja * p.Db;
+        const int64_t pan = Ja * p.Db;  // x panel of alpha string Ja
         if (kindB == kSelf) {
-            f.fma1(vbase + (int64_t)k * kTileRows, __ldg(pan + ib), acc);
+            f.term1(vbase + (int64_t)k * kTileRows, pan + ib, acc);
         } else if (kindB == kSingle) {
 #pragma unroll 4
             for (int xb = xb0; xb < xb1; ++xb, ++k)
-                f.fma1(vbase + (int64_t)k * kTileRows, __ldg(pan + st[xb * kTileRows + rr]), acc);
+                f.term1(vbase + (int64_t)k * kTileRows, pan + st[xb * kTileRows + rr], acc);
         } else {
             const uint32_t *dt = p.b.d_target + ib * p.b.nd;
 #pragma unroll 4
             for (int xb = xb0; xb < xb1; ++xb, ++k)
-                f.fma1(vbase + (int64_t)k * kTileRows, __ldg(pan + __ldg(dt + xb)), acc);
+                f.term1(vbase + (int64_t)k * kTileRows, pan + __ldg(dt + xb), acc);
         }
     }
 };
 
 template <typename F>
 __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, const F f,
-                                                             const typename F::X *__restrict__ x,
                                                              typename F::X *__restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *st = reinterpret_cast<uint32_t *>(smem);  // [nsb][kTileRows]
@@ -125,7 +123,7 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int W = fci_row_width(p);
-    MatvecRun<F> v{p, f, x, st, ia, active ? ib_raw : p.Db - 1, (ia * T + t) * (int64_t)W * kTileRows + rr, rr, {}};
+    MatvecRun<F> v{p, f, st, ia, active ? ib_raw : p.Db - 1, (ia * T + t) * (int64_t)W * kTileRows + rr, rr, {}};
     walk_slots(p, (int)((int64_t)W * ks / kSplits), (int)((int64_t)W * (ks + 1) / kSplits), v);
     part[ks][rr] = v.acc;
     __syncthreads();
@@ -239,14 +237,14 @@ size_t matvec_smem(const FciParams &p) { return (size_t)p.b.ns * kTileRows * 4; 
 size_t fill_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
 
 template <typename F>
-void launch_slots(const FciParams &p, const F &f, const typename F::X *x, typename F::X *y, cudaStream_t s) {
+void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t s) {
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_spmv_slots<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
         return true;
     }();
     (void)attr_set;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    k_spmv_slots<F><<<(unsigned)(p.a.D * T), kSlotThreads, matvec_smem(p), s>>>(p, f, x, y);
+    k_spmv_slots<F><<<(unsigned)(p.a.D * T), kSlotThreads, matvec_smem(p), s>>>(p, f, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -278,12 +276,12 @@ void fill_slots_launch(const FciParams &p0, float *hi, float *lo, cudaStream_t s
 }
 
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s) {
-    launch_slots(p, Plain<float>{val}, x, y, s);
+    launch_slots(p, Plain<float>{val, x}, y, s);
 }
 
-void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, double *y,
-                     cudaStream_t s) {
-    launch_slots(p, HiLo{hi, lo}, x, y, s);
+void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, const float *x32,
+                     double *y, cudaStream_t s) {
+    launch_slots(p, HiLo{hi, lo, x, x32}, y, s);
 }
 
 }  // namespace cigpu

@@ -16,8 +16,8 @@ int64_t slots_count(const FciParams &p);
 void fill_slots_launch(const FciParams &p, float *hi, float *lo, cudaStream_t s);
 // y = H x from FP32 slot values, FP32 x/y and accumulation.
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s);
-// FP64 y = H x from the split slot values hi + lo.
-void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, double *y,
-                     cudaStream_t s);
+// FP64 y = H x from the split slot values hi + lo; x32 is an FP32 copy of x.
+void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, const float *x32,
+                     double *y, cudaStream_t s);
 
 }  // namespace cigpu

@@ -28,7 +28,6 @@ namespace {
 template <typename F, int G, int U>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int64_t *__restrict__ row_ptr,
                                                             const uint32_t *__restrict__ col, const F f,
-                                                            const typename F::X *__restrict__ x,
                                                             typename F::X *__restrict__ y) {
     const int lane = threadIdx.x & (G - 1);
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
@@ -40,7 +39,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int
         // scalar head up to a 16-byte boundary of both arrays (4 elements)
         const int64_t s4 = (s + 3) & ~(int64_t)3;
         const int64_t head_end = s4 < e ? s4 : e;
-        if (s + lane < head_end) f.fma1(s + lane, __ldg(x + __ldcs(col + s + lane)), acc);
+        if (s + lane < head_end) f.term1(s + lane, __ldcs(col + s + lane), acc);
         const int64_t nb = (e > s4) ? ((e - s4) >> 2) : 0;
         const uint4 *c4 = reinterpret_cast<const uint4 *>(col + s4);
         for (int64_t b0 = 0; b0 < nb; b0 += G * U) {
@@ -60,16 +59,16 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (b0 + u * G + lane < nb) {
-                    f.fma(v[u], 0, __ldg(x + c[u].x), acc);
-                    f.fma(v[u], 1, __ldg(x + c[u].y), acc);
-                    f.fma(v[u], 2, __ldg(x + c[u].z), acc);
-                    f.fma(v[u], 3, __ldg(x + c[u].w), acc);
+                    f.term(v[u], 0, c[u].x, acc);
+                    f.term(v[u], 1, c[u].y, acc);
+                    f.term(v[u], 2, c[u].z, acc);
+                    f.term(v[u], 3, c[u].w, acc);
                 }
             }
         }
         // scalar tail (< 4 elements)
         const int64_t t0 = s4 + (nb << 2);
-        if (e > s4 && t0 + lane < e) f.fma1(t0 + lane, __ldg(x + __ldcs(col + t0 + lane)), acc);
+        if (e > s4 && t0 + lane < e) f.term1(t0 + lane, __ldcs(col + t0 + lane), acc);
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) f.reduce(acc, gmask, o);
         if (lane == 0) y[r] = f.result(acc);
@@ -95,34 +94,34 @@ int sm_count_spmv() {
 // free for the kernels of concurrent solves on other streams.
 template <typename F>
 static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const F &f,
-                        const typename F::X *x, typename F::X *y, cudaStream_t s) {
+                        typename F::X *y, cudaStream_t s) {
     const double chunks = n > 0 ? (double)nnz / n / 4.0 : 0;
     const int G = chunks >= 48 ? 32 : chunks >= 20 ? 16 : 8;
     const int64_t need = (n * G + kSpmvThreads - 1) / kSpmvThreads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(spmv_grid(), need));
     if (G == 32)
-        k_spmv_rows<F, 32, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, x, y);
+        k_spmv_rows<F, 32, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y);
     else if (G == 16)
-        k_spmv_rows<F, 16, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, x, y);
+        k_spmv_rows<F, 16, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y);
     else
-        k_spmv_rows<F, 8, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, x, y);
+        k_spmv_rows<F, 8, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
 
 void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
               double *y, cudaStream_t s) {
-    launch_rows(n, nnz, row_ptr, col, Plain<double>{val}, x, y, s);
+    launch_rows(n, nnz, row_ptr, col, Plain<double>{val, x}, y, s);
 }
 
 void spmv_f32(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x,
               float *y, cudaStream_t s) {
-    launch_rows(n, nnz, row_ptr, col, Plain<float>{val}, x, y, s);
+    launch_rows(n, nnz, row_ptr, col, Plain<float>{val, x}, y, s);
 }
 
 void spmv_hilo(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *hi, const float *lo,
-               const double *x, double *y, cudaStream_t s) {
-    launch_rows(n, nnz, row_ptr, col, HiLo{hi, lo}, x, y, s);
+               const double *x, const float *x32, double *y, cudaStream_t s) {
+    launch_rows(n, nnz, row_ptr, col, HiLo{hi, lo, x, x32}, y, s);
 }
 
 }  // namespace cigpu

@@ -15,7 +15,8 @@ void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *co
 void spmv_f32(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
               cudaStream_t s);
 
+// x32: FP32 copy of x (for the low parts)
 void spmv_hilo(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *hi, const float *lo,
-               const double *x, double *y, cudaStream_t s);
+               const double *x, const float *x32, double *y, cudaStream_t s);
 
 }  // namespace cigpu

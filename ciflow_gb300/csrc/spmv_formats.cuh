@@ -6,17 +6,20 @@
 
 namespace cigpu {
 
-// Value formats. A format loads 4 values with 16-byte loads (load4) or one value
-// (load1) and accumulates value * x into its accumulator.
+// Value formats. A format holds the matrix values and x; it loads 4 values with
+// 16-byte loads (load4) and accumulates value * x[col] for one of them (term), or
+// loads one value and accumulates it (term1).
 //   Plain<VT>: VT values, VT x/y, VT accumulation (FP64 method, FP32 matvec).
 //   HiLo: FP64 product from split FP32 values v = hi + lo (|v - hi - lo| <= 2^-48 |v|):
 //     hi * x accumulates in FP64 (one DFMA per element); lo * x is at most 2^-24 of
-//     the term, so FP32 arithmetic for it adds below 2^-48 relative error while
-//     halving the FP64 instructions (GB300 issues FP64 at 1/64 of the FP32 rate).
+//     the term, so it accumulates in FP32 from an FP32 copy of x (x32), adding below
+//     2^-48 relative error while keeping FP64 instructions to one per element
+//     (GB300 issues FP64 at 1/64 of the FP32 rate).
 template <typename VT>
 struct Plain {
     using X = VT;
     const VT *__restrict__ val;
+    const VT *__restrict__ x;
     struct Acc {  // value-initialise (Acc a{}) to zero
         VT s;
     };
@@ -25,8 +28,12 @@ struct Plain {
     };
     __device__ __forceinline__ void load4(int64_t at, Chunk &c) const;
     __device__ __forceinline__ void zero(Chunk &c) const { c.v[0] = c.v[1] = c.v[2] = c.v[3] = 0; }
-    __device__ __forceinline__ void fma(const Chunk &c, int j, X xv, Acc &a) const { a.s += c.v[j] * xv; }
-    __device__ __forceinline__ void fma1(int64_t at, X xv, Acc &a) const { a.s += __ldcs(val + at) * xv; }
+    __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
+        a.s += c.v[j] * __ldg(x + col);
+    }
+    __device__ __forceinline__ void term1(int64_t at, int64_t col, Acc &a) const {
+        a.s += __ldcs(val + at) * __ldg(x + col);
+    }
     __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const { a.s += __shfl_xor_sync(mask, a.s, o); }
     __device__ __forceinline__ void add(Acc &a, const Acc &b) const { a.s += b.s; }
     __device__ __forceinline__ X result(const Acc &a) const { return a.s; }
@@ -70,6 +77,8 @@ struct HiLo {
     using X = double;
     const float *__restrict__ hi;
     const float *__restrict__ lo;
+    const double *__restrict__ x;
+    const float *__restrict__ x32;  // FP32 copy of x
     struct Acc {  // value-initialise (Acc a{}) to zero
         double d;
         float f;
@@ -82,15 +91,15 @@ struct HiLo {
         c.l = __ldcs(reinterpret_cast<const float4 *>(lo + at));
     }
     __device__ __forceinline__ void zero(Chunk &c) const { c.h = c.l = make_float4(0, 0, 0, 0); }
-    __device__ __forceinline__ void fma(const Chunk &c, int j, X xv, Acc &a) const {
+    __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
         const float h = j == 0 ? c.h.x : j == 1 ? c.h.y : j == 2 ? c.h.z : c.h.w;
         const float l = j == 0 ? c.l.x : j == 1 ? c.l.y : j == 2 ? c.l.z : c.l.w;
-        a.d = ::fma(f2d_bits(h), xv, a.d);
-        a.f = fmaf(l, d2f_trunc(xv), a.f);
+        a.d = ::fma(f2d_bits(h), __ldg(x + col), a.d);
+        a.f = fmaf(l, __ldg(x32 + col), a.f);
     }
-    __device__ __forceinline__ void fma1(int64_t at, X xv, Acc &a) const {
-        a.d = ::fma(f2d_bits(__ldcs(hi + at)), xv, a.d);
-        a.f = fmaf(__ldcs(lo + at), d2f_trunc(xv), a.f);
+    __device__ __forceinline__ void term1(int64_t at, int64_t col, Acc &a) const {
+        a.d = ::fma(f2d_bits(__ldcs(hi + at)), __ldg(x + col), a.d);
+        a.f = fmaf(__ldcs(lo + at), __ldg(x32 + col), a.f);
     }
     __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const {
         a.d += __shfl_xor_sync(mask, a.d, o);
