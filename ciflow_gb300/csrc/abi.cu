@@ -307,8 +307,16 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
-        fci_launch(kCount, p, s);
-        tr.mark("count pass");
+        if (c.slots) {
+            // values-only layout: the fill counts the rows itself
+            c.val32.alloc(slots_count(p));
+            c.val32lo.alloc(slots_count(p));
+            fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
+            tr.mark("slot fill");
+        } else {
+            fci_launch(kCount, p, s);
+            tr.mark("count pass");
+        }
     } else {
         c.strings.alloc(dim);
         doci_strings_launch(c.L, c.nup, dim, c.strings.p, s);
@@ -342,8 +350,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     tr.mark("scans");
     const int mode = c.precision == CIGPU_MIXED ? kFill32 : kFill64;
     if (c.slots) {
-        c.val32.alloc(slots_count(c.fp));
-        c.val32lo.alloc(slots_count(c.fp));
+        // filled above
     } else if (mode == kFill64) {
         c.col.alloc(c.nnz_full);
         c.val64.alloc(c.nnz_full);
@@ -359,10 +366,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         c.fp.val64 = c.val64.p;
         c.fp.val32 = c.val32.p;
         c.fp.val32lo = c.val32lo.p;
-        if (c.slots)
-            fill_slots_launch(c.fp, c.val32.p, c.val32lo.p, s);
-        else
-            fci_launch(mode, c.fp, s);
+        if (!c.slots) fci_launch(mode, c.fp, s);
     } else {
         c.dp.row_ptr = c.row_ptr.p;
         c.dp.col = c.col.p;

@@ -14,16 +14,20 @@
 // the split values.
 //
 // Rows are grouped in tiles of kTileRows consecutive beta strings of one alpha
-// string; a tile stores its values slot-major, val[(tile * W + k) * kTileRows + row],
-// so a warp (32 rows) reads one slot of 32 rows with one coalesced 128-byte load and
-// every lane of the warp executes the same slot kind. The x entries a slot reads all
-// lie in the panel x[Ja * Db .. Ja * Db + Db) of one alpha string (L1-resident while
-// the slot run lasts). Elements with |v| <= 1e-14 are stored as zero; padding rows
-// of the last tile are zero and never written back.
+// string. Within a tile the values are stored in quads of 4 consecutive slots per
+// row, quad-major: val[((tile * Q + c) * kTileRows + row) * 4 + j] for slot 4c + j
+// (Q = ceil(W / 4), padding slots zero). A warp (32 rows) reads one quad of 32 rows
+// with one fully coalesced 512-byte load, 16 bytes per lane, and every lane handles
+// the same slot kinds. The slot -> (Ja, beta kind, xb) descriptors of the tile's
+// alpha string sit in shared memory and are read as broadcasts; the x entries a slot
+// reads all lie in the panel x[Ja * Db .. Ja * Db + Db) of one alpha string.
+// Elements with |v| <= 1e-14 are stored as zero; padding rows of the last tile are
+// zero and never written back.
 //
 // Replaces SparseMatrix_CRS_Sym::mvprod (SparseMatrix_CRS.cpp:700-723) for the FP32
-// values of the mixed method; the build below produces the same element values as
-// the CRS generator (build.cu), in slot order.
+// values of the mixed method. The fill below produces the same element values as
+// the CRS generator (build.cu), in slot order, and counts each row's stored
+// nonzeros and lower-triangle nonzeros on the way (the CRS row pointers of export).
 #include <algorithm>
 
 #include "slots.cuh"
@@ -33,99 +37,99 @@ namespace cigpu {
 
 namespace {
 
-constexpr int kSlotThreads = 256;  // 2 row halves x 4 slot quarters
+constexpr int kSlotThreads = 256;  // 2 row halves x 4 quad ranges
 constexpr int kSplits = 4;
+constexpr uint32_t kPad = 3;  // descriptor beta kind of a padding slot
 
-// Walks slots [k0, k1) in homogeneous runs: v.run(kindA, xa, kindB, xb0, xb1, k)
-// covers slots k .. k + (xb1 - xb0) - 1.
-template <typename V>
-__device__ __forceinline__ void walk_slots(const FciParams &p, int k0, int k1, V &v) {
-    const int nsa = p.a.ns, nda = p.a.nd, nsb = p.b.ns, ndb = p.b.nd;
-    const int WA = 1 + nsb + ndb, WS = 1 + nsb;
-    const int kS = WA, kD = WA + nsa * WS;
-    auto piece = [&](int kindA, int xa, int kindB, int xb_first, int k_first, int len) {
-        const int a = max(k_first, k0), b = min(k_first + len, k1);
-        if (a < b) v.run(kindA, xa, kindB, xb_first + (a - k_first), xb_first + (b - k_first), a);
-    };
-    if (k0 < WA) {
-        piece(kSelf, 0, kSelf, 0, 0, 1);
-        piece(kSelf, 0, kSingle, 0, 1, nsb);
-        piece(kSelf, 0, kDouble, 0, 1 + nsb, ndb);
+// Descriptor of slot k of alpha string ia: Ja | beta kind << 32 | xb << 34.
+__device__ __forceinline__ uint64_t slot_desc(const FciParams &p, int64_t ia, int k, int W) {
+    if (k >= W) return (uint64_t)kPad << 32;
+    const int nsa = p.a.ns, nsb = p.b.ns, ndb = p.b.nd;
+    const int WA = 1 + nsb + ndb, WS = 1 + nsb, kD = WA + nsa * WS;
+    uint64_t Ja, kindB, xb = 0;
+    if (k < WA) {
+        Ja = (uint64_t)ia;
+        kindB = k == 0 ? kSelf : (k <= nsb ? kSingle : kDouble);
+        if (k > 0) xb = k <= nsb ? k - 1 : k - 1 - nsb;
+    } else if (k < kD) {
+        const int xa = (k - WA) / WS, q = (k - WA) - xa * WS;
+        Ja = __ldg(p.a.s_target + ia * nsa + xa);
+        kindB = q == 0 ? kSelf : kSingle;
+        if (q > 0) xb = q - 1;
+    } else {
+        Ja = __ldg(p.a.d_target + ia * p.a.nd + (k - kD));
+        kindB = kSelf;
     }
-    if (k1 > kS && k0 < kD) {
-        const int x0 = max(0, (k0 - kS) / WS), x1 = min(nsa, (k1 - kS + WS - 1) / WS);
-        for (int xa = x0; xa < x1; ++xa) {
-            const int kb = kS + xa * WS;
-            piece(kSingle, xa, kSelf, 0, kb, 1);
-            piece(kSingle, xa, kSingle, 0, kb + 1, nsb);
-        }
-    }
-    if (k1 > kD) {  // alpha doubles: one slot per xa, passed as one run over xa
-        const int a = max(k0, kD), b = min(k1, kD + nda);
-        if (a < b) v.run(kDouble, a - kD, kSelf, 0, b - a, a);
-    }
+    return Ja | (kindB << 32) | (xb << 34);
 }
 
-// ---------------------------------------------------------------------------
-// Matvec. Block = one tile; warp w: rows (w & 1) * 32 + lane, slot quarter w >> 1.
-template <typename F>
-struct MatvecRun {
-    const FciParams &p;
-    const F &f;
-    const uint32_t *st;  // [nsb][kTileRows] beta single targets of the tile rows (shared)
-    int64_t ia, ib, vbase;
-    int rr;
-    typename F::Acc acc;
-    __device__ __forceinline__ void run(int kindA, int xa, int kindB, int xb0, int xb1, int k) {
-        int64_t Ja = ia;
-        if (kindA == kSingle) Ja = __ldg(p.a.s_target + ia * p.a.ns + xa);
-        if (kindA == kDouble) {
-            // alpha doubles: one slot per xa, beta self
-            for (int xd = xb0; xd < xb1; ++xd, ++k) {
-                const int64_t J = __ldg(p.a.d_target + ia * p.a.nd + xa + (xd - xb0));
-                f.term1(vbase + (int64_t)k * kTileRows, J * p.Db + ib, acc);
-            }
-            return;
-        }
-        const int64_t pan = Ja * p.Db;  // x panel of alpha string Ja
-        if (kindB == kSelf) {
-            f.term1(vbase + (int64_t)k * kTileRows, pan + ib, acc);
-        } else if (kindB == kSingle) {
-#pragma unroll 4
-            for (int xb = xb0; xb < xb1; ++xb, ++k)
-                f.term1(vbase + (int64_t)k * kTileRows, pan + st[xb * kTileRows + rr], acc);
-        } else {
-            const uint32_t *dt = p.b.d_target + ib * p.b.nd;
-#pragma unroll 4
-            for (int xb = xb0; xb < xb1; ++xb, ++k)
-                f.term1(vbase + (int64_t)k * kTileRows, pan + __ldg(dt + xb), acc);
-        }
-    }
-};
+// Column of a descriptor's slot in row (Ja row of the descriptor, ib); st: the
+// tile's beta single targets in shared memory, [nsb][kTileRows].
+__device__ __forceinline__ int64_t slot_col(const FciParams &p, uint64_t d, int64_t ib, const uint32_t *st, int rr) {
+    const uint32_t kind = (uint32_t)(d >> 32) & 3u;
+    const uint32_t xb = (uint32_t)(d >> 34);
+    const int64_t Jb = kind == kSelf     ? ib
+                       : kind == kSingle ? (int64_t)st[xb * kTileRows + rr]
+                                         : (int64_t)__ldg(p.b.d_target + ib * p.b.nd + xb);
+    return (int64_t)(uint32_t)d * p.Db + Jb;
+}
 
-template <typename F>
-__global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, const F f,
-                                                             typename F::X *__restrict__ y) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *st = reinterpret_cast<uint32_t *>(smem);  // [nsb][kTileRows]
-    __shared__ typename F::Acc part[kSplits][kTileRows];
-    const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+// Shared memory: descriptors [4Q] (8 bytes), beta single targets [nsb][kTileRows].
+__device__ __forceinline__ void stage_tile(const FciParams &p, int64_t ia, int64_t t, int W, int Q, uint64_t *desc,
+                                           uint32_t *st) {
+    for (int k = threadIdx.x; k < 4 * Q; k += blockDim.x) desc[k] = slot_desc(p, ia, k, W);
     const int nsb = p.b.ns;
-    for (int i = tid; i < nsb * kTileRows; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nsb * kTileRows; i += blockDim.x) {
         const int xb = i / kTileRows, r = i - xb * kTileRows;
         const int64_t ib = t * kTileRows + r;
         st[i] = ib < p.Db ? __ldg(p.b.s_target + ib * nsb + xb) : 0u;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Matvec. Block = one tile; warp w: rows (w & 1) * 32 + lane, quad range w >> 1.
+template <typename F>
+__global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, const F f,
+                                                             typename F::X *__restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ typename F::Acc part[kSplits][kTileRows];
+    const int W = fci_row_width(p), Q = (W + 3) >> 2;
+    uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *st = reinterpret_cast<uint32_t *>(desc + 4 * Q);
+    const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
+    const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
+    stage_tile(p, ia, t, W, Q, desc, st);
     __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = (warp & 1) * 32 + lane, ks = warp >> 1;
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
-    const int W = fci_row_width(p);
-    MatvecRun<F> v{p, f, st, ia, active ? ib_raw : p.Db - 1, (ia * T + t) * (int64_t)W * kTileRows + rr, rr, {}};
-    walk_slots(p, (int)((int64_t)W * ks / kSplits), (int)((int64_t)W * (ks + 1) / kSplits), v);
-    part[ks][rr] = v.acc;
+    const int64_t ib = active ? ib_raw : p.Db - 1;
+    const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
+    const int64_t qbase = (ia * T + t) * (int64_t)Q;
+    typename F::Acc acc{};
+    typename F::Chunk v[2];
+    // two quads in flight per lane
+    for (int c = c0; c < c1; c += 2) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (c + u < c1)
+                f.load4(((qbase + c + u) * kTileRows + rr) * 4, v[u]);
+            else
+                f.zero(v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (c + u < c1) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint64_t d = desc[4 * (c + u) + j];
+                    if (((uint32_t)(d >> 32) & 3u) != kPad) f.term(v[u], j, slot_col(p, d, ib, st, rr), acc);
+                }
+            }
+        }
+    }
+    part[ks][rr] = acc;
     __syncthreads();
     if (ks == 0 && active) {
         typename F::Acc s = part[0][rr];
@@ -136,85 +140,77 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
 }
 
 // ---------------------------------------------------------------------------
-// Build: the same element values as the CRS generator, as FP32 hi + lo splits
-// (zero where |v| <= 1e-14), written in slot order.
-struct FillRun {
-    const FciParams &p;
-    const float *slhi, *sllo;  // staged (ar ac|. .) slices of the alpha singles
-    int64_t ia, ib, r, vbase;
-    bool active;
-    float *hi_out, *lo_out;
-    __device__ __forceinline__ void put(int k, float h, float l) {
-        const int64_t at = vbase + (int64_t)k * kTileRows;
-        hi_out[at] = active ? h : 0.0f;
-        lo_out[at] = active ? l : 0.0f;
-    }
-    __device__ __forceinline__ void run(int kindA, int xa, int kindB, int xb0, int xb1, int k) {
-        const int L = p.L, L2 = L * L;
-        const int nsr = p.a.ns + p.b.ns;
-        if (kindA == kDouble) {
-            for (int xd = xb0; xd < xb1; ++xd, ++k) {
-                const size_t at = ia * p.a.nd + xa + (xd - xb0);
-                put(k, __ldg(p.a.d_hi + at), __ldg(p.a.d_lo + at));
-            }
-            return;
+// Fill: the same element values as the CRS generator, as FP32 hi + lo splits (zero
+// where |v| <= 1e-14), with each row's nonzero count and lower-triangle count.
+__device__ __forceinline__ void value_of(const FciParams &p, const float *slhi, const float *sllo, int64_t ia,
+                                         int64_t ib, int64_t r, int k, int W, float &h, float &l) {
+    h = l = 0.0f;
+    if (k >= W) return;
+    const int L = p.L, L2 = L * L;
+    const int nsa = p.a.ns, nsb = p.b.ns, ndb = p.b.nd;
+    const int nsr = nsa + nsb;
+    const int WA = 1 + nsb + ndb, WS = 1 + nsb, kD = WA + nsa * WS;
+    if (k < WA) {
+        if (k == 0) {
+            h = p.diag_hi[r];
+            l = p.diag_lo[r];
+        } else if (k <= nsb) {  // beta single (one_diff_orbital), precomputed per row
+            const size_t at = (size_t)r * nsr + nsa + (k - 1);
+            h = __ldg(p.sgl_hi + at);
+            l = __ldg(p.sgl_lo + at);
+        } else {  // beta-beta double
+            const size_t at = ib * ndb + (k - 1 - nsb);
+            h = __ldg(p.b.d_hi + at);
+            l = __ldg(p.b.d_lo + at);
         }
-        if (kindB == kSelf) {
-            if (kindA == kSelf) {
-                put(k, p.diag_hi[r], p.diag_lo[r]);
-            } else {
-                const size_t at = (size_t)r * nsr + xa;  // alpha single (one_diff_orbital)
-                put(k, __ldg(p.sgl_hi + at), __ldg(p.sgl_lo + at));
-            }
-            return;
-        }
-        if (kindA == kSelf) {
-            if (kindB == kSingle) {
-                for (int xb = xb0; xb < xb1; ++xb, ++k) {
-                    const size_t at = (size_t)r * nsr + p.a.ns + xb;  // beta single
-                    put(k, __ldg(p.sgl_hi + at), __ldg(p.sgl_lo + at));
-                }
-            } else {
-                for (int xb = xb0; xb < xb1; ++xb, ++k) {
-                    const size_t at = ib * p.b.nd + xb;  // beta-beta double
-                    put(k, __ldg(p.b.d_hi + at), __ldg(p.b.d_lo + at));
-                }
-            }
-            return;
-        }
-        // alpha-beta doubles (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457);
-        // the exact 8-fold symmetry of the stored integrals makes it row-independent
-        const uint32_t infoA = __ldg(p.a.s_info + ia * p.a.ns + xa);
-        const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
-        for (int xb = xb0; xb < xb1; ++xb, ++k) {
-            const uint32_t infoB = __ldg(p.b.s_info + ib * p.b.ns + xb);
+    } else if (k < kD) {
+        const int xa = (k - WA) / WS, q = (k - WA) - xa * WS;
+        if (q == 0) {  // alpha single
+            const size_t at = (size_t)r * nsr + xa;
+            h = __ldg(p.sgl_hi + at);
+            l = __ldg(p.sgl_lo + at);
+        } else {
+            // alpha-beta double (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457);
+            // the exact 8-fold symmetry of the stored integrals makes it row-independent
+            const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
+            const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + (q - 1));
             const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
             const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
-            float h, l;
             if (p.staged) {
                 h = slhi[xa * L2 + tt];
                 l = sllo[xa * L2 + tt];
             } else {
+                const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
                 const size_t at = ((size_t)ar * L + ac) * L2 + tt;
                 h = __ldg(p.eri_hi + at);
                 l = __ldg(p.eri_lo + at);
             }
-            put(k, __uint_as_float(__float_as_uint(h) ^ (odd << 31)), __uint_as_float(__float_as_uint(l) ^ (odd << 31)));
+            h = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
+            l = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
         }
+    } else {  // alpha-alpha double
+        const size_t at = ia * p.a.nd + (k - kD);
+        h = __ldg(p.a.d_hi + at);
+        l = __ldg(p.a.d_lo + at);
     }
-};
+}
 
 __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, float *__restrict__ hi,
-                                                             float *__restrict__ lo) {
+                                                             float *__restrict__ lo, uint32_t *__restrict__ count,
+                                                             uint32_t *__restrict__ lower) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t cnt[kSplits][kTileRows], low[kSplits][kTileRows];
+    const int W = fci_row_width(p), Q = (W + 3) >> 2;
     const int L2 = p.L * p.L, nsa = p.a.ns;
-    float *slhi = reinterpret_cast<float *>(smem);
+    uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *st = reinterpret_cast<uint32_t *>(desc + 4 * Q);
+    float *slhi = reinterpret_cast<float *>(st + p.b.ns * kTileRows);
     float *sllo = slhi + (size_t)nsa * L2;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
     const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_tile(p, ia, t, W, Q, desc, st);
     if (p.staged) {
-        for (int i = tid; i < nsa * L2; i += blockDim.x) {
+        for (int i = threadIdx.x; i < nsa * L2; i += blockDim.x) {
             const int xa = i / L2, tt = i - xa * L2;
             const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
             const int ar = (info >> 12) & 63, ac = (info >> 18) & 63;
@@ -224,17 +220,51 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
         }
     }
     __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = (warp & 1) * 32 + lane, ks = warp >> 1;
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;
-    const int W = fci_row_width(p);
-    FillRun v{p, slhi, sllo, ia, ib, ia * p.Db + ib, (ia * T + t) * (int64_t)W * kTileRows + rr, active, hi, lo};
-    walk_slots(p, (int)((int64_t)W * ks / kSplits), (int)((int64_t)W * (ks + 1) / kSplits), v);
+    const int64_t r = ia * p.Db + ib;
+    const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
+    const int64_t qbase = (ia * T + t) * (int64_t)Q;
+    uint32_t n_keep = 0, n_low = 0;
+    for (int c = c0; c < c1; ++c) {
+        float h4[4], l4[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = 4 * c + j;
+            value_of(p, slhi, sllo, ia, ib, r, k, W, h4[j], l4[j]);
+            if (!active) h4[j] = l4[j] = 0.0f;
+            if ((__float_as_uint(h4[j]) & 0x7FFFFFFFu) != 0u) {  // |v| > 1e-14
+                ++n_keep;
+                n_low += slot_col(p, desc[k], ib, st, rr) < r;
+            }
+        }
+        const int64_t at = ((qbase + c) * kTileRows + rr) * 4;
+        *reinterpret_cast<float4 *>(hi + at) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+        *reinterpret_cast<float4 *>(lo + at) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+    }
+    cnt[ks][rr] = n_keep;
+    low[ks][rr] = n_low;
+    __syncthreads();
+    if (ks == 0 && active) {
+        uint32_t a = 0, b = 0;
+#pragma unroll
+        for (int q = 0; q < kSplits; ++q) {
+            a += cnt[q][rr];
+            b += low[q][rr];
+        }
+        count[r] = a;
+        lower[r] = b;
+    }
 }
 
-size_t matvec_smem(const FciParams &p) { return (size_t)p.b.ns * kTileRows * 4; }
-size_t fill_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
+size_t tile_smem(const FciParams &p) {
+    const int W = fci_row_width(p), Q = (W + 3) >> 2;
+    return (size_t)4 * Q * 8 + (size_t)p.b.ns * kTileRows * 4;
+}
+size_t slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
 
 template <typename F>
 void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t s) {
@@ -244,7 +274,7 @@ void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t
     }();
     (void)attr_set;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    k_spmv_slots<F><<<(unsigned)(p.a.D * T), kSlotThreads, matvec_smem(p), s>>>(p, f, y);
+    k_spmv_slots<F><<<(unsigned)(p.a.D * T), kSlotThreads, tile_smem(p), s>>>(p, f, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -252,25 +282,26 @@ void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t
 }  // namespace
 
 bool slots_supported(const FciParams &p) {
-    return matvec_smem(p) <= kSlotsMaxSmem && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
-           (int64_t)fci_row_width(p) < (int64_t)INT32_MAX / 2;
+    return tile_smem(p) <= kSlotsMaxSmem && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
+           (int64_t)fci_row_width(p) < (int64_t)INT32_MAX / 8;
 }
 
 int64_t slots_count(const FciParams &p) {
-    return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * (int64_t)fci_row_width(p);
+    const int64_t Q = ((int64_t)fci_row_width(p) + 3) / 4;
+    return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * Q * 4;
 }
 
-void fill_slots_launch(const FciParams &p0, float *hi, float *lo, cudaStream_t s) {
+void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s) {
     FciParams p = p0;
-    const size_t sm = fill_smem(p);
-    p.staged = sm <= kSlotsMaxSmem ? 1 : 0;
+    const size_t base = tile_smem(p), sl = slice_smem(p);
+    p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fill_slots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
         return true;
     }();
     (void)attr_set;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    k_fill_slots<<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? sm : 0, s>>>(p, hi, lo);
+    k_fill_slots<<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, hi, lo, count, lower);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -10,10 +10,11 @@ constexpr size_t kSlotsMaxSmem = 96 * 1024;  // per-block shared memory of the s
 
 // Whether the layout applies (its shared-memory tables fit; indices fit 32 bits).
 bool slots_supported(const FciParams &p);
-// Stored values (FP32 each, hi and lo arrays): tiles x W x kTileRows.
+// Stored values (FP32 each, hi and lo arrays): tiles x kTileRows x W rounded up to 4.
 int64_t slots_count(const FciParams &p);
-// Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p).
-void fill_slots_launch(const FciParams &p, float *hi, float *lo, cudaStream_t s);
+// Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p) and
+// each row's stored-nonzero count and lower-triangle count (count, lower: [dim]).
+void fill_slots_launch(const FciParams &p, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s);
 // y = H x from FP32 slot values, FP32 x/y and accumulation.
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s);
 // FP64 y = H x from the split slot values hi + lo; x32 is an FP32 copy of x.
