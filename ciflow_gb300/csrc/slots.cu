@@ -2,27 +2,29 @@
 //
 // Every FCI row has the same structural width W = (1 + ns_b + nd_b) + ns_a (1 + ns_b)
 // + nd_a, and the meaning of each slot can be made the same for every row by
-// ordering a row's slots by excitation kind rather than by column:
-//   [alpha self]    beta self, beta singles xb = 0..ns_b-1, beta doubles xb = 0..nd_b-1
-//   [alpha single xa, xa = 0..ns_a-1]    beta self, beta singles xb
-//   [alpha double xa, xa = 0..nd_a-1]    beta self
+// ordering a row's slots by excitation kind rather than by column, in five
+// segments, each padded with zero slots to a multiple of 4:
+//   S0  alpha self, beta self                         (diagonal)
+//   S1  alpha self, beta singles xb = 0..ns_b-1
+//   S2  alpha self, beta doubles xb = 0..nd_b-1
+//   S3  alpha singles xa = 0..ns_a-1, then alpha doubles, beta self
+//   S4  alpha single xa x beta single xb, xa-major    (alpha-beta doubles)
 // (xa, xb index a string's singles/doubles in the order of its string tables). The
-// column of slot (alpha kind, xa, beta kind, xb) in row (Ia, Ib) is Ja * Db + Jb with
-// Ja = Ia or the xa-th alpha single/double target of Ia and Jb = Ib or the xb-th beta
-// single/double target of Ib, so no column index is stored: 4 bytes per element in
-// FP32 instead of the 8 of an FP32 CRS, 8 instead of 12 for the FP64 product from
-// the split values.
+// column of a slot in row (Ia, Ib) is Ja * Db + Jb with Ja = Ia or the xa-th alpha
+// single/double target of Ia and Jb = Ib or the xb-th beta single/double target of
+// Ib, so no column index is stored: 4 bytes per element in FP32 instead of the 8 of
+// an FP32 CRS, 8 instead of 12 for the FP64 product from the split values.
 //
 // Rows are grouped in tiles of kTileRows consecutive beta strings of one alpha
 // string. Within a tile the values are stored in quads of 4 consecutive slots per
-// row, quad-major: val[((tile * Q + c) * kTileRows + row) * 4 + j] for slot 4c + j
-// (Q = ceil(W / 4), padding slots zero). A warp (32 rows) reads one quad of 32 rows
-// with one fully coalesced 512-byte load, 16 bytes per lane, and every lane handles
-// the same slot kinds. The slot -> (Ja, beta kind, xb) descriptors of the tile's
-// alpha string sit in shared memory and are read as broadcasts; the x entries a slot
-// reads all lie in the panel x[Ja * Db .. Ja * Db + Db) of one alpha string.
-// Elements with |v| <= 1e-14 are stored as zero; padding rows of the last tile are
-// zero and never written back.
+// row, quad-major: val[((tile * Q + c) * kTileRows + row) * 4 + j] for slot 4c + j.
+// A warp (32 rows) reads one quad of 32 rows with one fully coalesced 512-byte load,
+// 16 bytes per lane; the 4 slots of a quad share their beta kind (the segments are
+// quad-aligned), so a quad is one branch-free group of 4 gathers. The slot ->
+// (Ja, xb) descriptors of the tile's alpha string sit in shared memory and are read
+// as broadcasts; the x entries a slot reads lie in the panel x[Ja * Db, Ja * Db + Db).
+// Elements with |v| <= 1e-14 and padding are stored as zero; padding rows of the
+// last tile are zero and never written back.
 //
 // Replaces SparseMatrix_CRS_Sym::mvprod (SparseMatrix_CRS.cpp:700-723) for the FP32
 // values of the mixed method. The fill below produces the same element values as
@@ -39,45 +41,55 @@ namespace {
 
 constexpr int kSlotThreads = 256;  // 2 row halves x 4 quad ranges
 constexpr int kSplits = 4;
-constexpr uint32_t kPad = 3;  // descriptor beta kind of a padding slot
 
-// Descriptor of slot k of alpha string ia: Ja | beta kind << 32 | xb << 34.
-__device__ __forceinline__ uint64_t slot_desc(const FciParams &p, int64_t ia, int k, int W) {
-    if (k >= W) return (uint64_t)kPad << 32;
-    const int nsa = p.a.ns, nsb = p.b.ns, ndb = p.b.nd;
-    const int WA = 1 + nsb + ndb, WS = 1 + nsb, kD = WA + nsa * WS;
-    uint64_t Ja, kindB, xb = 0;
-    if (k < WA) {
-        Ja = (uint64_t)ia;
-        kindB = k == 0 ? kSelf : (k <= nsb ? kSingle : kDouble);
-        if (k > 0) xb = k <= nsb ? k - 1 : k - 1 - nsb;
-    } else if (k < kD) {
-        const int xa = (k - WA) / WS, q = (k - WA) - xa * WS;
-        Ja = __ldg(p.a.s_target + ia * nsa + xa);
-        kindB = q == 0 ? kSelf : kSingle;
-        if (q > 0) xb = q - 1;
+__host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
+
+// Segment starts S1..S4 and the padded width Wp.
+struct SlotMap {
+    int s1, s2, s3, s4, wp;
+};
+__host__ __device__ inline SlotMap slot_map(const FciParams &p) {
+    SlotMap m;
+    m.s1 = 4;
+    m.s2 = m.s1 + pad4(p.b.ns);
+    m.s3 = m.s2 + pad4(p.b.nd);
+    m.s4 = m.s3 + pad4(p.a.ns + p.a.nd);
+    m.wp = m.s4 + pad4(p.a.ns * p.b.ns);
+    return m;
+}
+
+// Descriptor of slot k of alpha string ia: Ja | beta kind << 32 | xb << 34. Padding
+// slots carry their segment's kind with Ja = ia, xb = 0 (a valid column, value 0).
+__device__ __forceinline__ uint64_t slot_desc(const FciParams &p, const SlotMap &m, int64_t ia, int k) {
+    const int nsa = p.a.ns, nsb = p.b.ns;
+    uint64_t Ja = (uint64_t)ia, kindB = kSelf, xb = 0;
+    if (k < m.s1) {
+    } else if (k < m.s2) {
+        kindB = kSingle;
+        if (k - m.s1 < nsb) xb = k - m.s1;
+    } else if (k < m.s3) {
+        kindB = kDouble;
+        if (k - m.s2 < p.b.nd) xb = k - m.s2;
+    } else if (k < m.s4) {
+        const int i = k - m.s3;
+        if (i < nsa) Ja = __ldg(p.a.s_target + ia * nsa + i);
+        else if (i < nsa + p.a.nd) Ja = __ldg(p.a.d_target + ia * p.a.nd + (i - nsa));
     } else {
-        Ja = __ldg(p.a.d_target + ia * p.a.nd + (k - kD));
-        kindB = kSelf;
+        kindB = kSingle;
+        const int i = k - m.s4;
+        if (i < nsa * nsb) {
+            const int xa = i / nsb;
+            Ja = __ldg(p.a.s_target + ia * nsa + xa);
+            xb = i - xa * nsb;
+        }
     }
     return Ja | (kindB << 32) | (xb << 34);
 }
 
-// Column of a descriptor's slot in row (Ja row of the descriptor, ib); st: the
-// tile's beta single targets in shared memory, [nsb][kTileRows].
-__device__ __forceinline__ int64_t slot_col(const FciParams &p, uint64_t d, int64_t ib, const uint32_t *st, int rr) {
-    const uint32_t kind = (uint32_t)(d >> 32) & 3u;
-    const uint32_t xb = (uint32_t)(d >> 34);
-    const int64_t Jb = kind == kSelf     ? ib
-                       : kind == kSingle ? (int64_t)st[xb * kTileRows + rr]
-                                         : (int64_t)__ldg(p.b.d_target + ib * p.b.nd + xb);
-    return (int64_t)(uint32_t)d * p.Db + Jb;
-}
-
-// Shared memory: descriptors [4Q] (8 bytes), beta single targets [nsb][kTileRows].
-__device__ __forceinline__ void stage_tile(const FciParams &p, int64_t ia, int64_t t, int W, int Q, uint64_t *desc,
-                                           uint32_t *st) {
-    for (int k = threadIdx.x; k < 4 * Q; k += blockDim.x) desc[k] = slot_desc(p, ia, k, W);
+// Shared memory: descriptors [Wp] (8 bytes), beta single targets [nsb][kTileRows].
+__device__ __forceinline__ void stage_tile(const FciParams &p, const SlotMap &m, int64_t ia, int64_t t,
+                                           uint64_t *desc, uint32_t *st) {
+    for (int k = threadIdx.x; k < m.wp; k += blockDim.x) desc[k] = slot_desc(p, m, ia, k);
     const int nsb = p.b.ns;
     for (int i = threadIdx.x; i < nsb * kTileRows; i += blockDim.x) {
         const int xb = i / kTileRows, r = i - xb * kTileRows;
@@ -93,23 +105,25 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
                                                              typename F::X *__restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ typename F::Acc part[kSplits][kTileRows];
-    const int W = fci_row_width(p), Q = (W + 3) >> 2;
+    const SlotMap m = slot_map(p);
+    const int Q = m.wp >> 2;
     uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *st = reinterpret_cast<uint32_t *>(desc + 4 * Q);
+    uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
     const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
-    stage_tile(p, ia, t, W, Q, desc, st);
+    stage_tile(p, m, ia, t, desc, st);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = (warp & 1) * 32 + lane, ks = warp >> 1;
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;
+    const uint32_t *dt = p.b.d_target + ib * p.b.nd;
     const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
     const int64_t qbase = (ia * T + t) * (int64_t)Q;
     typename F::Acc acc{};
     typename F::Chunk v[2];
-    // two quads in flight per lane
+    // two quads in flight per lane; each quad has one beta kind (uniform branch)
     for (int c = c0; c < c1; c += 2) {
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
@@ -121,11 +135,22 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             if (c + u < c1) {
+                const uint64_t *d = desc + 4 * (c + u);
+                const uint32_t kind = (uint32_t)(d[0] >> 32) & 3u;
+                int64_t col[4];
+                if (kind == kSelf) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const uint64_t d = desc[4 * (c + u) + j];
-                    if (((uint32_t)(d >> 32) & 3u) != kPad) f.term(v[u], j, slot_col(p, d, ib, st, rr), acc);
+                    for (int j = 0; j < 4; ++j) col[j] = (int64_t)(uint32_t)d[j] * p.Db + ib;
+                } else if (kind == kSingle) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        col[j] = (int64_t)(uint32_t)d[j] * p.Db + st[(uint32_t)(d[j] >> 34) * kTileRows + rr];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) col[j] = (int64_t)(uint32_t)d[j] * p.Db + __ldg(dt + (uint32_t)(d[j] >> 34));
                 }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) f.term(v[u], j, col[j], acc);
             }
         }
     }
@@ -142,38 +167,50 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
 // ---------------------------------------------------------------------------
 // Fill: the same element values as the CRS generator, as FP32 hi + lo splits (zero
 // where |v| <= 1e-14), with each row's nonzero count and lower-triangle count.
-__device__ __forceinline__ void value_of(const FciParams &p, const float *slhi, const float *sllo, int64_t ia,
-                                         int64_t ib, int64_t r, int k, int W, float &h, float &l) {
+__device__ __forceinline__ void value_of(const FciParams &p, const SlotMap &m, const float *slhi, const float *sllo,
+                                         int64_t ia, int64_t ib, int64_t r, int k, float &h, float &l) {
     h = l = 0.0f;
-    if (k >= W) return;
     const int L = p.L, L2 = L * L;
     const int nsa = p.a.ns, nsb = p.b.ns, ndb = p.b.nd;
     const int nsr = nsa + nsb;
-    const int WA = 1 + nsb + ndb, WS = 1 + nsb, kD = WA + nsa * WS;
-    if (k < WA) {
+    if (k < m.s1) {
         if (k == 0) {
             h = p.diag_hi[r];
             l = p.diag_lo[r];
-        } else if (k <= nsb) {  // beta single (one_diff_orbital), precomputed per row
-            const size_t at = (size_t)r * nsr + nsa + (k - 1);
+        }
+    } else if (k < m.s2) {
+        const int xb = k - m.s1;
+        if (xb < nsb) {  // beta single (one_diff_orbital), precomputed per row
+            const size_t at = (size_t)r * nsr + nsa + xb;
             h = __ldg(p.sgl_hi + at);
             l = __ldg(p.sgl_lo + at);
-        } else {  // beta-beta double
-            const size_t at = ib * ndb + (k - 1 - nsb);
+        }
+    } else if (k < m.s3) {
+        const int xb = k - m.s2;
+        if (xb < ndb) {  // beta-beta double
+            const size_t at = ib * ndb + xb;
             h = __ldg(p.b.d_hi + at);
             l = __ldg(p.b.d_lo + at);
         }
-    } else if (k < kD) {
-        const int xa = (k - WA) / WS, q = (k - WA) - xa * WS;
-        if (q == 0) {  // alpha single
-            const size_t at = (size_t)r * nsr + xa;
+    } else if (k < m.s4) {
+        const int i = k - m.s3;
+        if (i < nsa) {  // alpha single
+            const size_t at = (size_t)r * nsr + i;
             h = __ldg(p.sgl_hi + at);
             l = __ldg(p.sgl_lo + at);
-        } else {
+        } else if (i < nsa + p.a.nd) {  // alpha-alpha double
+            const size_t at = ia * p.a.nd + (i - nsa);
+            h = __ldg(p.a.d_hi + at);
+            l = __ldg(p.a.d_lo + at);
+        }
+    } else {
+        const int i = k - m.s4;
+        if (i < nsa * nsb) {
             // alpha-beta double (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457);
             // the exact 8-fold symmetry of the stored integrals makes it row-independent
+            const int xa = i / nsb, xb = i - xa * nsb;
             const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
-            const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + (q - 1));
+            const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + xb);
             const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
             const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
             if (p.staged) {
@@ -188,11 +225,17 @@ __device__ __forceinline__ void value_of(const FciParams &p, const float *slhi, 
             h = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
             l = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
         }
-    } else {  // alpha-alpha double
-        const size_t at = ia * p.a.nd + (k - kD);
-        h = __ldg(p.a.d_hi + at);
-        l = __ldg(p.a.d_lo + at);
     }
+}
+
+// Column of slot descriptor d in row (., ib); st: the tile's beta single targets.
+__device__ __forceinline__ int64_t slot_col(const FciParams &p, uint64_t d, int64_t ib, const uint32_t *st, int rr) {
+    const uint32_t kind = (uint32_t)(d >> 32) & 3u;
+    const uint32_t xb = (uint32_t)(d >> 34);
+    const int64_t Jb = kind == kSelf     ? ib
+                       : kind == kSingle ? (int64_t)st[xb * kTileRows + rr]
+                                         : (int64_t)__ldg(p.b.d_target + ib * p.b.nd + xb);
+    return (int64_t)(uint32_t)d * p.Db + Jb;
 }
 
 __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, float *__restrict__ hi,
@@ -200,15 +243,16 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                                                              uint32_t *__restrict__ lower) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t cnt[kSplits][kTileRows], low[kSplits][kTileRows];
-    const int W = fci_row_width(p), Q = (W + 3) >> 2;
+    const SlotMap m = slot_map(p);
+    const int Q = m.wp >> 2;
     const int L2 = p.L * p.L, nsa = p.a.ns;
     uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *st = reinterpret_cast<uint32_t *>(desc + 4 * Q);
+    uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
     float *slhi = reinterpret_cast<float *>(st + p.b.ns * kTileRows);
     float *sllo = slhi + (size_t)nsa * L2;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
     const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
-    stage_tile(p, ia, t, W, Q, desc, st);
+    stage_tile(p, m, ia, t, desc, st);
     if (p.staged) {
         for (int i = threadIdx.x; i < nsa * L2; i += blockDim.x) {
             const int xa = i / L2, tt = i - xa * L2;
@@ -234,7 +278,7 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int k = 4 * c + j;
-            value_of(p, slhi, sllo, ia, ib, r, k, W, h4[j], l4[j]);
+            value_of(p, m, slhi, sllo, ia, ib, r, k, h4[j], l4[j]);
             if (!active) h4[j] = l4[j] = 0.0f;
             if ((__float_as_uint(h4[j]) & 0x7FFFFFFFu) != 0u) {  // |v| > 1e-14
                 ++n_keep;
@@ -260,10 +304,7 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     }
 }
 
-size_t tile_smem(const FciParams &p) {
-    const int W = fci_row_width(p), Q = (W + 3) >> 2;
-    return (size_t)4 * Q * 8 + (size_t)p.b.ns * kTileRows * 4;
-}
+size_t tile_smem(const FciParams &p) { return (size_t)slot_map(p).wp * 8 + (size_t)p.b.ns * kTileRows * 4; }
 size_t slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
 
 template <typename F>
@@ -283,12 +324,11 @@ void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t
 
 bool slots_supported(const FciParams &p) {
     return tile_smem(p) <= kSlotsMaxSmem && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
-           (int64_t)fci_row_width(p) < (int64_t)INT32_MAX / 8;
+           (int64_t)p.a.ns * p.b.ns < (int64_t)INT32_MAX / 8;
 }
 
 int64_t slots_count(const FciParams &p) {
-    const int64_t Q = ((int64_t)fci_row_width(p) + 3) / 4;
-    return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * Q * 4;
+    return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * (int64_t)slot_map(p).wp;
 }
 
 void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s) {

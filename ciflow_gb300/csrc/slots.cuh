@@ -10,7 +10,7 @@ constexpr size_t kSlotsMaxSmem = 96 * 1024;  // per-block shared memory of the s
 
 // Whether the layout applies (its shared-memory tables fit; indices fit 32 bits).
 bool slots_supported(const FciParams &p);
-// Stored values (FP32 each, hi and lo arrays): tiles x kTileRows x W rounded up to 4.
+// Stored values (FP32 each, hi and lo arrays): tiles x kTileRows x padded row width.
 int64_t slots_count(const FciParams &p);
 // Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p) and
 // each row's stored-nonzero count and lower-triangle count (count, lower: [dim]).
