@@ -307,7 +307,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         bytes_alg, layout = A.matvec_bytes(crs, tag == "fp32")
         ach = bytes_alg / t / 1e9
         roof[tag] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{args.config}"),
+                     "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{cfg['method'].lower()}_L{cfg['L']}_{cfg['nup']}a{cfg['ndown']}b"),
                      "algorithmic_bytes": bytes_alg, "layout": layout, "ms_per_launch": t * 1000,
                      "nnz_full": nf.value, "peak_source": peaks["source"]}
         lib.cigpu_crs_destroy(crs)
