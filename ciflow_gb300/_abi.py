@@ -40,6 +40,15 @@ class Request(ctypes.Structure):
                 ("econst", _D), ("tol", _D), ("h", _P), ("eri", _P), ("c0", _P)]
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("batched", ctypes.c_int32), ("individual", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("grid", ctypes.c_int32), ("steps", ctypes.c_int32), ("graph_launches", ctypes.c_int32),
+                ("tuned", ctypes.c_int32), ("reserved", ctypes.c_int32), ("seconds_build", _D), ("seconds", _D)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class Result(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("done", ctypes.c_int32), ("dim", _I64), ("info", SolveInfo),
                 ("queued_s", _D), ("latency_s", _D)]
@@ -70,6 +79,7 @@ SIGNATURES = {
     "cigpu_server_cancel": (_I, [_P, ctypes.c_uint64]),
     "cigpu_server_stats": (_I, [_P, _P, _P, _P, _P]),
     "cigpu_server_destroy": (_I, [_P]),
+    "cigpu_solve_batch": (_I, [_I, _P, _I64, _P, _P, _P, _P]),
     "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
 }
 

@@ -109,6 +109,19 @@ static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const ui
     count_launch();
 }
 
+void spmv_f64_shape(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
+                    double *y, int lanes, int grid, cudaStream_t s) {
+    const Plain<double> f{val, x};
+    switch (lanes) {
+        case 4: k_spmv_rows<Plain<double>, 4, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+        case 8: k_spmv_rows<Plain<double>, 8, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+        case 16: k_spmv_rows<Plain<double>, 16, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+        default: k_spmv_rows<Plain<double>, 32, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+    }
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
 void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
               double *y, cudaStream_t s) {
     launch_rows(n, nnz, row_ptr, col, Plain<double>{val, x}, y, s);

@@ -12,6 +12,10 @@ int sm_count_spmv();
 int spmv_grid();
 void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x, double *y,
               cudaStream_t s);
+// FP64 CRS matvec with an explicit shape: `lanes` (4, 8, 16 or 32) lanes per row,
+// `grid` blocks of kSpmvThreads (the batched solver's autotuner picks both).
+void spmv_f64_shape(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
+                    double *y, int lanes, int grid, cudaStream_t s);
 void spmv_f32(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
               cudaStream_t s);
 

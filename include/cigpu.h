@@ -157,7 +157,8 @@ int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *rdm1, double
  * the set_ham -> solve loop of the orbital optimisers, SimulatedAnnealing.cpp:72-86,
  * 130-134; CIMethod::set_ham CIMethod.cpp:117-126). Requests are admitted as
  * device memory (the HBM budget) and slots free up; admitted requests run
- * concurrently on separate streams; small ones are packed into batched launches. ---- */
+ * concurrently on separate streams (for many small problems known up front,
+ * cigpu_solve_batch below packs them into shared launches). ---- */
 typedef struct {
     int32_t L, nup, ndown;
     int32_t method;      /* cigpu_method */
@@ -193,6 +194,31 @@ int cigpu_server_cancel(cigpu_server *srv, uint64_t id);
 int cigpu_server_stats(cigpu_server *srv, int64_t *admitted, int64_t *completed, int64_t *inflight,
                        size_t *hbm_in_use);
 int cigpu_server_destroy(cigpu_server *srv);
+
+/* ---- batched solves: many independent lowest-eigenpair problems in one call.
+ * Replaces a loop of CIMethod::solve over Hamiltonians (CIMethod.cpp:241-264), as
+ * the orbital optimisers run it (SimulatedAnnealing.cpp:72-86). Problems with at
+ * most max_batched_dim determinants (0: 65536) are built as FP64 CRS matrices and
+ * solved together by a lockstep FP64 Lanczos whose steps are CUDA-graph launches
+ * serving every problem (their precision field is not used); larger problems are
+ * solved one by one with their requested precision, overlapping on worker
+ * streams. Request fields as for the server (want_rdm and c0 of batched problems
+ * are ignored). Outputs per request (each optional): e0, info, status (CIGPU_OK,
+ * CIGPU_ENOCONV, or the build error). Returns CIGPU_EINVAL for a malformed
+ * request before any work, else the first build/solve error or CIGPU_OK. ---- */
+typedef struct {
+    int32_t batched;         /* problems solved in lockstep */
+    int32_t individual;      /* problems above max_batched_dim */
+    int32_t lanes, grid;     /* SpMV shape picked by the autotuner (last batch) */
+    int32_t steps;           /* Lanczos steps of the longest batch */
+    int32_t graph_launches;  /* CUDA-graph launches (one per step of all problems) */
+    int32_t tuned;           /* batches whose shape was timed now (not cached) */
+    int32_t reserved;
+    double seconds_build;    /* building every problem (and solving the large ones) */
+    double seconds;          /* the whole call */
+} cigpu_batch_stats;
+int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_dim, double *e0,
+                      cigpu_solve_info *info, int *status, cigpu_batch_stats *stats);
 
 /* Device memory a request of this shape needs (bytes), as used by admission. */
 int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes);
