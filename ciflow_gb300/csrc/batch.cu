@@ -654,13 +654,23 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
         CIGPU_CUDA(cudaGetDevice(&device));
         // build every problem, and solve the ones above the batching limit, on worker streams
         std::vector<int> failed(nthreads, CIGPU_OK);
+        // worker streams live until the call returns: the built matrices keep them
+        std::vector<cudaStream_t> wstreams(nthreads, nullptr);
+        struct StreamsGuard {
+            std::vector<cudaStream_t> &v;
+            ~StreamsGuard() {
+                for (cudaStream_t w : v)
+                    if (w) {
+                        cudaStreamSynchronize(w);
+                        cudaStreamDestroy(w);
+                    }
+            }
+        } wguard{wstreams};
+        for (int t = 0; t < nthreads; ++t)
+            CIGPU_CUDA(cudaStreamCreateWithFlags(&wstreams[t], cudaStreamNonBlocking));
         auto worker = [&](int t) {
             cudaSetDevice(device);
-            cudaStream_t s = nullptr;
-            if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
-                failed[t] = CIGPU_ECUDA;
-                return;
-            }
+            cudaStream_t s = wstreams[t];
             StreamScope scope(s);
             for (int i = t; i < count; i += nthreads) {
                 Item &it = items[i];
@@ -684,7 +694,6 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 if (stc != CIGPU_OK && stc != CIGPU_ENOCONV && failed[t] == CIGPU_OK) failed[t] = stc;
             }
             cudaStreamSynchronize(s);
-            cudaStreamDestroy(s);
         };
         std::vector<std::thread> pool;
         for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
