@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -228,8 +230,11 @@ __global__ void __launch_bounds__(256) k_batch_analyse(Batch B) {
         lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     }
-    const double span0 = fmax(hi - lo, 1e-300);
-    lo -= 1e-12 * span0;
+    // widen by a margin that survives rounding (a 1 x 1 matrix has lo == hi)
+    const double scale = fmax(1.0, fmax(fabs(lo), fabs(hi)));
+    const double margin = 1e-12 * fmax(hi - lo, 0.0) + 1e-13 * scale;
+    lo -= margin;
+    hi += margin;
     for (int round = 0; round < 12; ++round) {
         const double step = (hi - lo) / 33.0;
         if (!(step > 0)) break;
@@ -247,7 +252,7 @@ __global__ void __launch_bounds__(256) k_batch_analyse(Batch B) {
     if (lane == 0) {
         const double theta = 0.5 * (lo + hi);
         // inverse iteration on T - lo I (positive semi-definite: lo <= lambda_min)
-        const double tiny = 1e-300;
+        const double tiny = 1e-15 * scale;  // pivot floor, relative to |T|
         for (int i = 0; i < m; ++i) s[i] = 1.0;
         for (int it = 0; it < 3; ++it) {
             // (T - lo I) x = s by LDL^T (no pivoting needed: the matrix is positive
@@ -264,10 +269,16 @@ __global__ void __launch_bounds__(256) k_batch_analyse(Batch B) {
             }
             s[m - 1] /= dv[m - 1];
             for (int i = m - 2; i >= 0; --i) s[i] = s[i] / dv[i] - (b[i] / dv[i]) * s[i + 1];
+            // normalise without overflow: by the largest entry first
+            double mx = 0;
+            for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(s[i]));
+            const double imx = mx > 0 ? 1.0 / mx : 0.0;
             double nrm = 0;
-            for (int i = 0; i < m; ++i) nrm += s[i] * s[i];
-            nrm = sqrt(nrm);
-            const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+            for (int i = 0; i < m; ++i) {
+                s[i] *= imx;
+                nrm += s[i] * s[i];
+            }
+            const double inv = nrm > 0 ? 1.0 / sqrt(nrm) : 0.0;
             for (int i = 0; i < m; ++i) s[i] *= inv;
         }
         const double res = fabs(bnew * s[m - 1]);
@@ -534,8 +545,36 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     CIGPU_CUDA(cudaGetLastError());
     count_launch(3);
 
+    // CIGPU_TRACE=1: the first problems' state after the start and the first steps
+    const char *tr_env = std::getenv("CIGPU_TRACE");
+    const bool trace = tr_env && tr_env[0] == '1';
+    auto trace_state = [&](const char *what) {
+        if (!trace) return;
+        const int np = std::min(P, 3);
+        std::vector<double> hv(std::min<int64_t>(N, 2)), hw(std::min<int64_t>(N, 2)), hn(1), ha(np * kBatchSteps),
+            hb(np * kBatchSteps), ht(np), hr(np);
+        std::vector<int> hj(np), hs(np), hact(np);
+        cudaMemcpyAsync(hv.data(), V.p, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hw.data(), W.p, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hn.data(), npart.p, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(ha.data(), alpha.p, sizeof(double) * ha.size(), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hb.data(), beta.p, sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(ht.data(), theta.p, sizeof(double) * np, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hr.data(), res_est.p, sizeof(double) * np, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hj.data(), j.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs.data(), status.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hact.data(), action.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        std::fprintf(stderr, "[cigpu batch] %s: V %g %g W %g %g npart0 %g\n", what, hv[0], hv.size() > 1 ? hv[1] : 0.0,
+                     hw[0], hw.size() > 1 ? hw[1] : 0.0, hn[0]);
+        for (int q = 0; q < np; ++q)
+            std::fprintf(stderr, "  p%d j %d status %d action %d alpha0 %g beta0 %g theta %g res %g\n", q, hj[q],
+                         hs[q], hact[q], ha[q * kBatchSteps], hb[q * kBatchSteps], ht[q], hr[q]);
+    };
+    trace_state("start");
     bool tuned_now = false;
     const auto shape = tune_spmv(N, NNZ, rp.p, col.p, val.p, V.p, W.p, s, &tuned_now);
+    trace_state("tuned");
     const int lanes = shape.first, sgrid = shape.second;
     const unsigned dot_y = (kBatchSteps + kDotVecs - 1) / kDotVecs;
 
@@ -571,6 +610,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
                 CIGPU_CUDA(cudaGraphLaunch(exec, s));
                 count_launch(10);
                 ++launches;
+                if (trace && launches <= 2) trace_state("after step");
             }
             steps += 8;
             CIGPU_CUDA(cudaMemcpyAsync(&h_active, n_active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
