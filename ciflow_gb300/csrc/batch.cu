@@ -7,10 +7,12 @@
 // trip. Here every problem up to max_batched_dim determinants is built with the
 // usual FP64 CRS generator, the matrices are concatenated into one block-diagonal
 // CRS, and all problems run an FP64 Lanczos in lockstep:
-//   * one step = 10 kernel launches that each serve every problem (the SpMV over
-//     the concatenated matrix; segmented dot products and updates over row
-//     chunks that never straddle two problems; a warp per problem for the
-//     tridiagonal analysis), captured once as a CUDA graph and replayed;
+//   * one step = 9 kernel launches plus one SpMV launch per row-length class, each
+//     serving every problem (the problems are ordered by mean row length, so each
+//     class is one row range of the concatenated matrix with its own SpMV shape;
+//     segmented dot products and updates over row chunks that never straddle two
+//     problems; a warp per problem for the tridiagonal analysis), captured once
+//     as a CUDA graph and replayed;
 //   * full two-pass Gram-Schmidt against the problem's own basis, kBatchSteps
 //     vectors per cycle, then an explicit restart from the Ritz vector;
 //   * the lowest Ritz value of each tridiagonal matrix by 32-way multisection on
@@ -18,8 +20,8 @@
 //     residual estimate beta * |s_last| — no host work per step;
 //   * per-problem state on the device; a converged problem idles while the
 //     others continue; the host reads one counter every 8 graph launches.
-// The SpMV shape (lanes per row, grid) is picked per batch by timing the
-// candidates on the batch's own matrix (autotuner, cached by matrix size).
+// The SpMV shape of each row-length class (lanes per row, grid) is picked by
+// timing candidates on the batch's own rows (autotuner, cached by range size).
 // Problems above max_batched_dim go through cigpu_solve with their requested
 // precision, on worker streams that overlap with each other.
 #include <algorithm>
@@ -430,8 +432,9 @@ __global__ void k_concat(const Part *parts, int P, int64_t *rp, uint32_t *col, d
 std::mutex g_tune_mutex;
 std::map<std::pair<int64_t, int64_t>, std::pair<int, int>> g_tuned;
 
-std::pair<int, int> tune_spmv(int64_t n, int64_t nnz, const int64_t *rp, const uint32_t *col, const double *val,
-                              const double *x, double *y, cudaStream_t s, bool *tuned_now) {
+// Candidates: lanes per row around the row-length class, grids of 4..16 blocks per SM.
+std::pair<int, int> tune_spmv(int64_t n, int64_t nnz, int lanes0, const int64_t *rp, const uint32_t *col,
+                              const double *val, const double *x, double *y, cudaStream_t s, bool *tuned_now) {
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tuned.find({n, nnz});
@@ -441,14 +444,14 @@ std::pair<int, int> tune_spmv(int64_t n, int64_t nnz, const int64_t *rp, const u
         }
     }
     const int sms = sm_count();
-    const int lanes_c[] = {4, 8, 16, 32};
     const int per_sm_c[] = {4, 8, 16};
     cudaEvent_t e0, e1;
     CIGPU_CUDA(cudaEventCreate(&e0));
     CIGPU_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
-    std::pair<int, int> pick{8, sms * 8};
-    for (int lanes : lanes_c)
+    std::pair<int, int> pick{lanes0, sms * 8};
+    for (int lanes : {lanes0 / 2, lanes0, lanes0 * 2}) {
+        if (lanes < 4 || lanes > 32) continue;
         for (int per_sm : per_sm_c) {
             const int64_t need = std::max<int64_t>(1, (n * lanes + kSpmvThreads - 1) / kSpmvThreads);
             const int grid = (int)std::min<int64_t>((int64_t)sms * per_sm, need);
@@ -464,6 +467,7 @@ std::pair<int, int> tune_spmv(int64_t n, int64_t nnz, const int64_t *rp, const u
                 pick = {lanes, grid};
             }
         }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -471,6 +475,9 @@ std::pair<int, int> tune_spmv(int64_t n, int64_t nnz, const int64_t *rp, const u
     *tuned_now = true;
     return pick;
 }
+
+// Lanes per row for a mean row length (the starting point of the tuner).
+int lanes_for(double mean_row) { return mean_row >= 160 ? 32 : mean_row >= 48 ? 16 : mean_row >= 16 ? 8 : 4; }
 
 struct Item {
     int idx;
@@ -485,6 +492,15 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
                     cigpu_batch_stats *st) {
     const int P = (int)items.size();
     if (P == 0) return;
+    // order by mean row length so that each row-length class is one contiguous row
+    // range: the SpMV runs one launch per class with its own shape
+    auto mean_row = [](const Item *it) { return (double)it->crs->nnz_full / (double)std::max<int64_t>(1, it->crs->dim); };
+    std::stable_sort(items.begin(), items.end(), [&](const Item *a, const Item *b) { return mean_row(a) < mean_row(b); });
+    struct Seg {
+        int64_t r0, r1, nnz;
+        int lanes, grid;
+    };
+    std::vector<Seg> segs;
     int64_t N = 0, NNZ = 0;
     std::vector<Part> parts(P);
     std::vector<int> chunk_prob, pc0(P), pc1(P), budget(P);
@@ -500,6 +516,10 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
         }
         pc1[p] = (int)chunk_prob.size();
         budget[p] = (int)std::min<int64_t>(4000, std::max<int64_t>(300, 3 * c.dim));
+        const int cls = lanes_for(mean_row(items[p]));
+        if (segs.empty() || segs.back().lanes != cls) segs.push_back(Seg{N, N, 0, cls, 0});
+        segs.back().r1 = N + c.dim;
+        segs.back().nnz += c.nnz_full;
         N += c.dim;
         NNZ += c.nnz_full;
     }
@@ -573,16 +593,28 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     };
     trace_state("start");
     bool tuned_now = false;
-    const auto shape = tune_spmv(N, NNZ, rp.p, col.p, val.p, V.p, W.p, s, &tuned_now);
+    for (Seg &g : segs) {
+        bool t = false;
+        const auto shape = tune_spmv(g.r1 - g.r0, g.nnz, g.lanes, rp.p + g.r0, col.p, val.p, V.p, W.p + g.r0, s, &t);
+        g.lanes = shape.first;
+        g.grid = shape.second;
+        tuned_now = tuned_now || t;
+    }
     trace_state("tuned");
-    const int lanes = shape.first, sgrid = shape.second;
+    auto spmv_all = [&]() {
+        for (const Seg &g : segs)
+            spmv_f64_shape(g.r1 - g.r0, rp.p + g.r0, col.p, val.p, V.p, W.p + g.r0, g.lanes, g.grid, s);
+    };
+    const Seg &main_seg = *std::max_element(segs.begin(), segs.end(),
+                                            [](const Seg &a, const Seg &b) { return a.nnz < b.nnz; });
+    const int lanes = main_seg.lanes, sgrid = main_seg.grid;
     const unsigned dot_y = (kBatchSteps + kDotVecs - 1) / kDotVecs;
 
     // one Lanczos step of every problem, captured once
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     CIGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    spmv_f64_shape(N, rp.p, col.p, val.p, V.p, W.p, lanes, sgrid, s);
+    spmv_all();
     k_batch_dots<<<dim3(C, dot_y), kRowThreads, 0, s>>>(B);
     k_batch_reduce<<<P, 64, 0, s>>>(B, h1.p);
     k_batch_update<<<C, kRowThreads, 0, s>>>(B, h1.p);
@@ -608,7 +640,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
         while (steps < max_steps + 1) {
             for (int k = 0; k < 8; ++k) {
                 CIGPU_CUDA(cudaGraphLaunch(exec, s));
-                count_launch(10);
+                count_launch(9 + (int)segs.size());
                 ++launches;
                 if (trace && launches <= 2) trace_state("after step");
             }
@@ -626,7 +658,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     cudaGraphDestroy(graph);
 
     // exact Rayleigh quotient and residual of every Ritz vector
-    spmv_f64_shape(N, rp.p, col.p, val.p, V.p, W.p, lanes, sgrid, s);
+    spmv_all();
     k_batch_rq_parts<<<C, kRowThreads, 0, s>>>(B);
     k_batch_rq<<<(P + 255) / 256, 256, 0, s>>>(B, E.p, vv.p);
     k_batch_res_parts<<<C, kRowThreads, 0, s>>>(B, E.p, vv.p);

@@ -209,7 +209,7 @@ int cigpu_server_destroy(cigpu_server *srv);
 typedef struct {
     int32_t batched;         /* problems solved in lockstep */
     int32_t individual;      /* problems above max_batched_dim */
-    int32_t lanes, grid;     /* SpMV shape picked by the autotuner (last batch) */
+    int32_t lanes, grid;     /* autotuned SpMV shape of the row class with most nonzeros (last batch) */
     int32_t steps;           /* Lanczos steps of the longest batch */
     int32_t graph_launches;  /* CUDA-graph launches (one per step of all problems) */
     int32_t tuned;           /* batches whose shape was timed now (not cached) */
