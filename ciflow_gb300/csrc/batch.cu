@@ -108,6 +108,12 @@ __global__ void __launch_bounds__(kRowThreads) k_chunk_norm2(Batch B, const doub
     if (threadIdx.x == 0) B.npart[c] = a;
 }
 
+// row_prob[r] = the problem of row r
+__global__ void __launch_bounds__(kRowThreads) k_row_prob(Batch B, int *row_prob) {
+    const int c = blockIdx.x, p = B.chunk_prob[c];
+    for (int64_t r = B.chunk_r0[c] + threadIdx.x; r < B.chunk_r1[c]; r += blockDim.x) row_prob[r] = p;
+}
+
 // V = V / |V_p| per problem, Q[0] = V
 __global__ void __launch_bounds__(kRowThreads) k_batch_start(Batch B) {
     const int c = blockIdx.x, p = B.chunk_prob[c];
@@ -551,7 +557,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     DevBuf<double> h1((size_t)kBatchSteps * P), h2((size_t)kBatchSteps * P);
     DevBuf<double> alpha((size_t)kBatchSteps * P), beta((size_t)kBatchSteps * P), sv((size_t)kBatchSteps * P);
     DevBuf<double> theta(P), res_est(P), inv_beta(P), E(P), vv(P), res(P);
-    DevBuf<int> j(P), status(P), action(P), restarts(P), mv(P), n_active(1);
+    DevBuf<int> j(P), status(P), action(P), restarts(P), mv(P), n_active(1), row_prob(N);
     for (auto *b : {&j, &status, &action, &restarts, &mv})
         CIGPU_CUDA(cudaMemsetAsync(b->p, 0, sizeof(int) * P, s));
     Batch B{P, C, N, rp.p, col.p, val.p, cprob.p, cr0.p, cr1.p, dpc0.p, dpc1.p, Q.p, V.p, W.p, part.p, npart.p,
@@ -559,11 +565,12 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
             restarts.p, mv.p, dbudget.p, n_active.p, tol};
 
     // start vectors: seeded random, normalised per problem
+    k_row_prob<<<C, kRowThreads, 0, s>>>(B, row_prob.p);
     k_batch_random<<<sm_count() * 4, 256, 0, s>>>(V.p, N, 0x5EEDull);
     k_chunk_norm2<<<C, kRowThreads, 0, s>>>(B, V.p);
     k_batch_start<<<C, kRowThreads, 0, s>>>(B);
     CIGPU_CUDA(cudaGetLastError());
-    count_launch(3);
+    count_launch(4);
 
     // CIGPU_TRACE=1: the first problems' state after the start and the first steps
     const char *tr_env = std::getenv("CIGPU_TRACE");
@@ -601,9 +608,11 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
         tuned_now = tuned_now || t;
     }
     trace_state("tuned");
-    auto spmv_all = [&]() {
+    // rows of finished problems are skipped inside the step (their W is not read)
+    auto spmv_all = [&](bool active_only) {
         for (const Seg &g : segs)
-            spmv_f64_shape(g.r1 - g.r0, rp.p + g.r0, col.p, val.p, V.p, W.p + g.r0, g.lanes, g.grid, s);
+            spmv_f64_shape(g.r1 - g.r0, rp.p + g.r0, col.p, val.p, V.p, W.p + g.r0, g.lanes, g.grid, s,
+                           active_only ? row_prob.p + g.r0 : nullptr, active_only ? status.p : nullptr);
     };
     const Seg &main_seg = *std::max_element(segs.begin(), segs.end(),
                                             [](const Seg &a, const Seg &b) { return a.nnz < b.nnz; });
@@ -614,7 +623,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     CIGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    spmv_all();
+    spmv_all(true);
     k_batch_dots<<<dim3(C, dot_y), kRowThreads, 0, s>>>(B);
     k_batch_reduce<<<P, 64, 0, s>>>(B, h1.p);
     k_batch_update<<<C, kRowThreads, 0, s>>>(B, h1.p);
@@ -658,7 +667,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     cudaGraphDestroy(graph);
 
     // exact Rayleigh quotient and residual of every Ritz vector
-    spmv_all();
+    spmv_all(false);
     k_batch_rq_parts<<<C, kRowThreads, 0, s>>>(B);
     k_batch_rq<<<(P + 255) / 256, 256, 0, s>>>(B, E.p, vv.p);
     k_batch_res_parts<<<C, kRowThreads, 0, s>>>(B, E.p, vv.p);

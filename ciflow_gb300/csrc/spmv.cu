@@ -25,15 +25,27 @@ namespace {
 // column loads and U value loads before its 4U gathers of x, so enough bytes are
 // in flight to cover HBM latency (a single chunk per lane left the kernel
 // latency-bound on the dependent gathers).
-template <typename F, int G, int U>
+// Row filters: every row, or only rows of problems still active (batched solves:
+// row_prob[r] is the row's problem, status[p] != 0 once it has finished).
+struct AllRows {
+    __device__ __forceinline__ bool skip(int64_t) const { return false; }
+};
+struct ActiveRows {
+    const int *__restrict__ row_prob;
+    const int *__restrict__ status;
+    __device__ __forceinline__ bool skip(int64_t r) const { return status[row_prob[r]] != 0; }
+};
+
+template <typename F, int G, int U, typename M = AllRows>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int64_t *__restrict__ row_ptr,
                                                             const uint32_t *__restrict__ col, const F f,
-                                                            typename F::X *__restrict__ y) {
+                                                            typename F::X *__restrict__ y, const M m = M{}) {
     const int lane = threadIdx.x & (G - 1);
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
     for (int64_t r = gid; r < n; r += ng) {
+        if (m.skip(r)) continue;  // the same for the G lanes of the row
         const int64_t s = row_ptr[r], e = row_ptr[r + 1];
         typename F::Acc acc{};
         // scalar head up to a 16-byte boundary of both arrays (4 elements)
@@ -110,13 +122,24 @@ static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const ui
 }
 
 void spmv_f64_shape(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
-                    double *y, int lanes, int grid, cudaStream_t s) {
+                    double *y, int lanes, int grid, cudaStream_t s, const int *row_prob, const int *status) {
     const Plain<double> f{val, x};
-    switch (lanes) {
-        case 4: k_spmv_rows<Plain<double>, 4, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
-        case 8: k_spmv_rows<Plain<double>, 8, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
-        case 16: k_spmv_rows<Plain<double>, 16, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
-        default: k_spmv_rows<Plain<double>, 32, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+    using P = Plain<double>;
+    if (row_prob) {
+        const ActiveRows m{row_prob, status};
+        switch (lanes) {
+            case 4: k_spmv_rows<P, 4, 4, ActiveRows><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y, m); break;
+            case 8: k_spmv_rows<P, 8, 4, ActiveRows><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y, m); break;
+            case 16: k_spmv_rows<P, 16, 4, ActiveRows><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y, m); break;
+            default: k_spmv_rows<P, 32, 4, ActiveRows><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y, m); break;
+        }
+    } else {
+        switch (lanes) {
+            case 4: k_spmv_rows<P, 4, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+            case 8: k_spmv_rows<P, 8, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+            case 16: k_spmv_rows<P, 16, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+            default: k_spmv_rows<P, 32, 4><<<grid, kSpmvThreads, 0, s>>>(n, row_ptr, col, f, y); break;
+        }
     }
     CIGPU_CUDA(cudaGetLastError());
     count_launch();

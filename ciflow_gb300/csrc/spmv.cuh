@@ -13,9 +13,12 @@ int spmv_grid();
 void spmv_f64(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x, double *y,
               cudaStream_t s);
 // FP64 CRS matvec with an explicit shape: `lanes` (4, 8, 16 or 32) lanes per row,
-// `grid` blocks of kSpmvThreads (the batched solver's autotuner picks both).
+// `grid` blocks of kSpmvThreads (the batched solver's autotuner picks both). With
+// row_prob non-null, row r is skipped when status[row_prob[r]] != 0 (finished
+// problems of a batch; y keeps its old value there).
 void spmv_f64_shape(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
-                    double *y, int lanes, int grid, cudaStream_t s);
+                    double *y, int lanes, int grid, cudaStream_t s, const int *row_prob = nullptr,
+                    const int *status = nullptr);
 void spmv_f32(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const float *val, const float *x, float *y,
               cudaStream_t s);
 
