@@ -46,6 +46,8 @@ def parse_args():
                     help="served-stream requests per form (0 skips the served stream)")
     ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
+    ap.add_argument("--batched-problems", type=int, default=512,
+                    help="uneven problems of the batched-solve comparison (0 skips it)")
     return ap.parse_args()
 
 
@@ -364,6 +366,13 @@ def run_cigpu(args, rank: int, world: int, dist):
             served["mixed"]["solves_per_s_all_ranks"] = float(t[0].item())
             served["plain_fp64"]["solves_per_s_all_ranks"] = float(t[1].item())
 
+    # batched uneven solves: one cigpu_solve_batch call against the same problems one at a time
+    batched = None
+    if args.batched_problems > 0:
+        from ciflow_gb300.batch_bench import run as run_batched
+        barrier()
+        batched = run_batched(args.batched_problems, seed=rank)
+
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
@@ -389,6 +398,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "gpu_launches_plain": launches_plain,
         "clocks": clk.summary(),
         "served": served,
+        "batched": batched,
         "cpu_baseline": cpu,
     }
     print(json.dumps(out), flush=True)

@@ -23,13 +23,14 @@ from .batch import random_problems, solve_batch
 
 
 def one_at_a_time(problems, tol: float):
+    """E0 and wall seconds of each problem solved alone through the C ABI."""
     lib = A.lib()
     e0 = np.empty(len(problems))
-    keep = []
+    secs = np.empty(len(problems))
     for i, (ints, method) in enumerate(problems):
+        t0 = time.perf_counter()
         hh = np.ascontiguousarray(ints.h)
         ee = np.ascontiguousarray(ints.eri)
-        keep.append((hh, ee))
         ham, crs = ctypes.c_void_p(), ctypes.c_void_p()
         A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(hh), A.ptr(ee),
                                      ctypes.byref(ham)))
@@ -41,41 +42,39 @@ def one_at_a_time(problems, tol: float):
         e0[i] = info.e0
         lib.cigpu_crs_destroy(crs)
         lib.cigpu_ham_destroy(ham)
-    return e0
+        secs[i] = time.perf_counter() - t0
+    return e0, secs
 
 
-def run(count: int = 512, seed: int = 0, tol: float = 1e-6, max_batched_dim: int = 0, reps: int = 1):
+def run(count: int = 512, seed: int = 0, tol: float = 1e-6, max_batched_dim: int = 0):
     problems = random_problems(count, seed=seed)
     dims = np.array([comb(i.L, i.nup) * (comb(i.L, i.ndown) if m == A.FCI else 1) for i, m in problems])
     lim = max_batched_dim or 65536
+    small = dims <= lim
     solve_batch(problems[: min(8, count)], tol=tol, max_batched_dim=max_batched_dim)  # warm-up
     one_at_a_time(problems[: min(8, count)], tol)
-    t_batch = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        e_b, infos, status, stats = solve_batch(problems, tol=tol, max_batched_dim=max_batched_dim)
-        t_batch.append(time.perf_counter() - t0)
     t0 = time.perf_counter()
-    e_s = one_at_a_time(problems, tol)
-    t_single = time.perf_counter() - t0
-    small = dims <= lim
+    e_b, infos, status, stats = solve_batch(problems, tol=tol, max_batched_dim=max_batched_dim)
+    t_batch = time.perf_counter() - t0
+    e_s, secs = one_at_a_time(problems, tol)
+    t_single = float(secs.sum())
+    small_probs = [p for p, f in zip(problems, small) if f]
     t0 = time.perf_counter()
-    e_bs, _, _, stats_small = solve_batch([p for p, s in zip(problems, small) if s], tol=tol,
-                                          max_batched_dim=max_batched_dim)
+    e_bs, infos_s, _, stats_small = solve_batch(small_probs, tol=tol, max_batched_dim=max_batched_dim)
     t_batch_small = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    one_at_a_time([p for p, s in zip(problems, small) if s], tol)
-    t_single_small = time.perf_counter() - t0
+    t_single_small = float(secs[small].sum())
+    mv = np.array([i["matvecs_fp64"] for i in infos_s]) if small_probs else np.zeros(1)
     de = np.abs(e_b - e_s)
     return {
         "problems": count, "dims": {"min": int(dims.min()), "max": int(dims.max()), "sum": int(dims.sum())},
         "batched_below": lim, "n_batched": int(small.sum()), "n_individual": int((~small).sum()),
-        "tol": tol,
-        "batch_s": min(t_batch), "one_at_a_time_s": t_single,
-        "solves_per_s_batch": count / min(t_batch), "solves_per_s_one_at_a_time": count / t_single,
-        "speedup": t_single / min(t_batch),
-        "small_only": {"batch_s": t_batch_small, "one_at_a_time_s": t_single_small,
-                       "speedup": t_single_small / t_batch_small, "stats": stats_small},
+        "tol": tol, "precision": "fp64 (both arms)",
+        "batch_s": t_batch, "one_at_a_time_s": t_single,
+        "solves_per_s_batch": count / t_batch, "solves_per_s_one_at_a_time": count / t_single,
+        "speedup": t_single / t_batch,
+        "small_only": {"problems": int(small.sum()), "batch_s": t_batch_small, "one_at_a_time_s": t_single_small,
+                       "speedup": t_single_small / t_batch_small,
+                       "matvecs_p50_p100": [float(np.percentile(mv, 50)), float(mv.max())], "stats": stats_small},
         "max_abs_dE0_batch_vs_single": float(de.max()),
         "not_converged": int(sum(1 for s in status if s != A.OK)),
         "stats": stats,
@@ -88,9 +87,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--max-batched-dim", type=int, default=0)
-    ap.add_argument("--reps", type=int, default=1)
     a = ap.parse_args()
-    print(json.dumps(run(a.count, a.seed, a.tol, a.max_batched_dim, a.reps)))
+    print(json.dumps(run(a.count, a.seed, a.tol, a.max_batched_dim)))
 
 
 if __name__ == "__main__":
