@@ -128,6 +128,24 @@ def ncu_traffic(kernel: str) -> float | None:
 
 
 # ---------------------------------------------------------------------------
+# Cross-rank reductions of the replica runs (one process per GPU; the timed
+# region's length is the slowest rank's, throughputs add up).
+def reduce_over_ranks(values, dist, op: str = "max", device: str = "cuda") -> list:
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return [float(v) for v in t.tolist()]
+
+
+def job_throughput(units_per_rank: float, seconds: float, world: int, dist, device: str = "cuda"):
+    """(whole-job units/s, slowest rank's seconds): every rank processed
+    units_per_rank; the job took as long as its slowest rank."""
+    slowest = reduce_over_ranks([seconds], dist, "max", device)[0]
+    return world * units_per_rank / slowest, slowest
+
+
 def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float, n_matvec: int) -> dict:
     """The CPU implementation of the path (the oracle's restatement of the reference
     build and serial Sym::mvprod), timed on a bounded sample of rows and
@@ -254,11 +272,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         barrier()
         launches = lib.cigpu_kernel_launches() - l0
         ms = [a.elapsed_time(b) for a, b in evs]
-        tot = sum(ms) / 1000.0
-        if dist is not None:
-            t = torch.tensor([tot], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
+        tot = reduce_over_ranks([sum(ms) / 1000.0], dist, "max")[0]
         return ms, tot, infos, launches
 
     uuid = None
@@ -343,12 +357,8 @@ def run_cigpu(args, rank: int, world: int, dist):
     for _ in range(n_e2e):
         e2e_once()
     barrier()
-    t_e2e = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": world * n_e2e / t_e2e, "unit": "solves/s",
+    e2e_value, t_e2e = job_throughput(n_e2e, time.perf_counter() - t0, world, dist)
+    e2e = {"value": e2e_value, "unit": "solves/s",
            "h2d_bytes_per_step": int(h.nbytes + eri.nbytes), "d2h_bytes_per_step": int(c_host.nbytes),
            "path": "cigpu_ham_create + cigpu_build(MIXED) + cigpu_solve(c_out host), pageable host buffers"}
 
@@ -361,10 +371,10 @@ def run_cigpu(args, rank: int, world: int, dist):
         served = run_served(args.served_requests, args.served_rate, args.served_inflight, tol_mixed=args.tol,
                             tol_fp64=args.tol, seed=4 + rank)
         if dist is not None:
-            t = torch.tensor([served["mixed"]["solves_per_s"], served["plain_fp64"]["solves_per_s"]], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.SUM)
-            served["mixed"]["solves_per_s_all_ranks"] = float(t[0].item())
-            served["plain_fp64"]["solves_per_s_all_ranks"] = float(t[1].item())
+            tm, tp = reduce_over_ranks([served["mixed"]["solves_per_s"], served["plain_fp64"]["solves_per_s"]],
+                                       dist, "sum")
+            served["mixed"]["solves_per_s_all_ranks"] = tm
+            served["plain_fp64"]["solves_per_s_all_ranks"] = tp
 
     # batched uneven solves: one cigpu_solve_batch call against the same problems one at a time
     batched = None
