@@ -729,14 +729,18 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
             if (q.method == CIGPU_DOCI && q.nup != q.ndown) return CIGPU_EINVAL;
             items[i].idx = i;
         }
+        std::vector<int> small_idx, big_idx;
+        for (int i = 0; i < count; ++i) {
+            const cigpu_request &q = req[i];
+            items[i].dim = q.method == CIGPU_DOCI ? d_binom(q.L, q.nup) : d_binom(q.L, q.nup) * d_binom(q.L, q.ndown);
+            (items[i].dim <= max_batched_dim ? small_idx : big_idx).push_back(i);
+        }
         int hw = (int)std::thread::hardware_concurrency();
-        const int nthreads = std::max(1, std::min({8, hw > 0 ? hw : 4, count}));
+        const int nthreads = std::max(1, std::min({8, hw > 0 ? hw : 4, (int)small_idx.size()}));
         int device = 0;
         CIGPU_CUDA(cudaGetDevice(&device));
-        // build every problem, and solve the ones above the batching limit, on worker streams
-        std::vector<int> failed(nthreads, CIGPU_OK);
-        // worker streams live until the call returns: the built matrices keep them
-        std::vector<cudaStream_t> wstreams(nthreads, nullptr);
+        // streams live until the call returns: the built matrices keep them
+        std::vector<cudaStream_t> wstreams(nthreads + 1, nullptr);
         struct StreamsGuard {
             std::vector<cudaStream_t> &v;
             ~StreamsGuard() {
@@ -747,41 +751,64 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                     }
             }
         } wguard{wstreams};
-        for (int t = 0; t < nthreads; ++t)
-            CIGPU_CUDA(cudaStreamCreateWithFlags(&wstreams[t], cudaStreamNonBlocking));
-        auto worker = [&](int t) {
+        for (auto &w : wstreams) CIGPU_CUDA(cudaStreamCreateWithFlags(&w, cudaStreamNonBlocking));
+        std::vector<int> failed(nthreads + 1, CIGPU_OK);
+        // Problems above the limit: one at a time, in their requested precision, on
+        // their own stream and thread. They are bandwidth-bound, so running several
+        // at once gains nothing; the batched problems (latency-bound) overlap them.
+        auto big_worker = [&]() {
             cudaSetDevice(device);
-            cudaStream_t s = wstreams[t];
+            cudaStream_t s = wstreams[nthreads];
             StreamScope scope(s);
-            for (int i = t; i < count; i += nthreads) {
+            for (int i : big_idx) {
                 Item &it = items[i];
                 const cigpu_request &q = req[i];
                 int stc = cigpu_ham_create(q.L, q.nup, q.ndown, q.econst, q.h, q.eri, &it.ham);
-                const int64_t dim = q.method == CIGPU_DOCI ? d_binom(q.L, q.nup)
-                                                           : d_binom(q.L, q.nup) * d_binom(q.L, q.ndown);
-                it.dim = dim;
-                const bool small = dim <= max_batched_dim;
-                if (stc == CIGPU_OK)
-                    stc = cigpu_build(it.ham, q.method, small ? CIGPU_FP64 : q.precision, s, &it.crs);
-                if (stc == CIGPU_OK && !small) {
+                if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, q.precision, s, &it.crs);
+                if (stc == CIGPU_OK) {
                     cigpu_solve_info in{};
                     stc = cigpu_solve(it.crs, q.tol, 0, q.c0, nullptr, &in);
                     if (e0) e0[i] = in.e0;
                     if (info) info[i] = in;
-                    cigpu_crs_destroy(it.crs);
-                    it.crs = nullptr;
                 }
+                if (it.crs) cigpu_crs_destroy(it.crs);
+                it.crs = nullptr;
+                if (it.ham) cigpu_ham_destroy(it.ham);
+                it.ham = nullptr;
                 it.status = stc;
-                if (stc != CIGPU_OK && stc != CIGPU_ENOCONV && failed[t] == CIGPU_OK) failed[t] = stc;
+                if (stc != CIGPU_OK && stc != CIGPU_ENOCONV && failed[nthreads] == CIGPU_OK) failed[nthreads] = stc;
+            }
+            cudaStreamSynchronize(s);
+        };
+        std::thread big_thread(big_worker);
+        struct Joiner {
+            std::thread &t;
+            ~Joiner() {
+                if (t.joinable()) t.join();
+            }
+        } big_join{big_thread};
+        // build the batched problems on worker streams
+        auto worker = [&](int t) {
+            cudaSetDevice(device);
+            cudaStream_t s = wstreams[t];
+            StreamScope scope(s);
+            for (size_t k = t; k < small_idx.size(); k += nthreads) {
+                const int i = small_idx[k];
+                Item &it = items[i];
+                const cigpu_request &q = req[i];
+                int stc = cigpu_ham_create(q.L, q.nup, q.ndown, q.econst, q.h, q.eri, &it.ham);
+                if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, CIGPU_FP64, s, &it.crs);
+                it.status = stc;
+                if (stc != CIGPU_OK && failed[t] == CIGPU_OK) failed[t] = stc;
             }
             cudaStreamSynchronize(s);
         };
         std::vector<std::thread> pool;
-        for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
+        for (int t = 0; t < nthreads && !small_idx.empty(); ++t) pool.emplace_back(worker, t);
         for (auto &th : pool) th.join();
         int first_err = CIGPU_OK;
-        for (int f : failed)
-            if (f != CIGPU_OK) first_err = f;
+        for (int t = 0; t < nthreads; ++t)
+            if (failed[t] != CIGPU_OK && first_err == CIGPU_OK) first_err = failed[t];
         const double t_build = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         // batched problems, in batches of at most kMaxBatchRows rows (one tolerance per batch)
         cudaStream_t s = nullptr;
@@ -806,6 +833,9 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 }
             }
         }
+        big_thread.join();
+        for (int f : failed)
+            if (f != CIGPU_OK && first_err == CIGPU_OK) first_err = f;
         for (auto &it : items) {
             if (it.crs) cigpu_crs_destroy(it.crs);
             if (it.ham) cigpu_ham_destroy(it.ham);

@@ -201,8 +201,8 @@ int cigpu_server_destroy(cigpu_server *srv);
  * most max_batched_dim determinants (0: 65536) are built as FP64 CRS matrices and
  * solved together by a lockstep FP64 Lanczos whose steps are CUDA-graph launches
  * serving every problem (their precision field is not used); larger problems are
- * solved one by one with their requested precision, overlapping on worker
- * streams. Request fields as for the server (want_rdm and c0 of batched problems
+ * solved one by one with their requested precision on a stream of their own,
+ * overlapping the batched ones. Request fields as for the server (want_rdm and c0 of batched problems
  * are ignored). Outputs per request (each optional): e0, info, status (CIGPU_OK,
  * CIGPU_ENOCONV, or the build error). Returns CIGPU_EINVAL for a malformed
  * request before any work, else the first build/solve error or CIGPU_OK. ---- */
@@ -214,7 +214,7 @@ typedef struct {
     int32_t graph_launches;  /* CUDA-graph launches (one per step of all problems) */
     int32_t tuned;           /* batches whose shape was timed now (not cached) */
     int32_t reserved;
-    double seconds_build;    /* building every problem (and solving the large ones) */
+    double seconds_build;    /* building the batched problems */
     double seconds;          /* the whole call */
 } cigpu_batch_stats;
 int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_dim, double *e0,
