@@ -33,6 +33,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <stdexcept>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -513,6 +514,8 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
     std::vector<int64_t> chunk_r0, chunk_r1;
     for (int p = 0; p < P; ++p) {
         cigpu_crs &c = *items[p]->crs;
+        if (c.precision != CIGPU_FP64 || c.slots || (c.nnz_full > 0 && (!c.col.p || !c.val64.p)))
+            throw std::invalid_argument("lockstep batch needs FP64 CRS matrices");
         parts[p] = Part{c.row_ptr.p, c.col.p, c.val64.p, c.dim, c.nnz_full, N, NNZ};
         pc0[p] = (int)chunk_prob.size();
         for (int64_t r = 0; r < c.dim; r += kChunkRows) {
@@ -816,8 +819,9 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
         std::unique_ptr<std::remove_pointer_t<cudaStream_t>, decltype(&cudaStreamDestroy)> sguard(s, cudaStreamDestroy);
         StreamScope scope(s);
         std::map<double, std::vector<Item *>> by_tol;
-        for (auto &it : items)
-            if (it.crs && it.status == CIGPU_OK) by_tol[req[it.idx].tol].push_back(&it);
+        // only the batched problems: the large-problem thread owns its items until joined
+        for (int i : small_idx)
+            if (items[i].crs && items[i].status == CIGPU_OK) by_tol[req[i].tol].push_back(&items[i]);
         for (auto &kv : by_tol) {
             std::vector<Item *> cur;
             int64_t rows = 0;
