@@ -41,6 +41,7 @@ namespace {
 
 constexpr int kSlotThreads = 256;  // 2 row halves x 4 quad ranges
 constexpr int kSplits = 4;
+constexpr int kQuadsInFlight = 2;  // 16-byte value loads in flight per lane (4 was slower at L=12)
 
 __host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
 
@@ -122,18 +123,18 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
     const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
     const int64_t qbase = (ia * T + t) * (int64_t)Q;
     typename F::Acc acc{};
-    typename F::Chunk v[2];
-    // two quads in flight per lane; each quad has one beta kind (uniform branch)
-    for (int c = c0; c < c1; c += 2) {
+    typename F::Chunk v[kQuadsInFlight];
+    // kQuadsInFlight quads in flight per lane; each quad has one beta kind (uniform branch)
+    for (int c = c0; c < c1; c += kQuadsInFlight) {
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kQuadsInFlight; ++u) {
             if (c + u < c1)
                 f.load4(((qbase + c + u) * kTileRows + rr) * 4, v[u]);
             else
                 f.zero(v[u]);
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kQuadsInFlight; ++u) {
             if (c + u < c1) {
                 const uint64_t *d = desc + 4 * (c + u);
                 const uint32_t kind = (uint32_t)(d[0] >> 32) & 3u;
