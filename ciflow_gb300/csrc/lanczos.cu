@@ -103,9 +103,11 @@ __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < kDotChunk; ++i) {
-        double a = (double)acc[i];
+        // warp tree in the accumulation type (FP64 adds here would run on GB300's
+        // slow FP64 pipe, 5 per thread and vector); block and grid sums are FP64
+        AT a = acc[i];
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) sh[i][warp] = a;
+        if (lane == 0) sh[i][warp] = (double)a;
     }
     __syncthreads();
     if (threadIdx.x < nv) {
@@ -135,9 +137,9 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
     }
     if (nrm) {
         __shared__ double sh[kVecThreads / 32];
-        double a = (double)acc;
+        AT a = acc;  // warp tree in the accumulation type, block sum in FP64
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)a;
         __syncthreads();
         if (threadIdx.x == 0) {
             double s = 0;
@@ -162,12 +164,12 @@ __global__ void k_scale_to(const IT *__restrict__ t, int64_t n, const double *__
 //        r = H c - E c is the exact FP64 anchor residual)
 //   t  = ru / (theta - H_ii)                                      (guarded)
 // and the partial ||ru||^2 (FP64 block sums).
-__global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const double *__restrict__ r64,
-                                                                const double *__restrict__ c64,
+__global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__restrict__ r32,
+                                                                const float *__restrict__ c32,
                                                                 const float *__restrict__ V, const float *__restrict__ HV,
                                                                 int64_t ld, int k, const double *__restrict__ y,
                                                                 double a0, double a0_de, double theta,
-                                                                const double *__restrict__ diag, float *__restrict__ t,
+                                                                const float *__restrict__ diag32, float *__restrict__ t,
                                                                 int64_t n, double *__restrict__ nrm,
                                                                 double *__restrict__ nrm_out, unsigned *__restrict__ ticket) {
     __shared__ float ys[kMaxBasis + 1];
@@ -176,20 +178,20 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const double *__
     const float fa0 = (float)a0, fa0de = (float)a0_de, fth = (float)theta;
     float acc = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        float ru = fa0 * (float)r64[r] + fa0de * (float)c64[r];
+        float ru = fa0 * r32[r] + fa0de * c32[r];
         for (int i = 0; i < k; ++i) {
             const int64_t o = (int64_t)(i + 1) * ld + r;  // corrections live in slots 1..k
             ru += ys[i] * (HV[o] - fth * V[o]);
         }
         acc += ru * ru;
-        float d = (float)(theta - diag[r]);
+        float d = fth - diag32[r];  // FP32 (no per-element FP64 or conversion work)
         if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
         t[r] = ru / d;
     }
     __shared__ double sh[kVecThreads / 32];
-    double a = (double)acc;
+    float a = acc;  // warp tree in FP32, block sum in FP64
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)a;
     __syncthreads();
     if (threadIdx.x == 0) {
         double sum = 0;
@@ -275,7 +277,10 @@ __global__ void k_add_unit_at(const int64_t *__restrict__ pi, double keep, doubl
 
 template <typename VT>
 __global__ void k_scale(VT *__restrict__ w, int64_t n, const double *__restrict__ nrm2) {
-    const VT inv = (VT)(1.0 / sqrt(*nrm2));
+    __shared__ VT inv_s;  // one FP64 divide and square root per block, not per thread
+    if (threadIdx.x == 0) inv_s = (VT)(1.0 / sqrt(*nrm2));
+    __syncthreads();
+    const VT inv = inv_s;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
         w[r] = w[r] * inv;
 }
@@ -795,7 +800,8 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     VecOps ops(s, n);
     Refine ref(n, s, ops);
     const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 2), n - 2);
-    DevBuf<float> V((size_t)(mmax + 2) * n), HV((size_t)(mmax + 2) * n), cr32((size_t)2 * n);
+    DevBuf<float> V((size_t)(mmax + 2) * n), HV((size_t)(mmax + 2) * n), cr32((size_t)2 * n), diag32(n);
+    dev_convert(P.diag, diag32.p, n, s);  // FP32 diagonal for the preconditioner
     DevBuf<double> yd(kMaxBasis + 1);
     int64_t mv32 = 0, mv64 = 0;
     if (!have_start) {
@@ -875,8 +881,8 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
             count_launch();
         } else {
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
-            k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, c_dev, V.p, HV.p, n, k, yd.p, a0, a0 * (E - theta),
-                                                            theta, P.diag, vnew, n, ops.partial.p,
+            k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(cr32.p + n, cr32.p, V.p, HV.p, n, k, yd.p, a0,
+                                                            a0 * (E - theta), theta, diag32.p, vnew, n, ops.partial.p,
                                                             ops.out.p + SLOT_R, ops.ticket.p);
             count_launch();
         }
