@@ -27,6 +27,7 @@
 #include <mutex>
 
 #include "lanczos.cuh"
+#include "small_eigh.h"
 
 namespace cigpu {
 
@@ -463,53 +464,7 @@ void small_eigh(int n, std::vector<double> &a, std::vector<double> &w, std::vect
         double t0 = wall();
         ~Acc() { g_clk.eigh += wall() - t0; ++g_clk.n_eigh; }
     } acc_;
-    z.assign((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
-    double fro = 0;
-    for (double x : a) fro += x * x;
-    for (int sweep = 0; sweep < 100; ++sweep) {
-        double off = 0;
-        for (int p = 0; p < n; ++p)
-            for (int q = p + 1; q < n; ++q) off += a[(size_t)p * n + q] * a[(size_t)p * n + q];
-        if (off <= 1e-30 * fro || off == 0.0) break;
-        for (int p = 0; p < n; ++p)
-            for (int q = p + 1; q < n; ++q) {
-                const double apq = a[(size_t)p * n + q];
-                if (std::fabs(apq) < 1e-300) continue;
-                const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
-                // Rutishauser's rotation: zero a_pq with t = tan(phi), the smaller root of
-                // t^2 + 2 theta t - 1 = 0, theta = (a_qq - a_pp) / (2 a_pq)
-                const double theta = (aqq - app) / (2.0 * apq);
-                double t = 1.0 / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                if (theta < 0) t = -t;
-                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < n; ++k) {
-                    const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
-                    a[(size_t)k * n + p] = c * akp - s * akq;
-                    a[(size_t)k * n + q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < n; ++k) {
-                    const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
-                    a[(size_t)p * n + k] = c * apk - s * aqk;
-                    a[(size_t)q * n + k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < n; ++k) {
-                    const double zkp = z[(size_t)k * n + p], zkq = z[(size_t)k * n + q];
-                    z[(size_t)k * n + p] = c * zkp - s * zkq;
-                    z[(size_t)k * n + q] = s * zkp + c * zkq;
-                }
-            }
-    }
-    std::vector<int> idx(n);
-    for (int i = 0; i < n; ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
-    w.resize(n);
-    std::vector<double> zs((size_t)n * n);
-    for (int k = 0; k < n; ++k) {
-        w[k] = a[(size_t)idx[k] * n + idx[k]];
-        for (int i = 0; i < n; ++i) zs[(size_t)i * n + k] = z[(size_t)i * n + idx[k]];
-    }
-    z.swap(zs);
+    symmetric_eigh(n, a, w, z);
 }
 
 void dev_fill_random(double *v, int64_t n, uint64_t seed, cudaStream_t s) {

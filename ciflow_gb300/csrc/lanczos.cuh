@@ -37,7 +37,7 @@ int solve_fp64(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool
 // projected problem and diagonal preconditioner, FP64 residual-correction restarts.
 int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, bool have_start, cigpu_solve_info &info);
 
-// Symmetric eigen-decomposition of a small dense matrix (cyclic Jacobi):
+// Symmetric eigen-decomposition of a small dense matrix (Householder + implicit QR, small_eigh.h):
 // a is n*n row-major (destroyed), w ascending, z columns are eigenvectors (z[i*n+k] = vec_k[i]).
 void small_eigh(int n, std::vector<double> &a, std::vector<double> &w, std::vector<double> &z);
 
