@@ -168,77 +168,6 @@ __global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, 
 // ---------------------------------------------------------------------------
 // Fill: the same element values as the CRS generator, as FP32 hi + lo splits (zero
 // where |v| <= 1e-14), with each row's nonzero count and lower-triangle count.
-__device__ __forceinline__ void value_of(const FciParams &p, const SlotMap &m, const float *slhi, const float *sllo,
-                                         int64_t ia, int64_t ib, int64_t r, int k, float &h, float &l) {
-    h = l = 0.0f;
-    const int L = p.L, L2 = L * L;
-    const int nsa = p.a.ns, nsb = p.b.ns, ndb = p.b.nd;
-    const int nsr = nsa + nsb;
-    if (k < m.s1) {
-        if (k == 0) {
-            h = p.diag_hi[r];
-            l = p.diag_lo[r];
-        }
-    } else if (k < m.s2) {
-        const int xb = k - m.s1;
-        if (xb < nsb) {  // beta single (one_diff_orbital), precomputed per row
-            const size_t at = (size_t)r * nsr + nsa + xb;
-            h = __ldg(p.sgl_hi + at);
-            l = __ldg(p.sgl_lo + at);
-        }
-    } else if (k < m.s3) {
-        const int xb = k - m.s2;
-        if (xb < ndb) {  // beta-beta double
-            const size_t at = ib * ndb + xb;
-            h = __ldg(p.b.d_hi + at);
-            l = __ldg(p.b.d_lo + at);
-        }
-    } else if (k < m.s4) {
-        const int i = k - m.s3;
-        if (i < nsa) {  // alpha single
-            const size_t at = (size_t)r * nsr + i;
-            h = __ldg(p.sgl_hi + at);
-            l = __ldg(p.sgl_lo + at);
-        } else if (i < nsa + p.a.nd) {  // alpha-alpha double
-            const size_t at = ia * p.a.nd + (i - nsa);
-            h = __ldg(p.a.d_hi + at);
-            l = __ldg(p.a.d_lo + at);
-        }
-    } else {
-        const int i = k - m.s4;
-        if (i < nsa * nsb) {
-            // alpha-beta double (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457);
-            // the exact 8-fold symmetry of the stored integrals makes it row-independent
-            const int xa = i / nsb, xb = i - xa * nsb;
-            const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
-            const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + xb);
-            const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
-            const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
-            if (p.staged) {
-                h = slhi[xa * L2 + tt];
-                l = sllo[xa * L2 + tt];
-            } else {
-                const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
-                const size_t at = ((size_t)ar * L + ac) * L2 + tt;
-                h = __ldg(p.eri_hi + at);
-                l = __ldg(p.eri_lo + at);
-            }
-            h = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
-            l = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
-        }
-    }
-}
-
-// Column of slot descriptor d in row (., ib); st: the tile's beta single targets.
-__device__ __forceinline__ int64_t slot_col(const FciParams &p, uint64_t d, int64_t ib, const uint32_t *st, int rr) {
-    const uint32_t kind = (uint32_t)(d >> 32) & 3u;
-    const uint32_t xb = (uint32_t)(d >> 34);
-    const int64_t Jb = kind == kSelf     ? ib
-                       : kind == kSingle ? (int64_t)st[xb * kTileRows + rr]
-                                         : (int64_t)__ldg(p.b.d_target + ib * p.b.nd + xb);
-    return (int64_t)(uint32_t)d * p.Db + Jb;
-}
-
 __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, float *__restrict__ hi,
                                                              float *__restrict__ lo, uint32_t *__restrict__ count,
                                                              uint32_t *__restrict__ lower) {
@@ -273,18 +202,90 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     const int64_t r = ia * p.Db + ib;
     const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
     const int64_t qbase = (ia * T + t) * (int64_t)Q;
+    const int nsb = p.b.ns, ndb = p.b.nd, nda = p.a.nd, nsr = nsa + nsb, L = p.L;
     uint32_t n_keep = 0, n_low = 0;
+    // one quad at a time; a quad lies in one segment, so the branch is uniform
     for (int c = c0; c < c1; ++c) {
-        float h4[4], l4[4];
+        const int k0 = 4 * c;
+        float h4[4] = {0, 0, 0, 0}, l4[4] = {0, 0, 0, 0};
+        bool lw[4] = {false, false, false, false};  // column below the diagonal
+        if (k0 < m.s1) {  // S0: the diagonal
+            h4[0] = p.diag_hi[r];
+            l4[0] = p.diag_lo[r];
+        } else if (k0 < m.s2) {  // S1: beta singles (one_diff_orbital), precomputed per row
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int xb = k0 - m.s1 + j;
+                if (xb < nsb) {
+                    const size_t at = (size_t)r * nsr + nsa + xb;
+                    h4[j] = __ldg(p.sgl_hi + at);
+                    l4[j] = __ldg(p.sgl_lo + at);
+                    lw[j] = st[xb * kTileRows + rr] < (uint32_t)ib;
+                }
+            }
+        } else if (k0 < m.s3) {  // S2: beta-beta doubles
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int xb = k0 - m.s2 + j;
+                if (xb < ndb) {
+                    const size_t at = ib * ndb + xb;
+                    h4[j] = __ldg(p.b.d_hi + at);
+                    l4[j] = __ldg(p.b.d_lo + at);
+                    lw[j] = __ldg(p.b.d_target + at) < (uint32_t)ib;
+                }
+            }
+        } else if (k0 < m.s4) {  // S3: alpha singles then alpha-alpha doubles, beta self
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = k0 - m.s3 + j;
+                if (i < nsa) {
+                    const size_t at = (size_t)r * nsr + i;
+                    h4[j] = __ldg(p.sgl_hi + at);
+                    l4[j] = __ldg(p.sgl_lo + at);
+                } else if (i < nsa + nda) {
+                    const size_t at = ia * nda + (i - nsa);
+                    h4[j] = __ldg(p.a.d_hi + at);
+                    l4[j] = __ldg(p.a.d_lo + at);
+                }
+                lw[j] = (uint32_t)desc[k0 + j] < (uint32_t)ia;
+            }
+        } else {  // S4: alpha-beta doubles (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457)
+            const int i0 = k0 - m.s4;
+            int xa = nsb > 0 ? i0 / nsb : 0, xb = i0 - xa * nsb;
+            uint32_t infoA = xa < nsa ? __ldg(p.a.s_info + ia * nsa + xa) : 0u;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (i0 + j < nsa * nsb) {
+                    const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + xb);
+                    const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
+                    const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
+                    float h, l;
+                    if (p.staged) {
+                        h = slhi[xa * L2 + tt];
+                        l = sllo[xa * L2 + tt];
+                    } else {
+                        const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
+                        const size_t at = ((size_t)ar * L + ac) * L2 + tt;
+                        h = __ldg(p.eri_hi + at);
+                        l = __ldg(p.eri_lo + at);
+                    }
+                    h4[j] = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
+                    l4[j] = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
+                    lw[j] = (uint32_t)desc[k0 + j] < (uint32_t)ia;
+                    if (++xb == nsb && j < 3) {
+                        xb = 0;
+                        ++xa;
+                        infoA = xa < nsa ? __ldg(p.a.s_info + ia * nsa + xa) : 0u;
+                    }
+                }
+            }
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int k = 4 * c + j;
-            value_of(p, m, slhi, sllo, ia, ib, r, k, h4[j], l4[j]);
             if (!active) h4[j] = l4[j] = 0.0f;
-            if ((__float_as_uint(h4[j]) & 0x7FFFFFFFu) != 0u) {  // |v| > 1e-14
-                ++n_keep;
-                n_low += slot_col(p, desc[k], ib, st, rr) < r;
-            }
+            const bool keep = (__float_as_uint(h4[j]) & 0x7FFFFFFFu) != 0u;  // |v| > 1e-14
+            n_keep += keep;
+            n_low += keep && lw[j];
         }
         const int64_t at = ((qbase + c) * kTileRows + rr) * 4;
         *reinterpret_cast<float4 *>(hi + at) = make_float4(h4[0], h4[1], h4[2], h4[3]);
