@@ -99,10 +99,22 @@ __device__ __forceinline__ void stage_tile(const FciParams &p, const SlotMap &m,
     }
 }
 
+// Blocks per SM the register budget is set for (measured at L=10..12): the FP32
+// matvec keeps its 48 registers (forcing 6 blocks at 40 registers lost ILP and ran
+// 5% slower); the hi/lo variant runs 2% faster held to 4 blocks (64 registers).
+template <typename F>
+struct SlotOccupancy {
+    static constexpr int kMinBlocks = 4;
+};
+template <>
+struct SlotOccupancy<Plain<float>> {
+    static constexpr int kMinBlocks = 1;
+};
+
 // ---------------------------------------------------------------------------
 // Matvec. Block = one tile; warp w: rows (w & 1) * 32 + lane, quad range w >> 1.
 template <typename F>
-__global__ void __launch_bounds__(kSlotThreads) k_spmv_slots(const FciParams p, const F f,
+__global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_spmv_slots(const FciParams p, const F f,
                                                              typename F::X *__restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ typename F::Acc part[kSplits][kTileRows];
