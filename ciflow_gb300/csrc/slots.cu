@@ -99,16 +99,16 @@ __device__ __forceinline__ void stage_tile(const FciParams &p, const SlotMap &m,
     }
 }
 
-// Blocks per SM the register budget is set for (measured at L=10..12): the FP32
-// matvec keeps its 48 registers (forcing 6 blocks at 40 registers lost ILP and ran
-// 5% slower); the hi/lo variant runs 2% faster held to 4 blocks (64 registers).
+// Blocks per SM the register budget is set for (measured at L=10..12): 5 for the
+// FP32 matvec (48 registers; forcing 6 blocks at 40 registers lost ILP and ran 5%
+// slower); the hi/lo variant runs 2% faster held to 4 blocks (64 registers).
 template <typename F>
 struct SlotOccupancy {
     static constexpr int kMinBlocks = 4;
 };
 template <>
 struct SlotOccupancy<Plain<float>> {
-    static constexpr int kMinBlocks = 1;
+    static constexpr int kMinBlocks = 5;
 };
 
 // ---------------------------------------------------------------------------
