@@ -220,8 +220,8 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
     // col + values (FP64, or FP32 hi + lo); the mixed FCI layout stores values only
     size_t b = (size_t)dim * W * 12;
-    if (method == CIGPU_FCI && precision == CIGPU_MIXED)  // slot tiles of 64 beta strings, hi + lo
-        b = (size_t)binom64(L, nup) * ((binom64(L, ndown) + 63) / 64 * 64) * W * 8;
+    if (method == CIGPU_FCI && precision == CIGPU_MIXED)  // slot tiles of kTileRows beta strings, hi + lo
+        b = (size_t)binom64(L, nup) * ((binom64(L, ndown) + kTileRows - 1) / kTileRows * kTileRows) * (W + 16) * 8;
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
     b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
     b += (size_t)dim * 8 * 5;                    // c, refinement vectors

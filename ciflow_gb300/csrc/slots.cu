@@ -39,8 +39,9 @@ namespace cigpu {
 
 namespace {
 
-constexpr int kSlotThreads = 256;  // 2 row halves x 4 quad ranges
-constexpr int kSplits = 4;
+constexpr int kSlotThreads = 256;
+constexpr int kRowWarps = kTileRows / 32;                // warps covering the tile's rows
+constexpr int kSplits = kSlotThreads / 32 / kRowWarps;  // quad ranges per row
 constexpr int kQuadsInFlight = 2;  // 16-byte value loads in flight per lane (4 was slower at L=12)
 
 __host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
@@ -112,7 +113,7 @@ struct SlotOccupancy<Plain<float>> {
 };
 
 // ---------------------------------------------------------------------------
-// Matvec. Block = one tile; warp w: rows (w & 1) * 32 + lane, quad range w >> 1.
+// Matvec. Block = one tile; warp w: rows (w % kRowWarps) * 32 + lane, quad range w / kRowWarps.
 template <typename F>
 __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_spmv_slots(const FciParams p, const F f,
                                                              typename F::X *__restrict__ y) {
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
     stage_tile(p, m, ia, t, desc, st);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rr = (warp & 1) * 32 + lane, ks = warp >> 1;
+    const int rr = (warp % kRowWarps) * 32 + lane, ks = warp / kRowWarps;
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rr = (warp & 1) * 32 + lane, ks = warp >> 1;
+    const int rr = (warp % kRowWarps) * 32 + lane, ks = warp / kRowWarps;
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;

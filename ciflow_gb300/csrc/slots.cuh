@@ -5,7 +5,7 @@
 
 namespace cigpu {
 
-constexpr int kTileRows = 64;                // beta strings per tile (rows of one alpha string)
+constexpr int kTileRows = 64;                // beta strings per tile (rows of one alpha string; 128 measured slower at L=11, 12)
 constexpr size_t kSlotsMaxSmem = 96 * 1024;  // per-block shared memory of the slot kernels
 
 // Whether the layout applies (its shared-memory tables fit; indices fit 32 bits).
