@@ -37,7 +37,7 @@ class SolveInfo(ctypes.Structure):
 class Request(ctypes.Structure):
     _fields_ = [("L", ctypes.c_int32), ("nup", ctypes.c_int32), ("ndown", ctypes.c_int32),
                 ("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("want_rdm", ctypes.c_int32),
-                ("econst", _D), ("tol", _D), ("h", _P), ("eri", _P), ("c0", _P)]
+                ("econst", _D), ("tol", _D), ("h", _P), ("eri", _P), ("c0", _P), ("rot", _P)]
 
 
 class BatchStats(ctypes.Structure):
@@ -62,6 +62,9 @@ SIGNATURES = {
     "cigpu_kernel_launches": (_I64, []),
     "cigpu_ham_create": (_I, [_I, _I, _I, _D, _P, _P, _P]),
     "cigpu_ham_destroy": (_I, [_P]),
+    "cigpu_ham_rotate": (_I, [_P, _P, _P, _P]),
+    "cigpu_unitary_exp": (_I, [_I, _P, _P]),
+    "cigpu_ham_export": (_I, [_P, _P, _P]),
     "cigpu_build": (_I, [_P, _I, _I, _P, _P]),
     "cigpu_crs_destroy": (_I, [_P]),
     "cigpu_crs_dims": (_I, [_P, _P, _P, _P]),

@@ -86,6 +86,27 @@ class Hamiltonian:
         return self._dev.value
 
 
+    def rotated(self, U: np.ndarray) -> "Hamiltonian":
+        """The Hamiltonian in rotated orbitals, h' = U h U^T and (ab|cd)' = sum U_ap U_bq
+        U_cr U_ds (pq|rs), computed on the device (cigpu_ham_rotate; the reference's
+        OrbitalTransform::fillHamCI, OrbitalTransform.cpp:64-135)."""
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        out = ctypes.c_void_p()
+        A.check(A.lib().cigpu_ham_rotate(self.device(), A.ptr(u), None, ctypes.byref(out)), "cigpu_ham_rotate")
+        H = Hamiltonian(self.L, 0, self.nup, self.ndown, self.Econst)
+        H._dev = _Handle(out.value, A.lib().cigpu_ham_destroy)
+        A.check(A.lib().cigpu_ham_export(H._dev.value, A.ptr(H.h), A.ptr(H.eri)), "cigpu_ham_export")
+        return H
+
+
+def unitary_exp(X: np.ndarray) -> np.ndarray:
+    """exp(X) of an antisymmetric generator (UnitaryMatrix.cpp:229-290), host code of the library."""
+    x = np.ascontiguousarray(X, dtype=np.float64)
+    u = np.empty_like(x)
+    A.check(A.lib().cigpu_unitary_exp(x.shape[0], A.ptr(x), A.ptr(u)), "cigpu_unitary_exp")
+    return u
+
+
 class _Handle:
     def __init__(self, value, destroy):
         self.value = value

@@ -730,6 +730,7 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 (q.precision != CIGPU_FP64 && q.precision != CIGPU_MIXED))
                 return CIGPU_EINVAL;
             if (q.method == CIGPU_DOCI && q.nup != q.ndown) return CIGPU_EINVAL;
+            if (q.rot && (q.L < 1 || q.L > kMaxL || validate_rotation(q.L, q.rot) != CIGPU_OK)) return CIGPU_EINVAL;
             items[i].idx = i;
         }
         std::vector<int> small_idx, big_idx;
@@ -767,6 +768,12 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 Item &it = items[i];
                 const cigpu_request &q = req[i];
                 int stc = cigpu_ham_create(q.L, q.nup, q.ndown, q.econst, q.h, q.eri, &it.ham);
+                if (stc == CIGPU_OK && q.rot) {  // orbital rotation on the device
+                    cigpu_ham *rotated = nullptr;
+                    stc = cigpu_ham_rotate(it.ham, q.rot, s, &rotated);
+                    cigpu_ham_destroy(it.ham);
+                    it.ham = rotated;
+                }
                 if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, q.precision, s, &it.crs);
                 if (stc == CIGPU_OK) {
                     cigpu_solve_info in{};
@@ -800,6 +807,12 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 Item &it = items[i];
                 const cigpu_request &q = req[i];
                 int stc = cigpu_ham_create(q.L, q.nup, q.ndown, q.econst, q.h, q.eri, &it.ham);
+                if (stc == CIGPU_OK && q.rot) {  // orbital rotation on the device
+                    cigpu_ham *rotated = nullptr;
+                    stc = cigpu_ham_rotate(it.ham, q.rot, s, &rotated);
+                    cigpu_ham_destroy(it.ham);
+                    it.ham = rotated;
+                }
                 if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, CIGPU_FP64, s, &it.crs);
                 it.status = stc;
                 if (stc != CIGPU_OK && failed[t] == CIGPU_OK) failed[t] = stc;

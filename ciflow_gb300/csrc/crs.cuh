@@ -51,4 +51,6 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
 int status_from_exception();
 // CIGPU_EINVAL unless h is symmetric and eri 8-fold symmetric (1e-10 relative) and all finite.
 int validate_integrals(int L, const double *h, const double *eri, bool *exact);
+// CIGPU_EINVAL unless U (L x L, row-major) is finite and orthogonal to 1e-10.
+int validate_rotation(int L, const double *U);
 }  // namespace cigpu

@@ -35,7 +35,7 @@ double now_s() { return std::chrono::duration<double>(std::chrono::steady_clock:
 struct Request {
     uint64_t id = 0;
     cigpu_request r{};
-    std::vector<double> h, eri, c0;
+    std::vector<double> h, eri, c0, rot;
     size_t bytes = 0;
     int64_t dim = 0;
     int status = CIGPU_OK;
@@ -60,6 +60,7 @@ int validate(const cigpu_request &q) {
     if (q.method == CIGPU_DOCI && q.nup != q.ndown) return CIGPU_EINVAL;
     if (!q.h || !q.eri || !(q.tol > 0) || !std::isfinite(q.econst)) return CIGPU_EINVAL;
     if (cigpu::validate_integrals(q.L, q.h, q.eri, nullptr) != CIGPU_OK) return CIGPU_EINVAL;
+    if (q.rot && cigpu::validate_rotation(q.L, q.rot) != CIGPU_OK) return CIGPU_EINVAL;
     const int64_t d = dim_of(q.L, q.nup, q.ndown, q.method);
     if (d < 1 || d > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     return CIGPU_OK;
@@ -114,6 +115,12 @@ struct cigpu_server {
         cigpu_ham *ham = nullptr;
         cigpu_crs *crs = nullptr;
         int st = cigpu_ham_create(q.r.L, q.r.nup, q.r.ndown, q.r.econst, q.h.data(), q.eri.data(), &ham);
+        if (st == CIGPU_OK && !q.rot.empty()) {  // orbital rotation on the device
+            cigpu_ham *rotated = nullptr;
+            st = cigpu_ham_rotate(ham, q.rot.data(), s, &rotated);
+            cigpu_ham_destroy(ham);
+            ham = rotated;
+        }
         if (st == CIGPU_OK) st = cigpu_build(ham, q.r.method, q.r.precision, s, &crs);
         bool cancelled;
         {
@@ -203,7 +210,8 @@ int cigpu_server_submit(cigpu_server *srv, const cigpu_request *req, uint64_t *i
     q->h.assign(req->h, req->h + L * L);
     q->eri.assign(req->eri, req->eri + L * L * L * L);
     if (req->c0) q->c0.assign(req->c0, req->c0 + q->dim);
-    q->r.h = q->r.eri = q->r.c0 = nullptr;
+    if (req->rot) q->rot.assign(req->rot, req->rot + L * L);
+    q->r.h = q->r.eri = q->r.c0 = q->r.rot = nullptr;
     q->bytes = cigpu::estimate_bytes(req->L, req->nup, req->ndown, req->method, req->precision);
     std::lock_guard<std::mutex> lock(srv->mu);
     if (q->bytes > srv->budget) return CIGPU_ENOMEM;  // can never fit

@@ -40,14 +40,16 @@ class Server:
         self._pending: dict[int, _Pending] = {}
 
     def submit(self, ints, method: int = A.FCI, precision: int = A.MIXED, tol: float = 1e-6,
-               want_rdm: bool = False, c0: np.ndarray | None = None) -> int:
+               want_rdm: bool = False, c0: np.ndarray | None = None, rot: np.ndarray | None = None) -> int:
         """Queues one lowest-eigenpair solve; raises CigpuError (EAGAIN: queue full,
-        ENOMEM: can never fit the budget, EINVAL: bad integrals)."""
+        ENOMEM: can never fit the budget, EINVAL: bad integrals or rotation). `rot`: an
+        orthogonal L x L matrix U; the integrals are rotated by it on the device first."""
         hh = np.ascontiguousarray(ints.h, dtype=np.float64)
         ee = np.ascontiguousarray(ints.eri, dtype=np.float64)
         cc = None if c0 is None else np.ascontiguousarray(c0, dtype=np.float64)
+        uu = None if rot is None else np.ascontiguousarray(rot, dtype=np.float64)
         req = A.Request(ints.L, ints.nup, ints.ndown, method, precision, int(want_rdm), ints.econst, tol,
-                        A.ptr(hh), A.ptr(ee), A.ptr(cc))
+                        A.ptr(hh), A.ptr(ee), A.ptr(cc), A.ptr(uu))
         rid = ctypes.c_uint64()
         A.check(A.lib().cigpu_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid)), "cigpu_server_submit")
         self._pending[rid.value] = _Pending(ints.L, request_dim(ints.L, ints.nup, ints.ndown, method), want_rdm)

@@ -86,6 +86,19 @@ int64_t cigpu_kernel_launches(void);
 int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, const double *eri,
                      cigpu_ham **out);
 int cigpu_ham_destroy(cigpu_ham *ham);
+/* ---- orbital rotation: replaces OrbitalTransform::fillHamCI and rotate_old_to_new
+ * (OrbitalTransform.cpp:64-170). Creates a new Hamiltonian with the integrals of
+ * `base` rotated on the device by the orthogonal L x L matrix U (row-major,
+ * U[a*L + p]): h'_ab = sum U_ap U_bq h_pq, (ab|cd)' = sum U_ap U_bq U_cr U_ds (pq|rs),
+ * made exactly 8-fold symmetric. Runs on `stream` (NULL: a private stream) and
+ * returns when done. CIGPU_EINVAL if U is not orthogonal to 1e-10. ---- */
+int cigpu_ham_rotate(const cigpu_ham *base, const double *U, cigpu_stream stream, cigpu_ham **out);
+/* Integrals held by a Hamiltonian (h: L*L, eri: L^4 chemist; either may be NULL),
+ * e.g. after cigpu_ham_rotate; getTmat/getVmat (Hamiltonian.cpp:255-320). */
+int cigpu_ham_export(const cigpu_ham *ham, double *h, double *eri);
+/* U = exp(X) for an antisymmetric L x L generator X (row-major), the unitary of
+ * UnitaryMatrix::updateUnitary (UnitaryMatrix.cpp:229-290). Host computation. */
+int cigpu_unitary_exp(int L, const double *X, double *U);
 
 /* ---- CRS build: replaces new FCI(ham) / new DOCI(ham), i.e.
  * CIMethod::build_parallel + FCI::construct_CI_matrix / DOCI::construct_CI_matrix
@@ -169,6 +182,8 @@ typedef struct {
     const double *h;     /* copied at submit */
     const double *eri;   /* copied at submit */
     const double *c0;    /* optional warm start (dim), copied at submit */
+    const double *rot;   /* optional L x L orbital rotation U applied to (h, eri) on the
+                            device before the build (cigpu_ham_rotate); copied at submit */
 } cigpu_request;
 
 typedef struct {

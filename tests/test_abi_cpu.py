@@ -79,3 +79,19 @@ def test_server_arguments_checked_on_host(lib):
     assert lib.cigpu_server_destroy(None) == A.OK
     if A.device_count() == 0:  # no GPU: refused, never a crash
         assert lib.cigpu_server_create(0, 0, 4, 16, ctypes.byref(out)) == A.ECUDA
+
+
+def test_unitary_exp_matches_scipy(lib):
+    import scipy.linalg
+    from ciflow_gb300.ciflow import unitary_exp
+    rng = np.random.default_rng(3)
+    for L, sigma in ((1, 0.1), (6, 0.05), (12, 0.3), (24, 2.0)):
+        k = np.triu(rng.normal(0, sigma, (L, L)), 1)
+        X = k - k.T
+        U = unitary_exp(X)
+        np.testing.assert_allclose(U, scipy.linalg.expm(X), atol=1e-13 * max(1.0, np.abs(X).max()) * L)
+        np.testing.assert_allclose(U @ U.T, np.eye(L), atol=1e-12 * L)
+    bad = np.ones((3, 3))  # not antisymmetric
+    assert lib.cigpu_unitary_exp(3, A.ptr(bad), A.ptr(np.empty((3, 3)))) == A.EINVAL
+    assert lib.cigpu_ham_rotate(None, None, None, None) == A.EINVAL
+    assert lib.cigpu_ham_export(None, None, None) == A.EINVAL
