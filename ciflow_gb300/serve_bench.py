@@ -2,7 +2,9 @@
 
 The stream is the L=10 5a5b FCI problem (63,504 determinants) under random
 orbital rotations U = exp(kappa) of one seeded base integral set, as in an
-orbital-optimisation sweep (CIFlow SimulatedAnnealing.cpp:72-86, 130-134), mixed
+orbital-optimisation sweep (CIFlow SimulatedAnnealing.cpp:72-86, 130-134); each
+such request carries the base integrals and its U, and the server rotates the
+integrals on the device (cigpu_ham_rotate) inside the measured path. Mixed
 with uneven problems of the batched-solve shape (L uniform in 6..12, FCI with
 1..L/2 electrons per spin or DOCI with 2..L/2 pairs) and a few L=12 6a6b
 requests. The same request list runs through the mixed FP32/FP64 form and the
@@ -22,11 +24,25 @@ import numpy as np
 
 from . import _abi as A
 from .server import Server
-from .synthetic import make_integrals, rotate_integrals
+from .ciflow import unitary_exp
+from .synthetic import make_integrals
+
+
+def rotation(L: int, sigma: float, seed: int) -> np.ndarray:
+    """U = exp(-kappa) with kappa antisymmetric, N(0, sigma) entries drawn as
+    synthetic.rotate_integrals draws them; rotating by U on the device gives the
+    integrals rotate_integrals computes on the host."""
+    rng = np.random.default_rng(seed)
+    k = np.zeros((L, L))
+    iu = np.triu_indices(L, 1)
+    k[iu] = rng.normal(0.0, sigma, size=len(iu[0]))
+    return unitary_exp(-(k - k.T))
 
 
 def make_stream(n: int, seed: int = 4, frac_other: float = 0.15, every_big: int = 100):
-    """Request list [(kind, ints, method)], deterministic in `seed`."""
+    """Request list [(kind, ints, method, rotation or None)], deterministic in `seed`.
+    The L=10 requests carry the base integrals and their rotation, applied on the
+    device by the server (cigpu_ham_rotate)."""
     rng = np.random.default_rng(seed + 17)
     base = make_integrals(10, 5, 5, nchol=16, seed=seed)
     big = None
@@ -35,17 +51,17 @@ def make_stream(n: int, seed: int = 4, frac_other: float = 0.15, every_big: int 
         if every_big and i % every_big == every_big // 2:
             if big is None:
                 big = make_integrals(12, 6, 6, nchol=16, seed=1)
-            out.append(("c1", big, A.FCI))
+            out.append(("c1", big, A.FCI, None))
         elif rng.random() < frac_other:
             L = int(rng.integers(6, 13))
             if rng.random() < 0.5:
                 ne = int(rng.integers(1, L // 2 + 1))
-                out.append(("c3", make_integrals(L, ne, ne, nchol=16, seed=1000 + i), A.FCI))
+                out.append(("c3", make_integrals(L, ne, ne, nchol=16, seed=1000 + i), A.FCI, None))
             else:
                 p = int(rng.integers(2, L // 2 + 1))
-                out.append(("c3", make_integrals(L, p, p, nchol=16, seed=1000 + i), A.DOCI))
+                out.append(("c3", make_integrals(L, p, p, nchol=16, seed=1000 + i), A.DOCI, None))
         else:
-            out.append(("c4", rotate_integrals(base, 0.05, seed=10**6 + i), A.FCI))
+            out.append(("c4", base, A.FCI, rotation(10, 0.05, 10**6 + i)))
     return out
 
 
@@ -60,22 +76,22 @@ def run_stream(stream, precision: int, rate: float, tol: float, max_inflight: in
     with Server(max_inflight=max_inflight, max_queue=1 << 16) as srv:
         # warm-up: one request of each kind builds the allocator cache and kernel state
         seen = set()
-        for kind, ints, m in stream:
+        for kind, ints, m, rot in stream:
             if kind not in seen:
                 seen.add(kind)
-                srv.wait(srv.submit(ints, method=m, precision=precision, tol=tol))
+                srv.wait(srv.submit(ints, method=m, precision=precision, tol=tol, rot=rot))
         ids = [None] * len(stream)
         results = [None] * len(stream)
         t0 = time.perf_counter()
 
         def submitter():
             t = t0
-            for i, (kind, ints, m) in enumerate(stream):
+            for i, (kind, ints, m, rot) in enumerate(stream):
                 t += gaps[i]
                 d = t - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
-                ids[i] = srv.submit(ints, method=m, precision=precision, tol=tol)
+                ids[i] = srv.submit(ints, method=m, precision=precision, tol=tol, rot=rot)
 
         th = threading.Thread(target=submitter)
         th.start()
@@ -89,7 +105,7 @@ def run_stream(stream, precision: int, rate: float, tol: float, max_inflight: in
 def summarise(stream, results, wall):
     lat = {"all": [r["latency_s"] for r in results]}
     for k in ("c4", "c3", "c1"):
-        lat[k] = [r["latency_s"] for (kind, _, _), r in zip(stream, results) if kind == k]
+        lat[k] = [r["latency_s"] for (kind, _, _, _), r in zip(stream, results) if kind == k]
     ok = sum(r["status"] == A.OK for r in results)
     return {
         "solves_per_s": len(results) / wall,
