@@ -54,6 +54,31 @@ class Result(ctypes.Structure):
                 ("queued_s", _D), ("latency_s", _D)]
 
 
+class OrboptConfig(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("tol", _D),
+                ("warm_start", ctypes.c_int32), ("reserved", ctypes.c_int32), ("seed", ctypes.c_uint64)]
+
+
+class AnnealParams(ctypes.Structure):
+    _fields_ = [("temp", _D), ("change_temp", _D), ("max_angle", _D), ("change_angle", _D),
+                ("steps", _I64), ("max_unaccept", _I64), ("min_angle", _D), ("speculate", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class LocalParams(ctypes.Structure):
+    _fields_ = [("conv_crit", _D), ("conv_steps", ctypes.c_int32), ("max_iters", ctypes.c_int32),
+                ("dist_choice", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class OrboptStats(ctypes.Structure):
+    _fields_ = [("e_current", _D), ("e_opt", _D), ("solves", _I64), ("steps", _I64), ("accepted", _I64),
+                ("rejected", _I64), ("speculative_waste", _I64), ("matvecs_fp64", _I64), ("matvecs_fp32", _I64),
+                ("seconds_solve", _D), ("seconds_scan", _D), ("seconds", _D)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # name -> (restype, argtypes); every symbol include/cigpu.h declares
 SIGNATURES = {
     "cigpu_get_version": (_I, []),
@@ -84,6 +109,17 @@ SIGNATURES = {
     "cigpu_server_destroy": (_I, [_P]),
     "cigpu_solve_batch": (_I, [_I, _P, _I64, _P, _P, _P, _P]),
     "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
+    "cigpu_ham_jacobi": (_I, [_P, _I, _I, _D, _P, _P]),
+    "cigpu_doci_pair_scan": (_I, [_P, _P, _P, _P, _P]),
+    "cigpu_orbopt_create": (_I, [_P, _P, _P]),
+    "cigpu_orbopt_destroy": (_I, [_P]),
+    "cigpu_orbopt_anneal": (_I, [_P, _P, _P]),
+    "cigpu_orbopt_local": (_I, [_P, _P, _P]),
+    "cigpu_orbopt_jacobi": (_I, [_P, _I, _I, _D, _P]),
+    "cigpu_orbopt_natural": (_I, [_P, _I, _P]),
+    "cigpu_orbopt_set_optimal": (_I, [_P]),
+    "cigpu_orbopt_get": (_I, [_P, _P, _P, _P, _P]),
+    "cigpu_orbopt_ham": (_I, [_P, _P]),
 }
 
 _lib = None

@@ -98,6 +98,17 @@ class Hamiltonian:
         A.check(A.lib().cigpu_ham_export(H._dev.value, A.ptr(H.h), A.ptr(H.eri)), "cigpu_ham_export")
         return H
 
+    def jacobi(self, k: int, l: int, theta: float) -> "Hamiltonian":
+        """The Hamiltonian with orbitals k, l rotated by theta (k' = cos k - sin l,
+        l' = sin k + cos l), computed on the device (cigpu_ham_jacobi; the reference's
+        OrbitalTransform::do_jacobi_rotation, OrbitalTransform.cpp:278-414)."""
+        out = ctypes.c_void_p()
+        A.check(A.lib().cigpu_ham_jacobi(self.device(), k, l, theta, None, ctypes.byref(out)), "cigpu_ham_jacobi")
+        H = Hamiltonian(self.L, 0, self.nup, self.ndown, self.Econst)
+        H._dev = _Handle(out.value, A.lib().cigpu_ham_destroy)
+        A.check(A.lib().cigpu_ham_export(H._dev.value, A.ptr(H.h), A.ptr(H.eri)), "cigpu_ham_export")
+        return H
+
 
 def unitary_exp(X: np.ndarray) -> np.ndarray:
     """exp(X) of an antisymmetric generator (UnitaryMatrix.cpp:229-290), host code of the library."""

@@ -283,6 +283,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     c.row_ptr.alloc(dim + 1);
     tr.mark("alloc small");
     if (c.method == CIGPU_FCI) {
+        if (!h.host_valid) throw std::logic_error("FCI build needs the host copy of the integrals");
         build_spin_tables(c.L, c.nup, h.h.data(), h.eri.data(), c.ta);
         tr.mark("host tables");
         c.da.upload(c.ta, s);
@@ -446,6 +447,27 @@ int validate_integrals(int L, const double *h, const double *eri, bool *exact_ou
                 }
     if (exact_out) *exact_out = exact;
     return CIGPU_OK;
+}
+
+int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, bool have_start, cigpu_solve_info &info,
+              cudaStream_t stream) {
+    cudaStream_t s = stream ? stream : crs.stream;
+    cigpu_crs *cp = &crs;
+    SolveProblem P;
+    P.n = crs.dim;
+    P.stream = s;
+    P.diag = crs.diag.p;
+    P.mv64 = [cp](const double *x, double *y, cudaStream_t st) { crs_mv64(*cp, x, y, st); };
+    if (crs.precision == CIGPU_MIXED)
+        P.mv32 = [cp](const float *x, float *y, cudaStream_t st) { crs_mv32(*cp, x, y, st); };
+    SolveOptions o;
+    o.tol = tol;
+    o.max_matvec = max_matvec;
+    info = cigpu_solve_info{};
+    const int st = crs.precision == CIGPU_MIXED ? solve_mixed(P, o, c_dev, have_start, info)
+                                                : solve_fp64(P, o, c_dev, have_start, info);
+    info.e0 += crs.ham->econst;
+    return st;
 }
 
 }  // namespace cigpu
@@ -706,20 +728,8 @@ int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0
     StreamScope scope(s);
     DevBuf<double> c(crs->dim);
     if (c0) CIGPU_CUDA(cudaMemcpyAsync(c.p, c0, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));
-    SolveProblem P;
-    P.n = crs->dim;
-    P.stream = s;
-    P.diag = crs->diag.p;
-    P.mv64 = [crs](const double *x, double *y, cudaStream_t st) { crs_mv64(*crs, x, y, st); };
-    if (crs->precision == CIGPU_MIXED)
-        P.mv32 = [crs](const float *x, float *y, cudaStream_t st) { crs_mv32(*crs, x, y, st); };
-    SolveOptions o;
-    o.tol = tol;
-    o.max_matvec = max_matvec;
     cigpu_solve_info inf{};
-    const int st = crs->precision == CIGPU_MIXED ? solve_mixed(P, o, c.p, c0 != nullptr, inf)
-                                                 : solve_fp64(P, o, c.p, c0 != nullptr, inf);
-    inf.e0 += crs->ham->econst;
+    const int st = solve_crs(*crs, tol, max_matvec, c.p, c0 != nullptr, inf);
     if (c_out) CIGPU_CUDA(cudaMemcpyAsync(c_out, c.p, sizeof(double) * crs->dim, cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaStreamSynchronize(s));
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -166,6 +166,9 @@ struct cigpu_ham {
     double econst;
     std::vector<double> h;    // host copy, L*L
     std::vector<double> eri;  // host copy, L^4 chemist
+    // false: h/eri are not filled (a Hamiltonian made on the device for a DOCI
+    // build, which reads the device tables only); the device tables are current
+    bool host_valid = true;
     cigpu::DevBuf<double> d_h;
     cigpu::DevBuf<double> d_eri;
     cigpu::DevBuf<float> d_eri_hi, d_eri_lo;  // FP32 split, zero where |v| <= 1e-14

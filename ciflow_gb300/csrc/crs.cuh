@@ -53,4 +53,18 @@ int status_from_exception();
 int validate_integrals(int L, const double *h, const double *eri, bool *exact);
 // CIGPU_EINVAL unless U (L x L, row-major) is finite and orthogonal to 1e-10.
 int validate_rotation(int L, const double *U);
+// Lowest eigenpair of a built CRS with a device vector: c_dev holds the start when
+// have_start, and the normalised eigenvector on return. Runs on `stream` (NULL:
+// the CRS stream); info.e0 includes Econst. Returns CIGPU_OK or CIGPU_ENOCONV.
+int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, bool have_start, cigpu_solve_info &info,
+              cudaStream_t stream = nullptr);
+// Rotated Hamiltonian h' = U h U^T, (ab|cd)' = sum U U U U (pq|rs) (host U, row-major).
+void rotate_ham(const cigpu_ham &base, const double *U, cigpu_ham &H, cudaStream_t s);
+// exp(X) of an antisymmetric L x L generator (host).
+void unitary_exp(int L, const double *X, double *U);
+// DOCI: blocks of partial sums doci_pair_matrices needs (partial holds 2 L^2 doubles per block).
+int doci_pair_partials();
+// DOCI pair matrices of device vector c (normalised): Pm[j][k] = Gamma_ab(jj,kk),
+// Dm[j][k] = Gamma_aa(jk,jk) (zero diagonal); device outputs, L x L each.
+void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, double *Pm, double *Dm, cudaStream_t s);
 }  // namespace cigpu

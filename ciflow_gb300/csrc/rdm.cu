@@ -440,6 +440,25 @@ __global__ void k_doci_rdm_finish(const double *__restrict__ partial, int G, int
     }
 }
 
+// The two L x L matrices a DOCI state's RDMs reduce to, in CIDens element terms:
+//   Pm[j][k] = get_two_rdm(1, j, j, k, k)   (pair hop B_jk; A_jj on the diagonal)
+//   Dm[j][k] = get_two_rdm(0, j, k, j, k)   (A_jk; zero on the diagonal)
+__global__ void k_doci_pairs_finish(const double *__restrict__ partial, int G, int L, double *__restrict__ Pm,
+                                    double *__restrict__ Dm) {
+    const int L2 = L * L;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L2) return;
+    const int j = t / L, k = t % L;
+    const int tb = j < k ? t : k * L + j;  // B is accumulated for j < k only
+    double A = 0, B = 0;
+    for (int b = 0; b < G; ++b) {
+        A += partial[((int64_t)b * 2) * L2 + t];
+        B += partial[((int64_t)b * 2 + 1) * L2 + tb];
+    }
+    Pm[t] = j == k ? A : B;
+    Dm[t] = j == k ? 0.0 : A;
+}
+
 template <typename T>
 DevBuf<T> upload(const std::vector<T> &v, cudaStream_t s) {
     DevBuf<T> d(std::max<size_t>(v.size(), 1));
@@ -566,6 +585,18 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
     if (bb) CIGPU_CUDA(cudaMemcpyAsync(bb, obb, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
     if (ab) CIGPU_CUDA(cudaMemcpyAsync(ab, oab, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaStreamSynchronize(s));
+}
+
+int doci_pair_partials() { return sm_count() * 4; }
+
+void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, double *Pm, double *Dm, cudaStream_t s) {
+    if (c.method != CIGPU_DOCI || c.L > 32) throw std::invalid_argument("DOCI pair matrices need a DOCI CRS, L <= 32");
+    const int L = c.L, G = doci_pair_partials();
+    const int th = ((L * L + 31) / 32) * 32;
+    k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial);
+    k_doci_pairs_finish<<<(L * L + 255) / 256, 256, 0, s>>>(partial, G, L, Pm, Dm);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch(2);
 }
 
 }  // namespace cigpu

@@ -200,6 +200,17 @@ int cigpu_unitary_exp(int L, const double *X, double *U) {
 
 int cigpu_ham_export(const cigpu_ham *ham, double *h, double *eri) {
     if (!ham) return CIGPU_EINVAL;
+    if (!ham->host_valid) {
+        // device-only Hamiltonian: its producer synchronised its stream, so plain copies are ordered
+        try {
+            const size_t L2 = (size_t)ham->L * ham->L;
+            if (h) CIGPU_CUDA(cudaMemcpy(h, ham->d_h.p, sizeof(double) * L2, cudaMemcpyDeviceToHost));
+            if (eri) CIGPU_CUDA(cudaMemcpy(eri, ham->d_eri.p, sizeof(double) * L2 * L2, cudaMemcpyDeviceToHost));
+            return CIGPU_OK;
+        } catch (...) {
+            return status_from_exception();
+        }
+    }
     if (h) std::memcpy(h, ham->h.data(), sizeof(double) * ham->h.size());
     if (eri) std::memcpy(eri, ham->eri.data(), sizeof(double) * ham->eri.size());
     return CIGPU_OK;

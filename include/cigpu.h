@@ -238,6 +238,104 @@ int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_d
 /* Device memory a request of this shape needs (bytes), as used by admission. */
 int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes);
 
+/* ---- Jacobi rotation of two orbitals: replaces OrbitalTransform::do_jacobi_rotation
+ * (OrbitalTransform.cpp:278-414) for point group C1. Creates a new Hamiltonian whose
+ * orbitals k and l are k' = cos(theta) k - sin(theta) l, l' = sin(theta) k + cos(theta) l
+ * (the rows of the unitary, UnitaryMatrix::jacobi_rotation, UnitaryMatrix.cpp:186-207),
+ * all other orbitals unchanged; the result is exactly 8-fold symmetric. Runs on
+ * `stream` (NULL: a private stream) and returns when done. ---- */
+int cigpu_ham_jacobi(const cigpu_ham *base, int k, int l, double theta, cigpu_stream stream, cigpu_ham **out);
+
+/* ---- DOCI pair scan: replaces LocalMinimizer::scan_orbitals (LocalMinimizer.cpp:73-128)
+ * with DensDOCI::find_min_angle and calc_rotate (CIDens.cpp:1279-1464), on the device.
+ * crs: a DOCI CRS (L <= 32); c: host, dim (its normalised ground state). For every
+ * orbital pair k < l (index k*L + l - (k+1)(k+2)/2) the Newton search for the Jacobi
+ * angle of lowest energy starts at 0.3 and, if it ends on a maximum, again at 0.01:
+ * theta[p] is that angle, energy[p] the energy after the rotation (without Econst, as
+ * calc_rotate returns it) and found[p] = 1 when it is a minimum with |theta| <= pi/2
+ * (the pairs scan_orbitals keeps). Host outputs of L(L-1)/2 entries. ---- */
+int cigpu_doci_pair_scan(cigpu_crs *crs, const double *c, double *theta, double *energy, int32_t *found);
+
+/* ---- orbital optimisation: replaces OrbitalOptimization with its subclasses
+ * SimulatedAnnealing (SimulatedAnnealing.cpp:42-156, 195-391) and LocalMinimizer
+ * (LocalMinimizer.cpp:23-29, 73-280): the set_ham -> solve loop over rotated orbitals,
+ * with every Hamiltonian, CRS, eigenvector and pair scan on the device. The
+ * optimiser owns a device copy of the starting Hamiltonian (`ham` may be destroyed
+ * after create), the current orbitals as a unitary U (row-major, U[a*L+p]: row a is
+ * the current orbital a in the starting orbitals, as UnitaryMatrix stores it) with
+ * their solved ground state, and the lowest energy seen with its unitary. ---- */
+typedef struct cigpu_orbopt cigpu_orbopt;
+
+typedef struct {
+    int32_t method;      /* cigpu_method: the CIMethod whose energy is optimised */
+    int32_t precision;   /* cigpu_precision of every build and solve */
+    double tol;          /* FP64 residual target of every solve */
+    int32_t warm_start;  /* 1: each solve starts from the current eigenvector (the
+                            reference restarts ARPACK from scratch) */
+    int32_t reserved;
+    uint64_t seed;       /* random streams of the optimisers (splitmix64) */
+} cigpu_orbopt_config;
+
+/* SimulatedAnnealing(cim, temp, change_temp, angle, change_angle) and its loop
+ * limits (SimulatedAnnealing.cpp:195-204, 306-391). */
+typedef struct {
+    double temp;           /* start temperature */
+    double change_temp;    /* temperature factor per step */
+    double max_angle;      /* start of the angle range: angle = max_angle (u1 - u2) */
+    double change_angle;   /* angle-range factor per step */
+    int64_t steps;         /* loop iterations (_c_steps, 20000 in the reference) */
+    int64_t max_unaccept;  /* stop after more consecutive rejections (2000) */
+    double min_angle;      /* stop when the angle range falls below (1e-7) */
+    int32_t speculate;     /* proposals solved concurrently (1: one at a time); the
+                              chain is the same for every value */
+    int32_t reserved;
+} cigpu_anneal_params;
+
+/* LocalMinimizer (LocalMinimizer.cpp:23-29, 130-235). */
+typedef struct {
+    double conv_crit;     /* |dE| counted as converged (1e-6) */
+    int32_t conv_steps;   /* converged iterations to stop (25) */
+    int32_t max_iters;    /* iteration limit (1000) */
+    int32_t dist_choice;  /* 1: draw the pair by energy gain (choose_orbitalpair) */
+    int32_t reserved;
+} cigpu_local_params;
+
+typedef struct {
+    double e_current;       /* energy of the current orbitals, with Econst */
+    double e_opt;           /* OrbitalOptimization::_opt_energy */
+    int64_t solves;         /* builds + eigensolves */
+    int64_t steps;          /* annealing steps decided / local iterations */
+    int64_t accepted, rejected;
+    int64_t speculative_waste;  /* solves of proposals discarded after an earlier acceptance */
+    int64_t matvecs_fp64, matvecs_fp32;
+    double seconds_solve;   /* rotation + build + eigensolve, summed over solves */
+    double seconds_scan;    /* DOCI pair matrices + pair scan */
+    double seconds;         /* wall time inside the optimiser calls */
+} cigpu_orbopt_stats;
+
+/* OrbitalOptimization(cim): copies the Hamiltonian and solves it (U = 1). */
+int cigpu_orbopt_create(const cigpu_ham *ham, const cigpu_orbopt_config *cfg, cigpu_orbopt **out);
+int cigpu_orbopt_destroy(cigpu_orbopt *opt);
+/* SimulatedAnnealing::optimize; e_last = the energy of the final current orbitals
+ * (the return value of the reference). Each call draws its proposals from a fresh
+ * stream derived from the seed and the call count. */
+int cigpu_orbopt_anneal(cigpu_orbopt *opt, const cigpu_anneal_params *p, double *e_last);
+/* LocalMinimizer::optimize (DOCI only); e_final as returned by the reference.
+ * CIGPU_ENOCONV when a scan finds no pair to rotate. */
+int cigpu_orbopt_local(cigpu_orbopt *opt, const cigpu_local_params *p, double *e_final);
+/* OrbitalOptimization::transform_orbitals + update_cim: one Jacobi rotation, solved. */
+int cigpu_orbopt_jacobi(cigpu_orbopt *opt, int k, int l, double theta, double *e);
+/* OrbitalOptimization::get_cim_no (density_method = the optimiser's method) or
+ * get_fci_no (CIGPU_FCI): rotate to the natural orbitals of that method's ground
+ * state in the current orbitals (SimulatedAnnealing.cpp:120-156) and solve. */
+int cigpu_orbopt_natural(cigpu_orbopt *opt, int density_method, double *e);
+/* OrbitalOptimization::set_cim_optimal: current orbitals = the best seen, solved. */
+int cigpu_orbopt_set_optimal(cigpu_orbopt *opt);
+/* Current state: U and U_opt (L*L), c (dim) and stats; each output optional. */
+int cigpu_orbopt_get(const cigpu_orbopt *opt, double *U, double *U_opt, double *c, cigpu_orbopt_stats *stats);
+/* A new Hamiltonian handle with the current orbitals' integrals (get_ham of the CIMethod). */
+int cigpu_orbopt_ham(const cigpu_orbopt *opt, cigpu_ham **out);
+
 #ifdef __cplusplus
 }
 #endif

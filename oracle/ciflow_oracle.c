@@ -120,7 +120,7 @@ static double diag_one(const ham_t *H, const int *o, int n) {
 
 /* CIMethod::diagonal (CIMethod.cpp:398-407) with get_diag_cont_jmix (:344-351). */
 static double diagonal(const ham_t *H, bits_t up, bits_t dn) {
-    int ou[64], od[64];
+    int ou[64] = {0}, od[64] = {0};
     int nu = get_orbs(up, ou), nd = get_orbs(dn, od);
     double tot = diag_one(H, ou, nu);
     tot += diag_one(H, od, nd);

@@ -92,6 +92,10 @@ def ref():
         lib.ref_ci_mvprod.argtypes = [_P] * 3
         lib.ref_ci_density.restype = ctypes.c_double
         lib.ref_ci_density.argtypes = [_P, ctypes.c_double] + [_P] * 5
+        lib.ref_jacobi.restype = ctypes.c_int
+        lib.ref_jacobi.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [_P] * 2 + [ctypes.c_int] + [_P] * 6
+        lib.ref_doci_scan.restype = ctypes.c_int
+        lib.ref_doci_scan.argtypes = [_P, ctypes.c_double] + [_P] * 4 + [ctypes.c_int] + [_P] * 2
         _ref = lib
     return _ref
 
@@ -299,6 +303,22 @@ class RefCI:
         ed = self.lib.ref_ci_density(self.h, e, _ptr(c), _ptr(r1), _ptr(aa), _ptr(ab), _ptr(bb))
         return (r1, aa, ab, bb), ed
 
+    def doci_scan(self, L: int, e: float, c: np.ndarray, fixed=()):
+        """DensDOCI::find_min_angle / calc_rotate for every pair k < l, with the
+        selection of LocalMinimizer::scan_orbitals: (theta, energy, found, fixed_energy)."""
+        np_ = L * (L - 1) // 2
+        th = np.zeros(np_)
+        en = np.zeros(np_)
+        fd = np.zeros(np_, np.int32)
+        fx = np.ascontiguousarray(np.asarray(fixed, dtype=np.float64))
+        fe = np.zeros((np_, len(fx)))
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        rc = self.lib.ref_doci_scan(self.h, e, _ptr(c), _ptr(th), _ptr(en), _ptr(fd), len(fx),
+                                    _ptr(fx) if len(fx) else None, _ptr(fe) if len(fx) else None)
+        if rc != 0:
+            raise ValueError("reference DOCI scan needs a DOCI object")
+        return th, en, fd, fe
+
     def close(self):
         if self.h:
             self.lib.ref_ci_destroy(self.h)
@@ -309,3 +329,21 @@ class RefCI:
             self.close()
         except Exception:
             pass
+
+
+def ref_jacobi(ints, rotations):
+    """OrbitalTransform::do_jacobi_rotation applied in order for (k, l, theta) in
+    `rotations`: (h, eri chemist, U row-major) from the reference."""
+    lib = ref()
+    L = ints.L
+    k = np.array([r[0] for r in rotations], np.int32)
+    l = np.array([r[1] for r in rotations], np.int32)
+    th = np.array([r[2] for r in rotations], np.float64)
+    hh = np.ascontiguousarray(ints.h, dtype=np.float64)
+    ee = np.ascontiguousarray(ints.eri, dtype=np.float64)
+    h = np.zeros((L, L))
+    eri = np.zeros((L,) * 4)
+    U = np.zeros((L, L))
+    lib.ref_jacobi(L, ints.nup, ints.ndown, ints.econst, _ptr(hh), _ptr(ee), len(k), _ptr(k), _ptr(l), _ptr(th),
+                   _ptr(h), _ptr(eri), _ptr(U))
+    return h, eri, U

@@ -14,7 +14,13 @@
 //     so scipy's ARPACK can drive the reference matvec;
 //   * install an eigenvector and run CIDens::construct_density
 //     (CIMethod.cpp:161-171, CIDens.cpp:323-334) and read the RDMs through
-//     get_one_rdm/get_two_rdm (CIDens.cpp:166-292).
+//     get_one_rdm/get_two_rdm (CIDens.cpp:166-292);
+//   * apply Jacobi rotations with OrbitalTransform::do_jacobi_rotation
+//     (OrbitalTransform.cpp:278-414) and read the rotated integrals and the
+//     accumulated unitary (UnitaryMatrix::get_full_transformation, UnitaryMatrix.cpp:167-183);
+//   * evaluate DensDOCI::find_min_angle / calc_rotate (CIDens.cpp:1279-1464) for
+//     every orbital pair, with the pair selection of LocalMinimizer::scan_orbitals
+//     (LocalMinimizer.cpp:89-118).
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -33,6 +39,8 @@
 #include "Hamiltonian.h"
 #include "SparseMatrix_CRS.h"
 #undef protected
+#include "OrbitalTransform.h"
+#include "UnitaryMatrix.h"
 
 namespace {
 
@@ -156,6 +164,70 @@ double ref_ci_density(void *p, double e, const double *c, double *rdm1, double *
                 for (int s = 0; s < L; ++s)
                     rdm2_ab[(p_ * L + q) * L2 + r_ * L + s] = d->get_two_rdm(1, p_, q, r_, s);
     return d->get_dens_energy();
+}
+
+// Applies nrot Jacobi rotations in order to the Hamiltonian built from h/eri
+// (OrbitalTransform::do_jacobi_rotation on the same Hamiltonian object, as the
+// optimisers do). Outputs: h_out (L*L), eri_out (L^4 chemist), U_out (L*L
+// row-major: U[a*L+p] = row a of the reference unitary).
+int ref_jacobi(int L, int nup, int ndown, double econst, const double *h, const double *eri, int nrot, const int *k,
+               const int *l, const double *theta, double *h_out, double *eri_out, double *U_out) {
+    Hamiltonian *ham = make_ham(L, nup, ndown, econst, h, eri);
+    {
+        OrbitalTransform tr(ham);
+        for (int i = 0; i < nrot; ++i) tr.do_jacobi_rotation(k[i], l[i], theta[i], ham);
+        const std::vector<double> u = tr.get_unitary().get_full_transformation();  // column-major
+        for (int a = 0; a < L; ++a)
+            for (int p_ = 0; p_ < L; ++p_) U_out[a * L + p_] = u[a + (size_t)L * p_];
+    }
+    const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1;
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j) h_out[i * L + j] = ham->getTmat(i, j);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j)
+            for (int k_ = 0; k_ < L; ++k_)
+                for (int l_ = 0; l_ < L; ++l_) eri_out[i * L3 + j * L2 + k_ * L1 + l_] = ham->getVmat(i, k_, j, l_);
+    delete ham;
+    return 0;
+}
+
+// DOCI pair scan with the reference density of the installed eigenpair (as in
+// ref_ci_density). For pair index P of k < l: theta/energy/found as
+// LocalMinimizer::scan_orbitals decides them (start 0.3, then 0.01 on a maximum;
+// found = minimum with |theta| <= pi/2), energy = calc_rotate(theta). fixed_energy
+// [P * nfixed + i] = calc_rotate(k, l, fixed[i]) pins the energy expression alone.
+int ref_doci_scan(void *p, double e, const double *c, double *theta, double *energy, int *found, int nfixed,
+                  const double *fixed, double *fixed_energy) {
+    RefCI *r = static_cast<RefCI *>(p);
+    if (r->method != 1) return -1;
+    CIMethod *cim = r->cim;
+    const int dim = cim->get_dim();
+    cim->_eigval = matrix(1, 1);
+    cim->_eigval(0, 0) = e;
+    cim->_eigvec = matrix(dim, 1);
+    for (int i = 0; i < dim; ++i) cim->_eigvec(i, 0) = c[i];
+    cim->_solved = true;
+    cim->_cid->reset_density();
+    cim->construct_density(0, true);
+    const DensDOCI *d = dynamic_cast<const DensDOCI *>(cim->_cid.get());
+    if (!d) return -2;
+    Hamiltonian &ham = *r->ham;
+    std::function<double(int, int)> T = [&ham](int a, int b) -> double { return ham.getTmat(a, b); };
+    std::function<double(int, int, int, int)> V = [&ham](int a, int b, int c_, int d_) -> double {
+        return ham.getVmat(a, b, c_, d_);
+    };
+    const int L = cim->get_l();
+    int P = 0;
+    for (int k = 0; k < L; ++k)
+        for (int l = k + 1; l < L; ++l, ++P) {
+            std::pair<double, bool> f = d->find_min_angle(k, l, 0.3, T, V);
+            if (!f.second) f = d->find_min_angle(k, l, 0.01, T, V);
+            theta[P] = f.first;
+            energy[P] = d->calc_rotate(k, l, f.first, T, V);
+            found[P] = (f.second && std::fabs(f.first) <= M_PI / 2.0) ? 1 : 0;
+            for (int i = 0; i < nfixed; ++i) fixed_energy[P * nfixed + i] = d->calc_rotate(k, l, fixed[i], T, V);
+        }
+    return 0;
 }
 
 }  // extern "C"

@@ -104,10 +104,45 @@ def case_config(name: str, rdm: bool):
     print(name, json.dumps(meta))
 
 
+# Orbital-optimiser pieces of the reference: a sequence of Jacobi rotations
+# (OrbitalTransform::do_jacobi_rotation with the accumulated unitary) and the DOCI
+# pair scan (DensDOCI::find_min_angle / calc_rotate, selection of scan_orbitals)
+# of a DOCI ground state, on seeded L=8 integrals (4 pairs, 70 pair determinants).
+ORBOPT_ROTATIONS = [(0, 3, 0.37), (2, 5, -0.81), (1, 7, 1.3), (0, 3, 0.2), (6, 4, 0.05)]
+ORBOPT_FIXED = [0.1, -0.7, 2.0]
+
+
+def case_orbopt(name: str):
+    from ciflow_gb300.synthetic import make_integrals
+    ints = make_integrals(8, 4, 4, nchol=16, seed=77)
+    h, eri, U = O.ref_jacobi(ints, ORBOPT_ROTATIONS)
+    out = {"h0": ints.h, "eri0": ints.eri, "jac_h": h, "jac_eri": eri, "jac_U": U}
+    meta = {"L": 8, "nup": 4, "ndown": 4, "econst": ints.econst, "seed": 77, "nchol": 16,
+            "rotations": ORBOPT_ROTATIONS, "fixed_angles": ORBOPT_FIXED}
+    # scans in the starting orbitals and after the rotations
+    from ciflow_gb300.synthetic import Integrals
+    for tag, (hh, ee) in (("scan0", (ints.h, ints.eri)), ("scan1", (h, eri))):
+        I = Integrals(8, 4, 4, ints.econst, hh, ee)
+        r = O.RefCI(O.DOCI, ints=I)
+        m = r.crs()
+        e, c = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
+        th, en, fd, fe = r.doci_scan(8, e, c, ORBOPT_FIXED)
+        r.close()
+        out.update({f"{tag}_c": c, f"{tag}_theta": th, f"{tag}_energy": en, f"{tag}_found": fd, f"{tag}_fixed": fe})
+        meta[f"{tag}_e0"] = e + ints.econst
+        meta[f"{tag}_found"] = int(fd.sum())
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta))
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4"]
+    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt"]
     for nm in names:
-        if nm == "beh2_sto3g":
+        if nm == "orbopt":
+            case_orbopt(nm)
+        elif nm == "beh2_sto3g":
             case_file(nm, "beh2_sto3g_1_5.dat")
         elif nm == "be_ccpvdz":
             case_file(nm, "Be_ccpVDZ.dat")
