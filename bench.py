@@ -46,6 +46,8 @@ def parse_args():
                     help="served-stream requests per form (0 skips the served stream)")
     ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
+    ap.add_argument("--orbopt-steps", type=int, default=600,
+                    help="simulated-annealing steps of the orbital-optimisation section (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=512,
                     help="uneven problems of the batched-solve comparison (0 skips it)")
     return ap.parse_args()
@@ -383,6 +385,13 @@ def run_cigpu(args, rank: int, world: int, dist):
         barrier()
         batched = run_batched(args.batched_problems, seed=rank)
 
+    # orbital optimisation: the optimisers' set_ham -> solve loop on the device
+    orbopt = None
+    if args.orbopt_steps > 0:
+        from ciflow_gb300.orbopt_bench import bench_section
+        barrier()
+        orbopt = bench_section(args.orbopt_steps, cpu_steps=20 if (rank == 0 and world == 1) else 0)
+
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
@@ -409,6 +418,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "clocks": clk.summary(),
         "served": served,
         "batched": batched,
+        "orbopt": orbopt,
         "cpu_baseline": cpu,
     }
     print(json.dumps(out), flush=True)

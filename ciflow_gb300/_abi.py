@@ -73,7 +73,8 @@ class LocalParams(ctypes.Structure):
 class OrboptStats(ctypes.Structure):
     _fields_ = [("e_current", _D), ("e_opt", _D), ("solves", _I64), ("steps", _I64), ("accepted", _I64),
                 ("rejected", _I64), ("speculative_waste", _I64), ("matvecs_fp64", _I64), ("matvecs_fp32", _I64),
-                ("seconds_solve", _D), ("seconds_scan", _D), ("seconds", _D)]
+                ("seconds_rotate", _D), ("seconds_build", _D), ("seconds_solve", _D), ("seconds_scan", _D),
+                ("seconds", _D)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -354,7 +354,7 @@ struct State {
     DevBuf<double> c;
     cigpu_solve_info info{};
     int status = CIGPU_OK;
-    double seconds = 0;
+    double t_rotate = 0, t_build = 0, t_solve = 0;
 };
 
 // Persistent worker threads, one stream each, for the speculative solves.
@@ -477,11 +477,14 @@ struct cigpu_orbopt {
         c.stream = ss;
         c.own_stream = false;
         build_crs(c, ss);
+        CIGPU_CUDA(cudaStreamSynchronize(ss));
+        const auto t1 = std::chrono::steady_clock::now();
+        out.t_build = std::chrono::duration<double>(t1 - t0).count();
         out.c.alloc(dim);
         if (c0) CIGPU_CUDA(cudaMemcpyAsync(out.c.p, c0, sizeof(double) * dim, cudaMemcpyDeviceToDevice, ss));
         out.status = solve_crs(c, cfg.tol, 0, out.c.p, c0 != nullptr, out.info, ss);
         CIGPU_CUDA(cudaStreamSynchronize(ss));
-        out.seconds = seconds_since(t0);
+        out.t_solve = seconds_since(t1);
     }
 
     // Jacobi-rotated current Hamiltonian, solved (warm start from the current vector).
@@ -489,22 +492,28 @@ struct cigpu_orbopt {
         const auto t0 = std::chrono::steady_clock::now();
         std::unique_ptr<cigpu_ham> H(new cigpu_ham);
         jacobi_ham(*cur.ham, k, l, angle, *H, ss, host_tables());
+        const double tr = seconds_since(t0);
         solve_into(out, std::move(H), cfg.warm_start ? cur.c.p : nullptr, ss);
-        out.seconds = seconds_since(t0);
+        out.t_rotate = tr;
     }
 
     // Fully rotated Hamiltonian from the start orbitals, solved from scratch.
     void rotate_and_solve(State &out, const std::vector<double> &u) {
+        const auto t0 = std::chrono::steady_clock::now();
         std::unique_ptr<cigpu_ham> H(new cigpu_ham);
         rotate_ham(*base, u.data(), *H, s);
+        const double tr = seconds_since(t0);
         solve_into(out, std::move(H), nullptr, s);
+        out.t_rotate = tr;
     }
 
     void account(const State &x) {
         ++st.solves;
         st.matvecs_fp64 += x.info.matvecs_fp64;
         st.matvecs_fp32 += x.info.matvecs_fp32;
-        st.seconds_solve += x.seconds;
+        st.seconds_rotate += x.t_rotate;
+        st.seconds_build += x.t_build;
+        st.seconds_solve += x.t_solve;
     }
 
     static int ok(int status) { return status == CIGPU_OK || status == CIGPU_ENOCONV; }
@@ -569,10 +578,14 @@ int anneal(cigpu_orbopt &o, const cigpu_anneal_params &p, double *e_last) {
     };
     std::vector<State> cand(K);
     bool stop = false;
+    // Proposals per round: about 1 / (recent acceptance rate), at most K. A round
+    // ends at its first acceptance, so at rate p it uses ~1/p of its proposals.
+    double rate = 0.5;
     while (!stop) {
-        draw((size_t)K);
+        const int want = std::max(1, std::min(K, (int)std::floor(1.0 / std::max(rate, 1e-3))));
+        draw((size_t)want);
         if (pending.empty()) break;
-        const int m = (int)std::min<size_t>(K, pending.size());
+        const int m = (int)std::min<size_t>(want, pending.size());
         std::vector<const Proposal *> batch;
         for (int j = 0; j < m; ++j) batch.push_back(&pending[j]);
         if (m == 1) {
@@ -601,6 +614,7 @@ int anneal(cigpu_orbopt &o, const cigpu_anneal_params &p, double *e_last) {
                 accept = !(o.acc.uniform() * (1 + cost) > cost);
             }
             ++o.st.steps;
+            rate = 0.9 * rate + (accept ? 0.1 : 0.0);
             if (accept) {
                 ++o.st.accepted;
                 e_old = e_new;

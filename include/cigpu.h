@@ -286,8 +286,9 @@ typedef struct {
     int64_t steps;         /* loop iterations (_c_steps, 20000 in the reference) */
     int64_t max_unaccept;  /* stop after more consecutive rejections (2000) */
     double min_angle;      /* stop when the angle range falls below (1e-7) */
-    int32_t speculate;     /* proposals solved concurrently (1: one at a time); the
-                              chain is the same for every value */
+    int32_t speculate;     /* at most this many proposals solved concurrently (1: one
+                              at a time); the number follows the recent acceptance
+                              rate (about 1 / rate); the chain is the same for every value */
     int32_t reserved;
 } cigpu_anneal_params;
 
@@ -308,7 +309,9 @@ typedef struct {
     int64_t accepted, rejected;
     int64_t speculative_waste;  /* solves of proposals discarded after an earlier acceptance */
     int64_t matvecs_fp64, matvecs_fp32;
-    double seconds_solve;   /* rotation + build + eigensolve, summed over solves */
+    double seconds_rotate;  /* integral rotations, summed over solves (concurrent ones add up) */
+    double seconds_build;   /* CRS builds, summed likewise */
+    double seconds_solve;   /* eigensolves, summed likewise */
     double seconds_scan;    /* DOCI pair matrices + pair scan */
     double seconds;         /* wall time inside the optimiser calls */
 } cigpu_orbopt_stats;

@@ -225,8 +225,12 @@ class _Ints:
 
 
 def solve(method: int, L: int, nup: int, ndown: int, econst: float, h, eri):
-    """(E0 with Econst, c) from the oracle CRS and a dense eigensolve."""
+    """(E0 with Econst, c) from the oracle CRS: a dense eigensolve up to 2000
+    determinants, above that ARPACK with the reference's settings."""
     m = O.build_upper(method, _Ints(L, nup, ndown, econst, h, eri))
+    if m.n > 2000:
+        e, c = O.lowest_eigenpair(m)
+        return e + econst, c
     w, v = np.linalg.eigh(m.full_csr().toarray())
     return float(w[0]) + econst, v[:, 0]
 
