@@ -14,9 +14,10 @@ LIB_PATH = os.path.join(HERE, "_lib", "libcigpu.so")
 
 OK, EINVAL, ENOMEM, EAGAIN, ECANCELED, ETIMEDOUT, ENOTSUP, ENOCONV, ECUDA, ENOTFOUND = (
     0, 22, 12, 11, 125, 110, 95, 200, 201, 202)
-FCI, DOCI = 0, 1
+FCI, DOCI, DETS = 0, 1, 2
+DETS_CRS, DETS_ONTHEFLY = 0, 1
 FP64, MIXED = 0, 1
-LAYOUT_CRS, LAYOUT_SLOTS = 0, 1
+LAYOUT_CRS, LAYOUT_SLOTS, LAYOUT_ONTHEFLY = 0, 1, 2
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -110,6 +111,8 @@ SIGNATURES = {
     "cigpu_server_destroy": (_I, [_P]),
     "cigpu_solve_batch": (_I, [_I, _P, _I64, _P, _P, _P, _P]),
     "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
+    "cigpu_build_dets": (_I, [_P, _I64, _I, _P, _P, _I, _I, _P, _P]),
+    "cigpu_dets_read": (_I, [ctypes.c_char_p, _I, _I64, _P, _P, _P, _P]),
     "cigpu_ham_jacobi": (_I, [_P, _I, _I, _D, _P, _P]),
     "cigpu_doci_pair_scan": (_I, [_P, _P, _P, _P, _P]),
     "cigpu_orbopt_create": (_I, [_P, _P, _P]),

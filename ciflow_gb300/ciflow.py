@@ -11,6 +11,9 @@ reads the same:
   (CIMethod.h:37-162).
 * ``SparseMatrix_CRS_Sym`` -- the upper-triangle CRS view with ``mvprod``,
   ``getn``/``getm``/``datasize`` and element access (SparseMatrix_CRS.h:33-130).
+* ``FCI_File`` / ``CI_Big`` -- determinant lists (CIMethod.h:164-189): the CRS
+  of a list, or no stored matrix and elements recomputed in every matvec;
+  ``read_determinants`` reads a determinant file (Permutator.cpp:179-224).
 * ``DensFCI`` / ``DensDOCI`` -- ``construct_density``, ``get_one_rdm``,
   ``get_two_rdm``, ``get_dens_energy`` (CIDens.h:29-174).
 
@@ -321,6 +324,62 @@ class DOCI(CIMethod):
 
     def get_density(self):
         return DensDOCI(self)
+
+
+def read_determinants(path: str, L: int):
+    """Permutator_File::read_file (Permutator.cpp:179-224) through the library's reader:
+    (up, down, words) with `words` 64-bit words per string (2 when L > 64)."""
+    words = 1 if L <= 64 else 2
+    n, nb = ctypes.c_int64(), ctypes.c_int()
+    p = path.encode()
+    A.check(A.lib().cigpu_dets_read(p, words, 0, None, None, ctypes.byref(n), ctypes.byref(nb)), "cigpu_dets_read")
+    up = np.zeros(n.value * words, np.uint64)
+    down = np.zeros(n.value * words, np.uint64)
+    A.check(A.lib().cigpu_dets_read(p, words, n.value, A.ptr(up), A.ptr(down), ctypes.byref(n), ctypes.byref(nb)),
+            "cigpu_dets_read")
+    return up, down, words
+
+
+class FCI_File(CIMethod):
+    """CI over a determinant list (FCI_File, CIMethod.h:164-173): rows in list order.
+    The list comes from a determinant file (``permfile``) or from ``up``/``down``
+    arrays of ``words`` 64-bit words per string."""
+
+    method = A.DETS
+    name = "FCI_File"
+    storage = A.DETS_CRS
+
+    def __init__(self, ham: Hamiltonian, permfile: str | None = None, precision: int = A.FP64,
+                 up: np.ndarray | None = None, down: np.ndarray | None = None, words: int | None = None,
+                 build: bool = True):
+        if permfile is not None:
+            up, down, words = read_determinants(permfile, ham.L)
+        if up is None or down is None:
+            raise ValueError("a determinant file or up/down arrays are needed")
+        self.words = words or (1 if ham.L <= 64 else 2)
+        self.up = np.ascontiguousarray(up, dtype=np.uint64)
+        self.down = np.ascontiguousarray(down, dtype=np.uint64)
+        super().__init__(ham, precision, build)
+
+    def build_ci(self) -> None:
+        out = ctypes.c_void_p()
+        A.check(A.lib().cigpu_build_dets(self._ham.device(), self._dim(), self.words, A.ptr(self.up), A.ptr(self.down),
+                                         self.storage, self.precision, None, ctypes.byref(out)), "cigpu_build_dets")
+        self._mat = SparseMatrix_CRS_Sym(_Handle(out.value, A.lib().cigpu_crs_destroy), self._ham)
+
+    def _dim(self) -> int:
+        return len(self.up) // self.words
+
+    def get_density(self):
+        raise NotImplementedError("RDMs of determinant lists are not built (cigpu_rdm returns ENOTSUP)")
+
+
+class CI_Big(FCI_File):
+    """CI_Big (CIMethod.h:176-189): the determinant list without a stored matrix; every
+    matvec recomputes the elements (FP64)."""
+
+    name = "CI_Big"
+    storage = A.DETS_ONTHEFLY
 
 
 class CIDens:

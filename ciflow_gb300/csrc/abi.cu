@@ -385,6 +385,10 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
 }
 
 void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
+    if (c.onthefly) {
+        dets_mv64(c, x, y, s);
+        return;
+    }
     if (c.precision == CIGPU_MIXED) {
         if (!c.x32.p) c.x32.alloc(std::max<int64_t>(c.dim, 1));
         dev_convert(x, c.x32.p, c.dim, s);
@@ -407,7 +411,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
 }
 
 void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
-    if (c.precision != CIGPU_MIXED) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
+    if (c.precision != CIGPU_MIXED || c.onthefly) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
     if (c.slots) {
         spmv_slots_f32(c.fp, c.val32.p, x, y, s);
         return;
@@ -474,11 +478,6 @@ int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, boo
 
 using namespace cigpu;
 
-#define CIGPU_TRY try {
-#define CIGPU_CATCH \
-    }               \
-    catch (...) { return status_from_exception(); }
-
 extern "C" {
 
 int cigpu_get_version(void) { return CIGPU_ABI_VERSION; }
@@ -514,7 +513,7 @@ int64_t cigpu_kernel_launches(void) { return g_launches.load(); }
 int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, const double *eri, cigpu_ham **out) {
     if (!out || !h || !eri) return CIGPU_EINVAL;
     *out = nullptr;
-    if (L < 1 || L > kMaxL || nup < 0 || ndown < 0 || nup > L || ndown > L) return CIGPU_EINVAL;
+    if (L < 1 || L > kMaxLDets || nup < 0 || ndown < 0 || nup > L || ndown > L) return CIGPU_EINVAL;
     if (!std::isfinite(econst)) return CIGPU_EINVAL;
     const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
     bool exact = true;
@@ -586,6 +585,7 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
     if (precision != CIGPU_FP64 && precision != CIGPU_MIXED) return CIGPU_EINVAL;
     if (method == CIGPU_DOCI && ham->nup != ham->ndown) return CIGPU_EINVAL;
     if (method == CIGPU_DOCI && ham->nup > 32) return CIGPU_ENOTSUP;
+    if (ham->L > kMaxL) return CIGPU_ENOTSUP;  // 64-bit strings; determinant lists go up to 128 orbitals
     const int64_t dim = method == CIGPU_DOCI ? binom64(ham->L, ham->nup)
                                              : binom64(ham->L, ham->nup) * binom64(ham->L, ham->ndown);
     if (dim < 1 || dim > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
@@ -635,13 +635,14 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
 
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
     if (!crs) return CIGPU_EINVAL;
-    if (layout) *layout = crs->slots ? CIGPU_LAYOUT_SLOTS : CIGPU_LAYOUT_CRS;
-    if (stored) *stored = crs->slots ? slots_count(crs->fp) : crs->nnz_full;
+    if (layout) *layout = crs->onthefly ? CIGPU_LAYOUT_ONTHEFLY : crs->slots ? CIGPU_LAYOUT_SLOTS : CIGPU_LAYOUT_CRS;
+    if (stored) *stored = crs->onthefly ? 0 : crs->slots ? slots_count(crs->fp) : crs->nnz_full;
     return CIGPU_OK;
 }
 
 int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val) {
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
+    if (crs->onthefly) return CIGPU_ENOTSUP;
     if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
@@ -669,6 +670,7 @@ int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double 
 
 int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *val) {
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
+    if (crs->onthefly) return CIGPU_ENOTSUP;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
@@ -740,6 +742,7 @@ int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0
 
 int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *aa, double *ab, double *bb) {
     if (!crs || !c) return CIGPU_EINVAL;
+    if (crs->method == CIGPU_DETS) return CIGPU_ENOTSUP;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
     StreamScope scope(s);

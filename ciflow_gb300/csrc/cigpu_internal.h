@@ -15,7 +15,8 @@ namespace cigpu {
 
 // SparseMatrix_CRS::_zero (SparseMatrix_CRS.cpp:44): |v| <= 1e-14 is not stored.
 constexpr double kZero = 1e-14;
-constexpr int kMaxL = 63;
+constexpr int kMaxL = 63;       // FCI / DOCI spaces (64-bit strings)
+constexpr int kMaxLDets = 128;  // Hamiltonians and determinant lists (two 64-bit words per string)
 
 enum Kind : uint32_t { kSelf = 0, kSingle = 1, kDouble = 2 };
 

@@ -30,6 +30,10 @@ struct cigpu_crs {
     cigpu::DevBuf<float> x32;  // MIXED: FP32 copy of x for the FP64 product from hi + lo
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};
+    // determinant lists (FCI_File / CI_Big)
+    int det_words = 0;              // 64-bit words per spin string: 1 (L <= 64) or 2 (L <= 128)
+    bool onthefly = false;          // CI_Big: no stored matrix, elements recomputed in every matvec
+    cigpu::DevBuf<uint64_t> dets;   // [dim][2 * det_words]: up words, then down words
     double build_seconds = 0;
 
     ~cigpu_crs() {
@@ -49,6 +53,8 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision);
 // RDMs of device vector c (normalised); host outputs as in cigpu_rdm.
 void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s);
 int status_from_exception();
+// y = H x of a determinant list without a stored matrix (every pair rescanned).
+void dets_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s);
 // CIGPU_EINVAL unless h is symmetric and eri 8-fold symmetric (1e-10 relative) and all finite.
 int validate_integrals(int L, const double *h, const double *eri, bool *exact);
 // CIGPU_EINVAL unless U (L x L, row-major) is finite and orthogonal to 1e-10.
@@ -68,3 +74,8 @@ int doci_pair_partials();
 // Dm[j][k] = Gamma_aa(jk,jk) (zero diagonal); device outputs, L x L each.
 void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, double *Pm, double *Dm, cudaStream_t s);
 }  // namespace cigpu
+
+#define CIGPU_TRY try {
+#define CIGPU_CATCH \
+    }               \
+    catch (...) { return status_from_exception(); }

@@ -1,0 +1,530 @@
+// Determinant-list CI: FCI_File and CI_Big (cigpu_build_dets), and the
+// Permutator_File reader (cigpu_dets_read).
+//
+// The reference builds a CI matrix over an arbitrary list of determinants read
+// from a text file (FCI_File::construct_CI_matrix, CIMethod.cpp:890-914): every
+// pair (i, j >= i) of the list goes through get_ham_element (CIMethod.cpp:459-487),
+// which classifies the pair by the popcounts of up1^up2 and down1^down2 and
+// evaluates the Slater-Condon rule (diagonal, one_diff_orbital, two_diff_orbitals;
+// CIMethod.cpp:329-457). CI_Big (CIMethod.cpp:591-609, 928-1144) keeps part of the
+// matrix and recomputes the rest in every matvec.
+//
+// Here the list lives on the device as records of 2W 64-bit words (up string, then
+// down string; W = 1 for L <= 64, W = 2 for L <= 128). One warp owns one row and
+// streams the list through shared memory in tiles; each lane tests one column
+// (popcount of the XORs, <= 2 excitations) and evaluates the element with the
+// reference's summation order, so the values are bit-identical to the reference's.
+// The full symmetric matrix is built row by row (every row scans the whole list;
+// columns come out ascending, the kept set compacted with a warp ballot), so no
+// transpose is needed and the upper triangle is the reference CRS. Storage:
+//   CIGPU_DETS_CRS      the CRS (FP64, or FP32 hi/lo for the mixed method);
+//   CIGPU_DETS_ONTHEFLY nothing but the list: every FP64 matvec rescans all pairs
+//                       and applies the elements as it computes them (CI_Big with
+//                       no stored part), y_i summed in a fixed order per row.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "crs.cuh"
+
+namespace cigpu {
+
+namespace {
+
+constexpr int kDetWarps = 8;   // rows per block (one warp each)
+constexpr int kDetTile = 256;  // determinants per shared-memory tile
+enum DetMode : int { kDetCount = 0, kDetFill64 = 1, kDetFill32 = 2, kDetMatvec = 3 };
+
+struct DetParams {
+    int L, nup, ndown;
+    int64_t n;
+    const uint64_t *dets;  // [n][2W]
+    const double *eri;     // chemist (pq|rs), L^4
+    const double *h;       // L^2
+    const double *diag;    // [n]
+    // count pass
+    uint32_t *row_count, *upper_off;
+    // fill pass
+    const int64_t *row_ptr;
+    uint32_t *col;
+    double *val64;
+    float *val32, *val32lo;
+};
+
+__device__ __forceinline__ double Tm(const DetParams &p, int i, int j) { return p.h[i * p.L + j]; }
+// physics <ij|kl> = chemist (ik|jl)
+__device__ __forceinline__ double Vm(const DetParams &p, int i, int j, int k, int l) {
+    const int64_t L = p.L;
+    return p.eri[((i * L + k) * L + j) * L + l];
+}
+
+// Set bits of `up` in [min(o0,o1), max(o0,o1)) (get_nstacked, CIMethod.cpp:382-396).
+template <int W>
+__device__ __forceinline__ int nstacked(int o0, int o1, const uint64_t *up) {
+    const int lo = min(o0, o1), hi = max(o0, o1);
+    int n = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int b0 = max(lo - 64 * w, 0), b1 = min(hi - 64 * w, 64);
+        if (b1 <= b0) continue;
+        uint64_t m = b1 == 64 ? ~(uint64_t)0 : (((uint64_t)1 << b1) - 1);
+        m &= ~(((uint64_t)1 << b0) - 1);
+        n += __popcll(up[w] & m);
+    }
+    return n;
+}
+
+// Orbitals of s in ascending order (get_orbs); at most `cap` of them.
+template <int W>
+__device__ __forceinline__ int orbitals(const uint64_t *s, int *o, int cap) {
+    int n = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t x = s[w]; x && n < cap; x &= x - 1) o[n++] = 64 * w + __ffsll((long long)x) - 1;
+    return n;
+}
+
+template <int W>
+__device__ __forceinline__ bool has_bit(const uint64_t *s, int o) {
+    return (s[o >> 6] >> (o & 63)) & 1;
+}
+
+// get_diag_cont_one_bitstring (CIMethod.cpp:329-342): sum of T, then of the pair terms
+template <int W>
+__device__ double diag_one(const DetParams &p, const uint64_t *s) {
+    int o[128];
+    const int n = orbitals<W>(s, o, 128);
+    double sum = 0;
+    for (int k = 0; k < n; ++k) sum += Tm(p, o[k], o[k]);
+    for (int k = 0; k + 1 < n; ++k)
+        for (int l = k + 1; l < n; ++l) sum += Vm(p, o[k], o[l], o[k], o[l]) - Vm(p, o[k], o[l], o[l], o[k]);
+    return sum;
+}
+
+// CIMethod::diagonal (CIMethod.cpp:398-407): (up part + down part) + the up-down part
+template <int W>
+__device__ double diagonal(const DetParams &p, const uint64_t *up, const uint64_t *dn) {
+    double tot = diag_one<W>(p, up);
+    tot += diag_one<W>(p, dn);
+    double mix = 0;
+#pragma unroll
+    for (int wu = 0; wu < W; ++wu)
+        for (uint64_t xu = up[wu]; xu; xu &= xu - 1) {
+            const int a = 64 * wu + __ffsll((long long)xu) - 1;
+#pragma unroll
+            for (int wd = 0; wd < W; ++wd)
+                for (uint64_t xd = dn[wd]; xd; xd &= xd - 1) {
+                    const int b = 64 * wd + __ffsll((long long)xd) - 1;
+                    mix += Vm(p, a, b, a, b);
+                }
+        }
+    tot += mix;
+    return tot;
+}
+
+// one_diff_orbital (CIMethod.cpp:409-427); `other` is the opposite-spin string
+template <int W>
+__device__ double one_diff(const DetParams &p, const uint64_t *s1, const uint64_t *s2, const uint64_t *other) {
+    uint64_t x[W], c[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        x[w] = s1[w] ^ s2[w];
+        c[w] = s1[w] & s2[w];
+    }
+    int o[2];
+    orbitals<W>(x, o, 2);
+    double e = Tm(p, o[0], o[1]);
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = c[w]; y; y &= y - 1) {
+            const int z = 64 * w + __ffsll((long long)y) - 1;
+            e += Vm(p, o[0], z, o[1], z) - Vm(p, o[0], z, z, o[1]);
+        }
+    const int diff = nstacked<W>(o[0], o[1], c);
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = other[w]; y; y &= y - 1) {
+            const int z = 64 * w + __ffsll((long long)y) - 1;
+            e += Vm(p, o[0], z, o[1], z);
+        }
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+
+// arrange_order (CIMethod.cpp:353-380): the orbitals occupied in s1 first, each
+// group in ascending order
+template <int W>
+__device__ __forceinline__ void arrange(int *o, int num, const uint64_t *s1) {
+    int r[4];
+    int a = 0, b = num / 2;
+    for (int i = 0; i < num; ++i) {
+        if (has_bit<W>(s1, o[i]))
+            r[a++] = o[i];
+        else
+            r[b++] = o[i];
+    }
+    for (int i = 0; i < num; ++i) o[i] = r[i];
+}
+
+// two_diff_orbitals(s1, s2) (CIMethod.cpp:429-442): same-spin double
+template <int W>
+__device__ double two_diff_same(const DetParams &p, const uint64_t *s1, const uint64_t *s2) {
+    uint64_t x[W], c[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        x[w] = s1[w] ^ s2[w];
+        c[w] = s1[w] & s2[w];
+    }
+    int o[4];
+    orbitals<W>(x, o, 4);
+    arrange<W>(o, 4, s1);
+    const int diff = nstacked<W>(o[0], o[1], c) + nstacked<W>(o[2], o[3], c);
+    double e = Vm(p, o[0], o[1], o[2], o[3]) - Vm(p, o[0], o[1], o[3], o[2]);
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+
+// two_diff_orbitals(u1, u2, d1, d2) (CIMethod.cpp:444-457): alpha-beta double
+template <int W>
+__device__ double two_diff_ab(const DetParams &p, const uint64_t *u1, const uint64_t *u2, const uint64_t *d1,
+                              const uint64_t *d2) {
+    uint64_t xu[W], cu[W], xd[W], cd[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        xu[w] = u1[w] ^ u2[w];
+        cu[w] = u1[w] & u2[w];
+        xd[w] = d1[w] ^ d2[w];
+        cd[w] = d1[w] & d2[w];
+    }
+    int a[2], b[2];
+    orbitals<W>(xu, a, 2);
+    orbitals<W>(xd, b, 2);
+    arrange<W>(a, 2, u1);
+    arrange<W>(b, 2, d1);
+    const int diff = nstacked<W>(a[0], a[1], cu) + nstacked<W>(b[0], b[1], cd);
+    double e = Vm(p, a[0], b[0], a[1], b[1]);
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+
+// get_ham_element (CIMethod.cpp:459-487), the off-diagonal cases
+template <int W>
+__device__ __forceinline__ double element(const DetParams &p, const uint64_t *u1, const uint64_t *d1,
+                                          const uint64_t *u2, const uint64_t *d2, int nu, int nd) {
+    if (nd > 4 || nu > 4) return 0.0;
+    if (nu == 4 && nd == 0) return two_diff_same<W>(p, u1, u2);
+    if (nu == 2) {
+        if (nd == 0) return one_diff<W>(p, u1, u2, d1);
+        if (nd == 2) return two_diff_ab<W>(p, u1, u2, d1, d2);
+        return 0.0;
+    }
+    if (nd == 4 && nu == 0) return two_diff_same<W>(p, d1, d2);
+    if (nd == 2 && nu == 0) return one_diff<W>(p, d1, d2, u1);
+    return 0.0;  // nu == nd == 0 is the diagonal, handled by the caller
+}
+
+template <int W>
+__global__ void k_dets_diag(DetParams p, double *diag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < p.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t *d = p.dets + i * 2 * W;
+        diag[i] = diagonal<W>(p, d, d + W);
+    }
+}
+
+template <int W, int MODE>
+__global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const double *__restrict__ x,
+                                                              double *__restrict__ y) {
+    __shared__ uint64_t tile[kDetTile * 2 * W];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (int64_t r0 = (int64_t)blockIdx.x * kDetWarps; r0 < p.n; r0 += (int64_t)gridDim.x * kDetWarps) {
+        const int64_t i = r0 + warp;
+        const bool active = i < p.n;
+        uint64_t ui[W], di[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            ui[w] = active ? p.dets[i * 2 * W + w] : 0;
+            di[w] = active ? p.dets[i * 2 * W + W + w] : 0;
+        }
+        uint32_t cnt = 0, lower = 0;
+        int64_t out = (MODE == kDetFill64 || MODE == kDetFill32) && active ? p.row_ptr[i] : 0;
+        double acc = 0;
+        for (int64_t base = 0; base < p.n; base += kDetTile) {
+            const int tn = (int)(p.n - base < kDetTile ? p.n - base : kDetTile);
+            __syncthreads();
+            for (int t = threadIdx.x; t < tn * 2 * W; t += blockDim.x) tile[t] = p.dets[base * 2 * W + t];
+            __syncthreads();
+            if (!active) continue;
+            for (int jj0 = 0; jj0 < tn; jj0 += 32) {
+                const int jj = jj0 + lane;
+                const int64_t j = base + jj;
+                double v = 0;
+                bool keep = false;
+                if (jj < tn) {
+                    const uint64_t *uj = tile + jj * 2 * W, *dj = uj + W;
+                    int nu = 0, nd = 0;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        nu += __popcll(ui[w] ^ uj[w]);
+                        nd += __popcll(di[w] ^ dj[w]);
+                    }
+                    if (nu + nd <= 4) {
+                        v = (j == i) ? p.diag[i] : element<W>(p, ui, di, uj, dj, nu, nd);
+                        keep = fabs(v) > kZero;  // SparseMatrix_CRS::PushToRow's drop threshold
+                    }
+                }
+                if (MODE == kDetCount) {
+                    cnt += keep;
+                    lower += keep && j < i;
+                } else if (MODE == kDetMatvec) {
+                    if (keep) acc = fma(v, x[j], acc);
+                } else {
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const int64_t pos = out + __popc(m & below);
+                        p.col[pos] = (uint32_t)j;
+                        if (MODE == kDetFill64) {
+                            p.val64[pos] = v;
+                        } else {
+                            split_fp32(v, p.val32[pos], p.val32lo[pos]);
+                        }
+                    }
+                    out += __popc(m);
+                }
+            }
+        }
+        if (!active) continue;
+        if (MODE == kDetCount) {
+            for (int o = 16; o > 0; o >>= 1) {
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+                lower += __shfl_xor_sync(0xffffffffu, lower, o);
+            }
+            if (lane == 0) {
+                p.row_count[i] = cnt;
+                p.upper_off[i] = lower;
+            }
+        } else if (MODE == kDetMatvec) {
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) y[i] = acc;
+        }
+    }
+}
+
+__global__ void k_sum_u32(const uint32_t *a, int64_t n, unsigned long long *out) {
+    unsigned long long s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);  // integer sum: exact in any order
+}
+
+int rows_grid(int64_t n) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + kDetWarps - 1) / kDetWarps, (int64_t)sm_count() * 16));
+}
+
+template <int W, int MODE>
+void launch_rows(const DetParams &p, const double *x, double *y, cudaStream_t s) {
+    k_dets_rows<W, MODE><<<rows_grid(p.n), 32 * kDetWarps, 0, s>>>(p, x, y);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+template <int MODE>
+void rows(const DetParams &p, int W, const double *x, double *y, cudaStream_t s) {
+    if (W == 1)
+        launch_rows<1, MODE>(p, x, y, s);
+    else
+        launch_rows<2, MODE>(p, x, y, s);
+}
+
+DetParams params_of(const cigpu_crs &c) {
+    DetParams p{};
+    p.L = c.L;
+    p.nup = c.nup;
+    p.ndown = c.ndown;
+    p.n = c.dim;
+    p.dets = c.dets.p;
+    p.eri = c.ham->d_eri.p;
+    p.h = c.ham->d_h.p;
+    p.diag = c.diag.p;
+    return p;
+}
+
+// one line of a determinant file: "<up bits>|<down bits>", most significant orbital first
+bool parse_line(const std::string &line, int words, uint64_t *up, uint64_t *down, int *nbits) {
+    const size_t bar = line.find('|');
+    if (bar == std::string::npos) return false;
+    auto parse = [&](const std::string &s, uint64_t *out) {
+        for (int w = 0; w < words; ++w) out[w] = 0;
+        int bit = 0;
+        for (size_t k = s.size(); k-- > 0;) {
+            const char ch = s[k];
+            if (ch == '0' || ch == '1') {
+                if (bit >= 64 * words) return -1;
+                if (ch == '1') out[bit >> 6] |= (uint64_t)1 << (bit & 63);
+                ++bit;
+            } else if (ch != ' ' && ch != '\t' && ch != '\r') {
+                return -1;
+            }
+        }
+        return bit;
+    };
+    const int a = parse(line.substr(0, bar), up), b = parse(line.substr(bar + 1), down);
+    if (a <= 0 || b <= 0) return false;
+    *nbits = std::max(a, b);
+    return true;
+}
+
+}  // namespace
+
+void dets_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
+    DetParams p = params_of(c);
+    rows<kDetMatvec>(p, c.det_words, x, y, s);
+}
+
+}  // namespace cigpu
+
+using namespace cigpu;
+
+extern "C" {
+
+int cigpu_dets_read(const char *path, int words, int64_t capacity, uint64_t *up, uint64_t *down, int64_t *ndet,
+                    int *max_orbitals) {
+    if (!path || !ndet || (words != 1 && words != 2) || capacity < 0) return CIGPU_EINVAL;
+    std::ifstream f(path);
+    if (!f.is_open()) return CIGPU_ENOTFOUND;
+    std::string line;
+    int64_t n = 0;
+    int maxb = 0;
+    uint64_t u[2], d[2];
+    while (std::getline(f, line)) {
+        if (line.find('#') != std::string::npos) continue;  // Permutator_File::read_file skips comment lines
+        if (line.find_first_not_of(" \t\r") == std::string::npos) continue;
+        int nb = 0;
+        if (!parse_line(line, words, u, d, &nb)) return CIGPU_EINVAL;
+        maxb = std::max(maxb, nb);
+        if (up && down && n < capacity) {
+            for (int w = 0; w < words; ++w) {
+                up[n * words + w] = u[w];
+                down[n * words + w] = d[w];
+            }
+        }
+        ++n;
+    }
+    *ndet = n;
+    if (max_orbitals) *max_orbitals = maxb;
+    return (up && down && n > capacity) ? CIGPU_ENOMEM : CIGPU_OK;
+}
+
+int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
+                     int precision, cigpu_stream stream, cigpu_crs **out) {
+    if (!ham || !up || !down || !out) return CIGPU_EINVAL;
+    *out = nullptr;
+    if (ndet < 1 || ndet > (int64_t)UINT32_MAX || (words != 1 && words != 2)) return CIGPU_EINVAL;
+    if (storage != CIGPU_DETS_CRS && storage != CIGPU_DETS_ONTHEFLY) return CIGPU_EINVAL;
+    if (precision != CIGPU_FP64 && precision != CIGPU_MIXED) return CIGPU_EINVAL;
+    if (storage == CIGPU_DETS_ONTHEFLY && precision != CIGPU_FP64) return CIGPU_ENOTSUP;
+    const int W = ham->L <= 64 ? 1 : 2;
+    if (words < W) return CIGPU_EINVAL;
+    // every determinant: nup / ndown electrons inside the L orbitals (the reference
+    // takes the counts from the Hamiltonian and assumes them)
+    std::vector<uint64_t> rec((size_t)ndet * 2 * W, 0);
+    for (int64_t i = 0; i < ndet; ++i) {
+        int cu = 0, cd = 0;
+        for (int w = 0; w < words; ++w) {
+            const uint64_t u = up[i * words + w], d = down[i * words + w];
+            const int lo = 64 * w;
+            const uint64_t valid = ham->L - lo >= 64 ? ~(uint64_t)0 : (ham->L - lo <= 0 ? 0 : (((uint64_t)1 << (ham->L - lo)) - 1));
+            if ((u & ~valid) || (d & ~valid)) return CIGPU_EINVAL;
+            cu += __builtin_popcountll(u);
+            cd += __builtin_popcountll(d);
+            if (w < W) {
+                rec[(size_t)i * 2 * W + w] = u;
+                rec[(size_t)i * 2 * W + W + w] = d;
+            }
+        }
+        if (cu != ham->nup || cd != ham->ndown) return CIGPU_EINVAL;
+    }
+    CIGPU_TRY
+    std::unique_ptr<cigpu_crs> c(new cigpu_crs);
+    c->ham = ham;
+    c->method = CIGPU_DETS;
+    c->precision = precision;
+    c->L = ham->L;
+    c->nup = ham->nup;
+    c->ndown = ham->ndown;
+    c->dim = ndet;
+    c->det_words = W;
+    c->onthefly = storage == CIGPU_DETS_ONTHEFLY;
+    if (stream) {
+        c->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        CIGPU_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    cudaStream_t s = c->stream;
+    StreamScope scope(s);
+    const auto t0 = std::chrono::steady_clock::now();
+    c->dets.alloc(rec.size());
+    CIGPU_CUDA(cudaMemcpyAsync(c->dets.p, rec.data(), rec.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    c->diag.alloc(ndet);
+    DetParams p = params_of(*c);
+    {
+        const int g = (int)std::max<int64_t>(1, std::min<int64_t>((ndet + 255) / 256, (int64_t)sm_count() * 8));
+        if (W == 1)
+            k_dets_diag<1><<<g, 256, 0, s>>>(p, c->diag.p);
+        else
+            k_dets_diag<2><<<g, 256, 0, s>>>(p, c->diag.p);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+    }
+    if (!c->onthefly) {
+        DevBuf<uint32_t> count(ndet);
+        c->upper_off.alloc(ndet);
+        c->row_ptr.alloc(ndet + 1);
+        p.row_count = count.p;
+        p.upper_off = c->upper_off.p;
+        rows<kDetCount>(p, W, nullptr, nullptr, s);
+        exclusive_scan_u32(count.p, c->row_ptr.p, ndet, s);
+        DevBuf<unsigned long long> lower(1);
+        CIGPU_CUDA(cudaMemsetAsync(lower.p, 0, sizeof(unsigned long long), s));
+        k_sum_u32<<<(int)std::min<int64_t>((ndet + 255) / 256, 1024), 256, 0, s>>>(c->upper_off.p, ndet, lower.p);
+        CIGPU_CUDA(cudaGetLastError());
+        count_launch();
+        int64_t nnz = 0;
+        unsigned long long nlow = 0;
+        CIGPU_CUDA(cudaMemcpyAsync(&nnz, c->row_ptr.p + ndet, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(&nlow, lower.p, sizeof(nlow), cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+        c->nnz_full = nnz;
+        c->nnz_upper = nnz - (int64_t)nlow;
+        c->col.alloc(std::max<int64_t>(nnz, 1));
+        p.row_ptr = c->row_ptr.p;
+        p.col = c->col.p;
+        if (precision == CIGPU_FP64) {
+            c->val64.alloc(std::max<int64_t>(nnz, 1));
+            p.val64 = c->val64.p;
+            rows<kDetFill64>(p, W, nullptr, nullptr, s);
+        } else {
+            c->val32.alloc(std::max<int64_t>(nnz, 1));
+            c->val32lo.alloc(std::max<int64_t>(nnz, 1));
+            p.val32 = c->val32.p;
+            p.val32lo = c->val32lo.p;
+            rows<kDetFill32>(p, W, nullptr, nullptr, s);
+        }
+    }
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+    c->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *out = c.release();
+    return CIGPU_OK;
+    CIGPU_CATCH
+}
+
+}  // extern "C"

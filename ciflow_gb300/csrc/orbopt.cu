@@ -778,6 +778,7 @@ int cigpu_orbopt_create(const cigpu_ham *ham, const cigpu_orbopt_config *cfg, ci
     if (!(cfg->tol > 0)) return CIGPU_EINVAL;
     if (cfg->method == CIGPU_DOCI && (ham->nup != ham->ndown || ham->L > 32)) return CIGPU_ENOTSUP;
     if (cfg->method == CIGPU_FCI && !ham->host_valid) return CIGPU_EINVAL;
+    if (ham->L > kMaxL) return CIGPU_ENOTSUP;
     const int64_t dim = cfg->method == CIGPU_DOCI ? binom_i64(ham->L, ham->nup)
                                                   : binom_i64(ham->L, ham->nup) * binom_i64(ham->L, ham->ndown);
     if (dim < 1 || dim > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;

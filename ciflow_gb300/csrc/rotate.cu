@@ -219,6 +219,7 @@ int cigpu_ham_export(const cigpu_ham *ham, double *h, double *eri) {
 int cigpu_ham_rotate(const cigpu_ham *base, const double *U, cigpu_stream stream, cigpu_ham **out) {
     if (!base || !U || !out) return CIGPU_EINVAL;
     *out = nullptr;
+    if (base->L > kMaxL) return CIGPU_ENOTSUP;  // U is staged in shared memory
     if (validate_rotation(base->L, U) != CIGPU_OK) return CIGPU_EINVAL;  // orthogonal to 1e-10
     try {
         cudaStream_t s = static_cast<cudaStream_t>(stream);

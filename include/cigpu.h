@@ -49,7 +49,8 @@ enum cigpu_status {
     CIGPU_ENOTFOUND = 202  /* unknown request id */
 };
 
-enum cigpu_method { CIGPU_FCI = 0, CIGPU_DOCI = 1 };
+/* CIGPU_DETS: a CRS made by cigpu_build_dets from a determinant list (FCI_File / CI_Big). */
+enum cigpu_method { CIGPU_FCI = 0, CIGPU_DOCI = 1, CIGPU_DETS = 2 };
 /* FP64: FP64 CRS values, FP64 Krylov vectors, FP64 matvec.
  * MIXED: FP32 CRS values and FP32 Krylov vectors with FP32 row accumulation;
  *        FP64 orthogonalisation coefficients, recurrence, projected eigensolve,
@@ -85,6 +86,7 @@ int64_t cigpu_kernel_launches(void);
  * are copied to the device as dense tables. ---- */
 int cigpu_ham_create(int L, int nup, int ndown, double econst, const double *h, const double *eri,
                      cigpu_ham **out);
+/* (L <= 128; FCI/DOCI builds, rotations and the server need L <= 63, determinant lists take up to 128.) */
 int cigpu_ham_destroy(cigpu_ham *ham);
 /* ---- orbital rotation: replaces OrbitalTransform::fillHamCI and rotate_old_to_new
  * (OrbitalTransform.cpp:64-170). Creates a new Hamiltonian with the integrals of
@@ -115,7 +117,7 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
  * structural slot of every row (zeros included, rows padded to tiles of 64 beta
  * strings), stored = that slot count; columns are regenerated from the string
  * tables. */
-enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1 };
+enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1, CIGPU_LAYOUT_ONTHEFLY = 2 };
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored);
 /* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
  * SparseMatrix_CRS.h:107-111): row[dim+1], col[nnz_upper], val[nnz_upper]. Host buffers. */
@@ -234,6 +236,30 @@ typedef struct {
 } cigpu_batch_stats;
 int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_dim, double *e0,
                       cigpu_solve_info *info, int *status, cigpu_batch_stats *stats);
+
+/* ---- determinant lists: replaces FCI_File (CIMethod.h:164-173, CIMethod.cpp:890-919)
+ * and CI_Big (CIMethod.h:176-189, CIMethod.cpp:591-609, 928-1144) with
+ * get_ham_element (CIMethod.cpp:459-487): a CI matrix over an arbitrary list of
+ * determinants in list order. up/down: ndet strings of `words` 64-bit words each
+ * (word 0 holds orbitals 0..63; words = 2 for L up to 128), each with the
+ * Hamiltonian's nup / ndown electrons (CIGPU_EINVAL otherwise). storage:
+ * CIGPU_DETS_CRS builds the CRS (its upper triangle is the reference's
+ * SparseMatrix_CRS_Sym for the list, precision FP64 or MIXED);
+ * CIGPU_DETS_ONTHEFLY stores no matrix (FP64 only): every matvec recomputes the
+ * elements from the list, as CI_Big does for the part it does not keep. The CRS
+ * handle works with cigpu_solve, cigpu_mvprod and (CRS storage) the exports;
+ * cigpu_rdm returns CIGPU_ENOTSUP for it. ---- */
+enum { CIGPU_DETS_CRS = 0, CIGPU_DETS_ONTHEFLY = 1 };
+int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
+                     int precision, cigpu_stream stream, cigpu_crs **out);
+/* Permutator_File::read_file (Permutator.cpp:179-224): a determinant file with one
+ * "<up>|<down>" line per determinant (binary strings, orbital 0 rightmost; lines
+ * holding '#' are skipped). Call with up/down NULL to count: *ndet = number of
+ * determinants, *max_orbitals = longest string; then with arrays of capacity*words
+ * words each. CIGPU_ENOTFOUND if the file cannot be opened, CIGPU_EINVAL on a
+ * malformed line or a string longer than 64*words bits. Host code. */
+int cigpu_dets_read(const char *path, int words, int64_t capacity, uint64_t *up, uint64_t *down, int64_t *ndet,
+                    int *max_orbitals);
 
 /* Device memory a request of this shape needs (bytes), as used by admission. */
 int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes);

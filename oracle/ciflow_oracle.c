@@ -861,3 +861,150 @@ void orc_sym_mvprod_rows(int64_t r0, int64_t nrows, const int64_t *row, const ui
         }
     }
 }
+
+/* ---- determinant lists: FCI_File::construct_CI_matrix (CIMethod.cpp:890-914) with
+ *      get_ham_element (CIMethod.cpp:459-487), strings of up to 128 orbitals ---- */
+typedef unsigned __int128 wide_t;
+
+static inline int popc_w(wide_t x) {
+    return __builtin_popcountll((uint64_t)x) + __builtin_popcountll((uint64_t)(x >> 64));
+}
+static inline int ctz_w(wide_t x) {
+    const uint64_t lo = (uint64_t)x;
+    return lo ? __builtin_ctzll(lo) : 64 + __builtin_ctzll((uint64_t)(x >> 64));
+}
+static inline int get_orbs_w(wide_t s, int *o) {
+    int n = 0;
+    while (s) {
+        o[n++] = ctz_w(s);
+        s &= s - 1;
+    }
+    return n;
+}
+static inline int nstacked_w(int o0, int o1, wide_t up) {
+    int lo = o0 < o1 ? o0 : o1, hi = o0 < o1 ? o1 : o0;
+    int sum = 0;
+    for (int i = lo; i < hi; ++i)
+        if ((up >> i) & 1) ++sum;
+    return sum;
+}
+static inline void arrange_w(int *orbs, int num, wide_t up1) {
+    int re[4];
+    int a = 0, b = (num == 4) ? 2 : 1;
+    for (int i = 0; i < num; ++i) {
+        if ((up1 >> orbs[i]) & 1)
+            re[a++] = orbs[i];
+        else
+            re[b++] = orbs[i];
+    }
+    for (int i = 0; i < num; ++i) orbs[i] = re[i];
+}
+static double diag_one_w(const ham_t *H, wide_t s) {
+    int o[128];
+    const int n = get_orbs_w(s, o);
+    return diag_one(H, o, n);
+}
+static double diagonal_w(const ham_t *H, wide_t up, wide_t dn) {
+    int ou[128] = {0}, od[128] = {0};
+    const int nu = get_orbs_w(up, ou), nd = get_orbs_w(dn, od);
+    double tot = diag_one(H, ou, nu);
+    tot += diag_one(H, od, nd);
+    double mix = 0;
+    for (int k = 0; k < nu; ++k)
+        for (int l = 0; l < nd; ++l) mix += V(H, ou[k], od[l], ou[k], od[l]);
+    tot += mix;
+    (void)diag_one_w;
+    return tot;
+}
+static double one_diff_w(const ham_t *H, wide_t s1, wide_t s2, wide_t other) {
+    int orbs[128], com[128], oth[128];
+    get_orbs_w(s1 ^ s2, orbs);
+    double e = T(H, orbs[0], orbs[1]);
+    const int nc = get_orbs_w(s1 & s2, com);
+    for (int z = 0; z < nc; ++z)
+        e += V(H, orbs[0], com[z], orbs[1], com[z]) - V(H, orbs[0], com[z], com[z], orbs[1]);
+    const int diff = nstacked_w(orbs[0], orbs[1], s1 & s2);
+    const int no = get_orbs_w(other, oth);
+    for (int z = 0; z < no; ++z) e += V(H, orbs[0], oth[z], orbs[1], oth[z]);
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+static double two_same_w(const ham_t *H, wide_t s1, wide_t s2) {
+    int o[128];
+    get_orbs_w(s1 ^ s2, o);
+    arrange_w(o, 4, s1);
+    const wide_t c = s1 & s2;
+    const int diff = nstacked_w(o[0], o[1], c) + nstacked_w(o[2], o[3], c);
+    double e = V(H, o[0], o[1], o[2], o[3]) - V(H, o[0], o[1], o[3], o[2]);
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+static double two_ab_w(const ham_t *H, wide_t u1, wide_t u2, wide_t d1, wide_t d2) {
+    int a[128], b[128];
+    get_orbs_w(u1 ^ u2, a);
+    get_orbs_w(d1 ^ d2, b);
+    arrange_w(a, 2, u1);
+    arrange_w(b, 2, d1);
+    const int diff = nstacked_w(a[0], a[1], u1 & u2) + nstacked_w(b[0], b[1], d1 & d2);
+    double e = V(H, a[0], b[0], a[1], b[1]);
+    if (diff % 2 != 0) e *= -1;
+    return e;
+}
+static double ham_element_w(const ham_t *H, wide_t up1, wide_t down1, wide_t up2, wide_t down2) {
+    const int nu = popc_w(up1 ^ up2), nd = popc_w(down1 ^ down2);
+    if (nd > 4 || nu > 4) return 0;
+    if (nu == 4 && nd == 0) return two_same_w(H, up1, up2);
+    if (nu == 2) {
+        if (nd == 0) return one_diff_w(H, up1, up2, down1);
+        if (nd == 2) return two_ab_w(H, up1, up2, down1, down2);
+        return 0;
+    }
+    if (nd == 4 && nu == 0) return two_same_w(H, down1, down2);
+    if (nd == 2 && nu == 0) return one_diff_w(H, down1, down2, up1);
+    if (nd == 0 && nu == 0) return diagonal_w(H, up1, down1);
+    return 0;
+}
+
+int orc_build_dets(int L, int nup, int ndown, const double *h, const double *eri, int64_t ndet, int words,
+                   const uint64_t *up, const uint64_t *down, int64_t *row, uint32_t *col, double *val) {
+    if (L < 1 || L > 128 || ndet < 1 || (words != 1 && words != 2)) return 1;
+    ham_t H = {L, nup, ndown, h, eri, (size_t)L, (size_t)L * L, (size_t)L * L * L};
+    wide_t *us = (wide_t *)malloc((size_t)ndet * sizeof(wide_t));
+    wide_t *ds = (wide_t *)malloc((size_t)ndet * sizeof(wide_t));
+    for (int64_t i = 0; i < ndet; ++i) {
+        us[i] = up[i * words];
+        ds[i] = down[i * words];
+        if (words == 2) {
+            us[i] |= (wide_t)up[i * words + 1] << 64;
+            ds[i] |= (wide_t)down[i * words + 1] << 64;
+        }
+    }
+    const int fill = (col != NULL);
+#pragma omp parallel
+    {
+        rowbuf_t r;
+        r.col = (uint32_t *)malloc((size_t)ndet * sizeof(uint32_t));
+        r.val = (double *)malloc((size_t)ndet * sizeof(double));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t i = 0; i < ndet; ++i) {
+            r.n = 0;
+            for (int64_t j = i; j < ndet; ++j) push_row(&r, (uint32_t)j, ham_element_w(&H, us[i], ds[i], us[j], ds[j]), 1);
+            if (!fill) {
+                row[i + 1] = r.n;
+            } else {
+                memcpy(col + row[i], r.col, (size_t)r.n * sizeof(uint32_t));
+                memcpy(val + row[i], r.val, (size_t)r.n * sizeof(double));
+            }
+        }
+        free(r.col);
+        free(r.val);
+    }
+    if (!fill) {
+        row[0] = 0;
+        for (int64_t i = 0; i < ndet; ++i) row[i + 1] += row[i];
+    }
+    free(us);
+    free(ds);
+    return 0;
+}
+

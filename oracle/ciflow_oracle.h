@@ -6,7 +6,8 @@
  *
  * Integrals: h is L*L row-major; eri is chemist (pq|rs), L^4 row-major. The
  * physics element the reference uses is V(i,j,k,l) = <ij|kl> = (ik|jl).
- * Bitstrings are 64-bit, so L <= 63. nup must equal ndown for DOCI.
+ * Bitstrings are 64-bit, so L <= 63 (determinant lists: 128-bit, L <= 128).
+ * nup must equal ndown for DOCI.
  */
 #ifndef CIGPU_ORACLE_H
 #define CIGPU_ORACLE_H
@@ -50,6 +51,12 @@ int orc_rdm_pairs(int method, int L, int nup, int ndown, const double *c, double
                   double *bb);
 int orc_rdm_excitations(int method, int L, int nup, int ndown, const double *c, double *rdm1, double *aa,
                         double *ab, double *bb);
+
+/* Upper-triangle CRS of a determinant list in list order (FCI_File::construct_CI_matrix
+ * with get_ham_element): strings of `words` 64-bit words (L <= 128). Two calls as
+ * orc_build_upper. */
+int orc_build_dets(int L, int nup, int ndown, const double *h, const double *eri, int64_t ndet, int words,
+                   const uint64_t *up, const uint64_t *down, int64_t *row, uint32_t *col, double *val);
 
 /* Bounded samples for the CPU baseline: rows [r0, r1) of the upper CRS (see the .c file). */
 int64_t orc_build_rows(int method, int L, int nup, int ndown, const double *h, const double *eri, int64_t r0,

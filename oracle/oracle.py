@@ -92,6 +92,10 @@ def ref():
         lib.ref_ci_mvprod.argtypes = [_P] * 3
         lib.ref_ci_density.restype = ctypes.c_double
         lib.ref_ci_density.argtypes = [_P, ctypes.c_double] + [_P] * 5
+        lib.ref_file_ci_create.restype = _P
+        lib.ref_file_ci_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           _P, _P, ctypes.c_char_p]
+        lib.ref_file_dets.argtypes = [_P, _P, _P]
         lib.ref_jacobi.restype = ctypes.c_int
         lib.ref_jacobi.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [_P] * 2 + [ctypes.c_int] + [_P] * 6
         lib.ref_doci_scan.restype = ctypes.c_int
@@ -267,10 +271,18 @@ def ref_read_file(filename: str):
 class RefCI:
     """A reference FCI/DOCI object (CRS built by the reference constructor)."""
 
-    def __init__(self, method: int, ints=None, filename: str | None = None):
+    def __init__(self, method: int, ints=None, filename: str | None = None, det_file: str | None = None):
         lib = ref()
         self.lib = lib
-        if filename is not None:
+        if det_file is not None:  # FCI_File over a determinant list
+            if filename is not None:
+                self.h = lib.ref_file_ci_create(filename.encode(), 0, 0, 0, 0.0, None, None, det_file.encode())
+            else:
+                hh = np.ascontiguousarray(ints.h)
+                ee = np.ascontiguousarray(ints.eri)
+                self.h = lib.ref_file_ci_create(None, ints.L, ints.nup, ints.ndown, ints.econst, _ptr(hh), _ptr(ee),
+                                                det_file.encode())
+        elif filename is not None:
             self.h = lib.ref_ci_create(method, filename.encode(), 0, 0, 0, 0.0, None, None)
         else:
             hh = np.ascontiguousarray(ints.h)
@@ -302,6 +314,14 @@ class RefCI:
         c = np.ascontiguousarray(c, dtype=np.float64)
         ed = self.lib.ref_ci_density(self.h, e, _ptr(c), _ptr(r1), _ptr(aa), _ptr(ab), _ptr(bb))
         return (r1, aa, ab, bb), ed
+
+    def dets(self):
+        """(up, down) uint64 arrays of a FCI_File object's determinant list."""
+        n = self.lib.ref_ci_dim(self.h)
+        up = np.zeros(n, np.uint64)
+        dn = np.zeros(n, np.uint64)
+        self.lib.ref_file_dets(self.h, _ptr(up), _ptr(dn))
+        return up, dn
 
     def doci_scan(self, L: int, e: float, c: np.ndarray, fixed=()):
         """DensDOCI::find_min_angle / calc_rotate for every pair k < l, with the
@@ -347,3 +367,25 @@ def ref_jacobi(ints, rotations):
     lib.ref_jacobi(L, ints.nup, ints.ndown, ints.econst, _ptr(hh), _ptr(ee), len(k), _ptr(k), _ptr(l), _ptr(th),
                    _ptr(h), _ptr(eri), _ptr(U))
     return h, eri, U
+
+
+def build_dets(ints, up: np.ndarray, down: np.ndarray, words: int = 1) -> UpperCRS:
+    """The oracle's FCI_File CRS of a determinant list (strings of `words` 64-bit words)."""
+    lib = port()
+    lib.orc_build_dets.restype = ctypes.c_int
+    lib.orc_build_dets.argtypes = [ctypes.c_int] * 3 + [_P, _P, ctypes.c_int64, ctypes.c_int] + [_P] * 5
+    n = len(up) // words
+    h = np.ascontiguousarray(ints.h, dtype=np.float64)
+    eri = np.ascontiguousarray(ints.eri, dtype=np.float64)
+    up = np.ascontiguousarray(up, dtype=np.uint64)
+    down = np.ascontiguousarray(down, dtype=np.uint64)
+    row = np.zeros(n + 1, np.int64)
+    if lib.orc_build_dets(ints.L, ints.nup, ints.ndown, _ptr(h), _ptr(eri), n, words, _ptr(up), _ptr(down), _ptr(row),
+                          None, None) != 0:
+        raise ValueError("oracle rejected the determinant list")
+    col = np.empty(row[-1], np.uint32)
+    val = np.empty(row[-1], np.float64)
+    lib.orc_build_dets(ints.L, ints.nup, ints.ndown, _ptr(h), _ptr(eri), n, words, _ptr(up), _ptr(down), _ptr(row),
+                       _ptr(col), _ptr(val))
+    return UpperCRS(row, col, val)
+

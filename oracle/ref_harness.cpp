@@ -15,6 +15,7 @@
 //   * install an eigenvector and run CIDens::construct_density
 //     (CIMethod.cpp:161-171, CIDens.cpp:323-334) and read the RDMs through
 //     get_one_rdm/get_two_rdm (CIDens.cpp:166-292);
+//   * build FCI_File from a determinant file and read back its list;
 //   * apply Jacobi rotations with OrbitalTransform::do_jacobi_rotation
 //     (OrbitalTransform.cpp:278-414) and read the rotated integrals and the
 //     accumulated unitary (UnitaryMatrix::get_full_transformation, UnitaryMatrix.cpp:167-183);
@@ -40,6 +41,7 @@
 #include "SparseMatrix_CRS.h"
 #undef protected
 #include "OrbitalTransform.h"
+#include "Permutator.h"
 #include "UnitaryMatrix.h"
 
 namespace {
@@ -164,6 +166,32 @@ double ref_ci_density(void *p, double e, const double *c, double *rdm1, double *
                 for (int s = 0; s < L; ++s)
                     rdm2_ab[(p_ * L + q) * L2 + r_ * L + s] = d->get_two_rdm(1, p_, q, r_, s);
     return d->get_dens_energy();
+}
+
+// FCI_File(ham, det_file) (CIMethod.cpp:890-919): the Hamiltonian from a psi4 text
+// dump (ham_file) or from h/eri, the determinant list read by Permutator_File
+// (Permutator.cpp:179-224); the CRS is built by the constructor. Works with the
+// ref_ci_* accessors above.
+void *ref_file_ci_create(const char *ham_file, int L, int nup, int ndown, double econst, const double *h,
+                         const double *eri, const char *det_file) {
+    RefCI *r = new RefCI;
+    r->method = 2;
+    r->ham = ham_file ? new Hamiltonian(std::string(ham_file)) : make_ham(L, nup, ndown, econst, h, eri);
+    r->cim = new FCI_File(r->ham, std::string(det_file));
+    return r;
+}
+
+// The determinant list of a FCI_File object in list order (64-bit strings).
+void ref_file_dets(void *p, unsigned long long *up, unsigned long long *down) {
+    CIMethod *cim = static_cast<RefCI *>(p)->cim;
+    Permutator *perm = cim->get_perm();
+    const int n = perm->get_dim();
+    TYPE det[2];
+    for (int i = 0; i < n; ++i) {
+        perm->permutate_bit(det, i);
+        up[i] = (unsigned long long)det[0];
+        down[i] = (unsigned long long)det[1];
+    }
 }
 
 // Applies nrot Jacobi rotations in order to the Hamiltonian built from h/eri

@@ -137,11 +137,81 @@ def case_orbopt(name: str):
     print(name, json.dumps(meta))
 
 
+# Determinant-list CI (FCI_File): the reference's own test cases. BeH2 STO-3G with
+# the full 1225-determinant list of tests/data/fci_beh2_sto-3gdeterminants.dat
+# (TestDensity.cpp), Be cc-pVDZ with the 100-determinant GKCI list (TestDetFile.cpp:
+# E0 = -14.5951673370889), and the 70-orbital Be case of Testmp.cpp (E0 =
+# -14.346369472944886), which needs 128-bit strings: the reference build here has
+# 64-bit strings, so for it the pin is the known answer (and the oracle's 128-bit
+# restatement), not the reference CRS. Integrals are stored as their canonical
+# nonzero elements (p>=q, r>=s, pq>=rs) and the one-body upper triangle.
+DETS_CASES = {
+    "beh2": ("beh2_sto3g_1_5.dat", "fci_beh2_sto-3gdeterminants.dat", None),
+    "be_gkci": ("Be_ccpVDZ.dat", "GKCI_Be_cntSp_cc-pVDZ_0100.txt", -14.5951673370889),
+    "be70": ("mpbe5zmatrixelements.dat", "mpbe5zcut70determinants.dat", -14.346369472944886),
+}
+
+
+def sparse_integrals(ints):
+    L = ints.L
+    idx = np.argwhere(ints.eri != 0)
+    p, q, r, s = idx.T
+    keep = (p >= q) & (r >= s) & ((p * L + q) >= (r * L + s))
+    hi = np.argwhere(np.triu(ints.h) != 0)
+    return {"eri_idx": idx[keep].astype(np.uint8), "eri_val": ints.eri[tuple(idx[keep].T)],
+            "h_idx": hi.astype(np.uint8), "h_val": ints.h[tuple(hi.T)]}
+
+
+def read_det_file(path, words):
+    up, down = [], []
+    for line in open(path):
+        if "#" in line or "|" not in line:
+            continue
+        a, b = line.strip().split("|")
+        for s, out in ((a, up), (b, down)):
+            v = int(s, 2)
+            out.extend([(v >> (64 * w)) & ((1 << 64) - 1) for w in range(words)])
+    return np.array(up, np.uint64), np.array(down, np.uint64)
+
+
+def case_dets(name: str):
+    out, meta = {}, {}
+    for tag, (hf, df, known) in DETS_CASES.items():
+        ints = O.ref_read_file(os.path.join(O.REF_ROOT, "tests", "data", hf))
+        words = 1 if ints.L <= 64 else 2
+        up, dn = read_det_file(os.path.join(O.REF_ROOT, "tests", "data", df), words)
+        m_or = O.build_dets(ints, up, dn, words)
+        e_or, _ = O.lowest_eigenpair(m_or)
+        rec = {"L": ints.L, "nup": ints.nup, "ndown": ints.ndown, "econst": ints.econst, "words": words,
+               "dim": m_or.n, "nnz": m_or.nnz, "crs_sha256": crs_sha256(m_or), "e0_oracle": e_or + ints.econst,
+               "source": f"tests/data/{hf} + tests/data/{df}"}
+        if known is not None:
+            rec["e0_known_answer"] = known
+        if words == 1:
+            r = O.RefCI(O.FCI, filename=os.path.join(O.REF_ROOT, "tests", "data", hf),
+                        det_file=os.path.join(O.REF_ROOT, "tests", "data", df))
+            m = r.crs()
+            ru, rd = r.dets()
+            assert np.array_equal(ru, up) and np.array_equal(rd, dn), "reference list differs from the parse"
+            e, _ = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
+            rec.update({"crs_sha256_reference": crs_sha256(m), "e0_reference": e + ints.econst})
+            r.close()
+        meta[tag] = rec
+        out.update({f"{tag}_up": up, f"{tag}_down": dn})
+        out.update({f"{tag}_{k}": v for k, v in sparse_integrals(ints).items()})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta, indent=1))
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt"]
+    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets"]
     for nm in names:
         if nm == "orbopt":
             case_orbopt(nm)
+        elif nm == "dets":
+            case_dets(nm)
         elif nm == "beh2_sto3g":
             case_file(nm, "beh2_sto3g_1_5.dat")
         elif nm == "be_ccpvdz":

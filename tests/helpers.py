@@ -33,3 +33,26 @@ def crs_sha256(row, col, val) -> str:
 
 def integrals(name):
     return config_integrals(name)
+
+
+def dets_case(tag):
+    """A determinant-list golden case (tests/golden/dets.*): (Integrals, up, down, words, meta)."""
+    import json
+    import numpy as np
+    from ciflow_gb300.synthetic import Integrals
+    with open(os.path.join(GOLDEN, "dets.json")) as f:
+        meta = json.load(f)[tag]
+    g = np.load(os.path.join(GOLDEN, "dets.npz"))
+    L = meta["L"]
+    h = np.zeros((L, L))
+    hi, hv = g[f"{tag}_h_idx"].astype(int), g[f"{tag}_h_val"]
+    h[hi[:, 0], hi[:, 1]] = hv
+    h[hi[:, 1], hi[:, 0]] = hv
+    eri = np.zeros((L,) * 4)
+    ei, ev = g[f"{tag}_eri_idx"].astype(int), g[f"{tag}_eri_val"]
+    for p, q, r, s in ((0, 1, 2, 3), (1, 0, 2, 3), (0, 1, 3, 2), (1, 0, 3, 2),
+                       (2, 3, 0, 1), (3, 2, 0, 1), (2, 3, 1, 0), (3, 2, 1, 0)):
+        eri[ei[:, p], ei[:, q], ei[:, r], ei[:, s]] = ev
+    ints = Integrals(L, meta["nup"], meta["ndown"], meta["econst"], h, eri)
+    return ints, g[f"{tag}_up"], g[f"{tag}_down"], meta["words"], meta
+
