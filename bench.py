@@ -46,6 +46,8 @@ def parse_args():
                     help="served-stream requests per form (0 skips the served stream)")
     ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
+    ap.add_argument("--dets-orbitals", type=int, default=32,
+                    help="orbitals of the CISD determinant-list section (0: skip); electrons per spin = L/4")
     ap.add_argument("--orbopt-steps", type=int, default=600,
                     help="simulated-annealing steps of the orbital-optimisation section (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=512,
@@ -392,6 +394,14 @@ def run_cigpu(args, rank: int, world: int, dist):
         barrier()
         orbopt = bench_section(args.orbopt_steps, cpu_steps=20 if (rank == 0 and world == 1) else 0)
 
+    # determinant lists (FCI_File / CI_Big): a CISD list, stored CRS and on-the-fly matvecs
+    dets = None
+    if args.dets_orbitals > 0:
+        from ciflow_gb300.dets_bench import run as run_dets
+        barrier()
+        dets = run_dets(args.dets_orbitals, args.dets_orbitals // 4,
+                        cpu_rows=20000 if (rank == 0 and world == 1) else 0)
+
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
@@ -419,6 +429,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "served": served,
         "batched": batched,
         "orbopt": orbopt,
+        "dets": dets,
         "cpu_baseline": cpu,
     }
     print(json.dumps(out), flush=True)

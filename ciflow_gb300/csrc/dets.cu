@@ -91,6 +91,31 @@ __device__ __forceinline__ int orbitals(const uint64_t *s, int *o, int cap) {
     return n;
 }
 
+// -e when odd, on the sign bit (exact, and off GB300's slow FP64 pipe)
+__device__ __forceinline__ double negate_if(double e, int odd) {
+    return __longlong_as_double(__double_as_longlong(e) ^ ((long long)odd << 63));
+}
+
+// |v| > 1e-14 (SparseMatrix_CRS::PushToRow's drop threshold) as an integer compare of
+// the magnitude bits; the values are finite (the integrals are validated)
+__device__ __forceinline__ bool keep_value(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull) > 0x3D06849B86A12B9Bull;
+}
+
+// Lowest set orbital of x (cleared from x); x is a register array (constant indices).
+template <int W>
+__device__ __forceinline__ int pop_lowest(uint64_t *x) {
+    int o = -1;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        if (o < 0 && x[w]) {
+            o = 64 * w + __ffsll((long long)x[w]) - 1;
+            x[w] &= x[w] - 1;
+        }
+    }
+    return o;
+}
+
 template <int W>
 __device__ __forceinline__ bool has_bit(const uint64_t *s, int o) {
     return (s[o >> 6] >> (o & 63)) & 1;
@@ -131,51 +156,53 @@ __device__ double diagonal(const DetParams &p, const uint64_t *up, const uint64_
 
 // one_diff_orbital (CIMethod.cpp:409-427); `other` is the opposite-spin string
 template <int W>
-__device__ double one_diff(const DetParams &p, const uint64_t *s1, const uint64_t *s2, const uint64_t *other) {
+__device__ __forceinline__ double one_diff(const DetParams &p, const uint64_t *s1, const uint64_t *s2, const uint64_t *other) {
     uint64_t x[W], c[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         x[w] = s1[w] ^ s2[w];
         c[w] = s1[w] & s2[w];
     }
-    int o[2];
-    orbitals<W>(x, o, 2);
-    double e = Tm(p, o[0], o[1]);
+    const int o0 = pop_lowest<W>(x), o1 = pop_lowest<W>(x);
+    double e = Tm(p, o0, o1);
 #pragma unroll
     for (int w = 0; w < W; ++w)
         for (uint64_t y = c[w]; y; y &= y - 1) {
             const int z = 64 * w + __ffsll((long long)y) - 1;
-            e += Vm(p, o[0], z, o[1], z) - Vm(p, o[0], z, z, o[1]);
+            e += Vm(p, o0, z, o1, z) - Vm(p, o0, z, z, o1);
         }
-    const int diff = nstacked<W>(o[0], o[1], c);
+    const int diff = nstacked<W>(o0, o1, c);
 #pragma unroll
     for (int w = 0; w < W; ++w)
         for (uint64_t y = other[w]; y; y &= y - 1) {
             const int z = 64 * w + __ffsll((long long)y) - 1;
-            e += Vm(p, o[0], z, o[1], z);
+            e += Vm(p, o0, z, o1, z);
         }
-    if (diff % 2 != 0) e *= -1;
-    return e;
+    return negate_if(e, diff & 1);
 }
 
-// arrange_order (CIMethod.cpp:353-380): the orbitals occupied in s1 first, each
-// group in ascending order
+// arrange_order (CIMethod.cpp:353-380) for four ascending orbitals of which two are
+// occupied in s1: (a0, a1) those of s1, (b0, b1) the others, each pair ascending.
+// Written with register selects (no indexed local arrays).
 template <int W>
-__device__ __forceinline__ void arrange(int *o, int num, const uint64_t *s1) {
-    int r[4];
-    int a = 0, b = num / 2;
-    for (int i = 0; i < num; ++i) {
-        if (has_bit<W>(s1, o[i]))
-            r[a++] = o[i];
-        else
-            r[b++] = o[i];
+__device__ __forceinline__ void arrange4(const int *o, const uint64_t *s1, int &a0, int &a1, int &b0, int &b1) {
+    int na = 0, nb = 0;
+    a0 = a1 = b0 = b1 = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (has_bit<W>(s1, o[k])) {
+            if (na == 0) a0 = o[k]; else a1 = o[k];
+            ++na;
+        } else {
+            if (nb == 0) b0 = o[k]; else b1 = o[k];
+            ++nb;
+        }
     }
-    for (int i = 0; i < num; ++i) o[i] = r[i];
 }
 
 // two_diff_orbitals(s1, s2) (CIMethod.cpp:429-442): same-spin double
 template <int W>
-__device__ double two_diff_same(const DetParams &p, const uint64_t *s1, const uint64_t *s2) {
+__device__ __forceinline__ double two_diff_same(const DetParams &p, const uint64_t *s1, const uint64_t *s2) {
     uint64_t x[W], c[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) {
@@ -183,17 +210,18 @@ __device__ double two_diff_same(const DetParams &p, const uint64_t *s1, const ui
         c[w] = s1[w] & s2[w];
     }
     int o[4];
-    orbitals<W>(x, o, 4);
-    arrange<W>(o, 4, s1);
-    const int diff = nstacked<W>(o[0], o[1], c) + nstacked<W>(o[2], o[3], c);
-    double e = Vm(p, o[0], o[1], o[2], o[3]) - Vm(p, o[0], o[1], o[3], o[2]);
-    if (diff % 2 != 0) e *= -1;
-    return e;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = pop_lowest<W>(x);
+    int a0, a1, b0, b1;
+    arrange4<W>(o, s1, a0, a1, b0, b1);
+    const int diff = nstacked<W>(a0, a1, c) + nstacked<W>(b0, b1, c);
+    double e = Vm(p, a0, a1, b0, b1) - Vm(p, a0, a1, b1, b0);
+    return negate_if(e, diff & 1);
 }
 
 // two_diff_orbitals(u1, u2, d1, d2) (CIMethod.cpp:444-457): alpha-beta double
 template <int W>
-__device__ double two_diff_ab(const DetParams &p, const uint64_t *u1, const uint64_t *u2, const uint64_t *d1,
+__device__ __forceinline__ double two_diff_ab(const DetParams &p, const uint64_t *u1, const uint64_t *u2, const uint64_t *d1,
                               const uint64_t *d2) {
     uint64_t xu[W], cu[W], xd[W], cd[W];
 #pragma unroll
@@ -203,15 +231,22 @@ __device__ double two_diff_ab(const DetParams &p, const uint64_t *u1, const uint
         xd[w] = d1[w] ^ d2[w];
         cd[w] = d1[w] & d2[w];
     }
-    int a[2], b[2];
-    orbitals<W>(xu, a, 2);
-    orbitals<W>(xd, b, 2);
-    arrange<W>(a, 2, u1);
-    arrange<W>(b, 2, d1);
-    const int diff = nstacked<W>(a[0], a[1], cu) + nstacked<W>(b[0], b[1], cd);
-    double e = Vm(p, a[0], b[0], a[1], b[1]);
-    if (diff % 2 != 0) e *= -1;
-    return e;
+    // arrange_order with two orbitals: the one occupied in the first string first
+    int a0 = pop_lowest<W>(xu), a1 = pop_lowest<W>(xu);
+    if (!has_bit<W>(u1, a0)) {
+        const int t = a0;
+        a0 = a1;
+        a1 = t;
+    }
+    int b0 = pop_lowest<W>(xd), b1 = pop_lowest<W>(xd);
+    if (!has_bit<W>(d1, b0)) {
+        const int t = b0;
+        b0 = b1;
+        b1 = t;
+    }
+    const int diff = nstacked<W>(a0, a1, cu) + nstacked<W>(b0, b1, cd);
+    double e = Vm(p, a0, b0, a1, b1);
+    return negate_if(e, diff & 1);
 }
 
 // get_ham_element (CIMethod.cpp:459-487), the off-diagonal cases
@@ -227,7 +262,7 @@ __device__ __forceinline__ double element(const DetParams &p, const uint64_t *u1
     }
     if (nd == 4 && nu == 0) return two_diff_same<W>(p, d1, d2);
     if (nd == 2 && nu == 0) return one_diff<W>(p, d1, d2, u1);
-    return 0.0;  // nu == nd == 0 is the diagonal, handled by the caller
+    return 0.0;
 }
 
 template <int W>
@@ -276,8 +311,9 @@ __global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const
                         nd += __popcll(di[w] ^ dj[w]);
                     }
                     if (nu + nd <= 4) {
-                        v = (j == i) ? p.diag[i] : element<W>(p, ui, di, uj, dj, nu, nd);
-                        keep = fabs(v) > kZero;  // SparseMatrix_CRS::PushToRow's drop threshold
+                        // the row itself, or a repeat of its determinant in the list, is the diagonal
+                        v = (nu + nd == 0) ? p.diag[i] : element<W>(p, ui, di, uj, dj, nu, nd);
+                        keep = keep_value(v);
                     }
                 }
                 if (MODE == kDetCount) {
