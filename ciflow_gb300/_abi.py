@@ -113,6 +113,10 @@ SIGNATURES = {
     "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
     "cigpu_build_dets": (_I, [_P, _I64, _I, _P, _P, _I, _I, _P, _P]),
     "cigpu_dets_read": (_I, [ctypes.c_char_p, _I, _I64, _P, _P, _P, _P]),
+    "cigpu_ham_read_psi4": (_I, [ctypes.c_char_p, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "cigpu_ham_write_psi4": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P, _D]),
+    "cigpu_write_civec": (_I, [ctypes.c_char_p, _I, _I, _I, _I, _I64, _P, _D, _D, _D, _P, _P, _I, ctypes.c_char_p]),
+    "cigpu_write_rdm": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _P]),
     "cigpu_ham_jacobi": (_I, [_P, _I, _I, _D, _P, _P]),
     "cigpu_doci_pair_scan": (_I, [_P, _P, _P, _P, _P]),
     "cigpu_orbopt_create": (_I, [_P, _P, _P]),

@@ -101,6 +101,31 @@ class Hamiltonian:
         A.check(A.lib().cigpu_ham_export(H._dev.value, A.ptr(H.h), A.ptr(H.eri)), "cigpu_ham_export")
         return H
 
+    @classmethod
+    def read_file(cls, path: str) -> "Hamiltonian":
+        """Hamiltonian(filename) for a psi4 integral text dump (Hamiltonian::read_file,
+        Hamiltonian.cpp:707-885), parsed by the library; point-group labels are read
+        and not used (C1)."""
+        L, na, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ec, hf = ctypes.c_double(), ctypes.c_double()
+        p = path.encode()
+        A.check(A.lib().cigpu_ham_read_psi4(p, ctypes.byref(L), ctypes.byref(na), ctypes.byref(nb), ctypes.byref(ec),
+                                            None, None, None, None), "cigpu_ham_read_psi4")
+        n = L.value
+        h, eri = np.zeros((n, n)), np.zeros((n,) * 4)
+        A.check(A.lib().cigpu_ham_read_psi4(p, ctypes.byref(L), ctypes.byref(na), ctypes.byref(nb), ctypes.byref(ec),
+                                            A.ptr(h), A.ptr(eri), None, ctypes.byref(hf)), "cigpu_ham_read_psi4")
+        H = cls(n, 0, na.value, nb.value, ec.value, h, eri)
+        H.hf_energy = hf.value
+        return H
+
+    def save_file(self, path: str, hf_energy: float = 0.0) -> None:
+        """The psi4 integral text dump (Hamiltonian::save_file's format, C1, 17 digits)."""
+        h = np.ascontiguousarray(self.h)
+        e = np.ascontiguousarray(self.eri)
+        A.check(A.lib().cigpu_ham_write_psi4(path.encode(), self.L, self.nup, self.ndown, self.Econst, A.ptr(h),
+                                             A.ptr(e), hf_energy), "cigpu_ham_write_psi4")
+
     def jacobi(self, k: int, l: int, theta: float) -> "Hamiltonian":
         """The Hamiltonian with orbitals k, l rotated by theta (k' = cos k - sin l,
         l' = sin k + cos l), computed on the device (cigpu_ham_jacobi; the reference's
@@ -282,6 +307,27 @@ class CIMethod:
             return self._eigvec[:, numvec].copy()
         return float(self._eigvec[numstate, numvec])
 
+    # --- output ---
+    def print_ci_vec(self, path: str, threshold: float = -1.0) -> None:
+        """The CI-vector text of the reference's output (print_solutions + print_ci_vec,
+        Output.cpp:135-144, 190-263): coefficients with |c| >= threshold."""
+        c = np.ascontiguousarray(self.get_eigvec())
+        up = getattr(self, "up", None)
+        down = getattr(self, "down", None)
+        name = getattr(self, "list_name", None)
+        A.check(A.lib().cigpu_write_civec(path.encode(), self.method, self.get_l(), self.gNup(), self.gNdown(), len(c),
+                                          A.ptr(c), self.get_ci_energy(), self.get_econst(), threshold, A.ptr(up),
+                                          A.ptr(down), getattr(self, "words", 1),
+                                          name.encode() if name else None), "cigpu_write_civec")
+
+    def print_rdm(self, path: str, twordm: bool = True) -> None:
+        """CIMethod::print_one_rdm / print_two_rdm text (CIMethod.cpp:184-195)."""
+        self.construct_density(0, twordm)
+        one, aa, ab, bb = self._cid.arrays()
+        A.check(A.lib().cigpu_write_rdm(path.encode(), self.get_l(), A.ptr(one), A.ptr(aa) if twordm else None,
+                                        A.ptr(ab) if twordm else None, A.ptr(bb) if twordm else None),
+                "cigpu_write_rdm")
+
     # --- density ---
     def get_density(self):
         raise NotImplementedError
@@ -352,8 +398,14 @@ class FCI_File(CIMethod):
     def __init__(self, ham: Hamiltonian, permfile: str | None = None, precision: int = A.FP64,
                  up: np.ndarray | None = None, down: np.ndarray | None = None, words: int | None = None,
                  build: bool = True):
+        self.list_name = None
         if permfile is not None:
             up, down, words = read_determinants(permfile, ham.L)
+            # Permutator::get_clean_detfile (Permutator.cpp:88-100): the file name without
+            # directory and extension, with the characters _()-./\ removed
+            import os
+            base = os.path.splitext(os.path.basename(permfile))[0]
+            self.list_name = "".join(ch for ch in base if ch not in "_()-./\\")
         if up is None or down is None:
             raise ValueError("a determinant file or up/down arrays are needed")
         self.words = words or (1 if ham.L <= 64 else 2)

@@ -261,6 +261,38 @@ int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up
 int cigpu_dets_read(const char *path, int words, int64_t capacity, uint64_t *up, uint64_t *down, int64_t *ndet,
                     int *max_orbitals);
 
+/* ---- on-disk formats (host code, no GPU needed) ----
+ * cigpu_ham_read_psi4: Hamiltonian::read_file (Hamiltonian.cpp:707-885), the psi4
+ * plugin's integral text dump: call with h == eri == NULL for L, nup, ndown, Econst
+ * (and irreps[L] when given), then with h (L*L) and eri (L^4, chemist (pq|rs)) to
+ * fill them; every listed element sets its symmetry partners, unlisted ones are 0.
+ * Values are parsed as the reference parses them (the text after the indices
+ * without the line's last character). Optional overlap / unitary sections are
+ * skipped. hf_energy (optional) = the "HF Energy" trailer. CIGPU_ENOTFOUND /
+ * CIGPU_EINVAL for a missing or malformed file.
+ * cigpu_ham_write_psi4: Hamiltonian::save_file's format (Hamiltonian.cpp:646-705)
+ * for point group C1, with 17 significant digits (exact round trip; the reference
+ * writes 15) and each two-electron element once (p >= q, r >= s, pq >= rs). */
+int cigpu_ham_read_psi4(const char *path, int *L, int *nup, int *ndown, double *econst, double *h, double *eri,
+                        int *irreps, double *hf_energy);
+int cigpu_ham_write_psi4(const char *path, int L, int nup, int ndown, double econst, const double *h,
+                         const double *eri, double hf_energy);
+/* The CI-vector text of the reference's output (OutputSingleFile::print_solutions +
+ * OutputSFFCI / OutputSFDOCI / OutputSFFCI_File::print_ci_vec, Output.cpp:135-144,
+ * 190-263): e0 (with Econst) and every coefficient with |c| >= threshold, with its
+ * determinant's strings. method: CIGPU_FCI, CIGPU_DOCI (colex order) or CIGPU_DETS
+ * (up/down: the list, `words` 64-bit words per string). Each DOCI line carries its
+ * own pair string (the reference advances the string only on printed lines).
+ * list_name (CIGPU_DETS, optional): the list's name in the header line. */
+int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, int64_t dim, const double *c,
+                      double e0, double econst, double threshold, const uint64_t *up, const uint64_t *down,
+                      int words, const char *list_name);
+/* The RDM text of CIMethod::print_one_rdm / print_two_rdm (CIMethod.cpp:184-195,
+ * CIDens.cpp:978-1026) from arrays laid out as cigpu_rdm fills them; the 2-RDM part
+ * is written when all three 2-RDM arrays are given. */
+int cigpu_write_rdm(const char *path, int L, const double *rdm1, const double *rdm2_aa, const double *rdm2_ab,
+                    const double *rdm2_bb);
+
 /* Device memory a request of this shape needs (bytes), as used by admission. */
 int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, size_t *bytes);
 

@@ -96,6 +96,10 @@ def ref():
         lib.ref_file_ci_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            _P, _P, ctypes.c_char_p]
         lib.ref_file_dets.argtypes = [_P, _P, _P]
+        lib.ref_print_civec.restype = ctypes.c_int
+        lib.ref_print_civec.argtypes = [_P, ctypes.c_double, _P, ctypes.c_double, ctypes.c_char_p]
+        lib.ref_print_rdm.restype = ctypes.c_int
+        lib.ref_print_rdm.argtypes = [_P, ctypes.c_double, _P, ctypes.c_char_p]
         lib.ref_jacobi.restype = ctypes.c_int
         lib.ref_jacobi.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [_P] * 2 + [ctypes.c_int] + [_P] * 6
         lib.ref_doci_scan.restype = ctypes.c_int
@@ -314,6 +318,18 @@ class RefCI:
         c = np.ascontiguousarray(c, dtype=np.float64)
         ed = self.lib.ref_ci_density(self.h, e, _ptr(c), _ptr(r1), _ptr(aa), _ptr(ab), _ptr(bb))
         return (r1, aa, ab, bb), ed
+
+    def print_civec(self, e: float, c: np.ndarray, nauw: float, path: str) -> None:
+        """The reference's CI-vector text block for (e without Econst, c)."""
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        if self.lib.ref_print_civec(self.h, e, _ptr(c), nauw, path.encode()) != 0:
+            raise OSError(path)
+
+    def print_rdm(self, e: float, c: np.ndarray, path: str) -> None:
+        """The reference's RDM text (print_one_rdm + print_two_rdm) for (e, c)."""
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        if self.lib.ref_print_rdm(self.h, e, _ptr(c), path.encode()) != 0:
+            raise OSError(path)
 
     def dets(self):
         """(up, down) uint64 arrays of a FCI_File object's determinant list."""

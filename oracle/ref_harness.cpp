@@ -24,6 +24,7 @@
 //     (LocalMinimizer.cpp:89-118).
 #include <cmath>
 #include <cstring>
+#include <fstream>
 #include <functional>
 #include <iomanip>
 #include <iostream>
@@ -38,6 +39,7 @@
 #include "CIDens.h"
 #include "CIMethod.h"
 #include "Hamiltonian.h"
+#include "Output.h"
 #include "SparseMatrix_CRS.h"
 #undef protected
 #include "OrbitalTransform.h"
@@ -166,6 +168,46 @@ double ref_ci_density(void *p, double e, const double *c, double *rdm1, double *
                 for (int s = 0; s < L; ++s)
                     rdm2_ab[(p_ * L + q) * L2 + r_ * L + s] = d->get_two_rdm(1, p_, q, r_, s);
     return d->get_dens_energy();
+}
+
+// Installs eigenpair (e without Econst, c) as ref_ci_density does.
+static void install(CIMethod *cim, double e, const double *c) {
+    const int dim = cim->get_dim();
+    cim->_eigval = matrix(1, 1);
+    cim->_eigval(0, 0) = e;
+    cim->_eigvec = matrix(dim, 1);
+    for (int i = 0; i < dim; ++i) cim->_eigvec(i, 0) = c[i];
+    cim->_solved = true;
+}
+
+// The CI-vector block of the reference output (OutputSFFCI / OutputSFDOCI /
+// OutputSFFCI_File::print_ci_vec, Output.cpp:190-263) for eigenpair (e, c), written
+// to `path` with the precision the reference's report has there (16).
+int ref_print_civec(void *p, double e, const double *c, double nauw, const char *path) {
+    CIMethod *cim = static_cast<RefCI *>(p)->cim;
+    install(cim, e, c);
+    OutputSingleFile *o = cim->_output.get();
+    o->_file.open(path, std::ios::out);
+    if (!o->_file.is_open()) return -1;
+    o->_file.precision(16);
+    o->print_ci_vec(0, nauw);
+    o->_file.close();
+    return 0;
+}
+
+// The RDM text of CIMethod::print_one_rdm / print_two_rdm (CIMethod.cpp:184-195,
+// CIDens.cpp:978-1026) for eigenpair (e, c), precision 16 as OutputSingleFile::print_rdm.
+int ref_print_rdm(void *p, double e, const double *c, const char *path) {
+    CIMethod *cim = static_cast<RefCI *>(p)->cim;
+    install(cim, e, c);
+    cim->_cid->reset_density();
+    cim->construct_density(0, true);
+    std::ofstream f(path);
+    if (!f.is_open()) return -1;
+    f.precision(16);
+    cim->print_one_rdm(f);
+    cim->print_two_rdm(f);
+    return 0;
 }
 
 // FCI_File(ham, det_file) (CIMethod.cpp:890-919): the Hamiltonian from a psi4 text

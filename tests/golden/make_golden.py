@@ -205,10 +205,48 @@ def case_dets(name: str):
     print(name, json.dumps(meta, indent=1))
 
 
+# Text formats: the reference's own CI-vector blocks (OutputSFFCI / OutputSFDOCI /
+# OutputSFFCI_File::print_ci_vec) and RDM dumps (print_one_rdm / print_two_rdm) for
+# the BeH2 STO-3G eigenvectors stored in beh2_sto3g.npz, written by the reference.
+def case_formats(name: str):
+    import tempfile
+    meta = json.load(open(os.path.join(OUT, "beh2_sto3g.json")))
+    arr = np.load(os.path.join(OUT, "beh2_sto3g.npz"))
+    path = os.path.join(O.REF_ROOT, "tests", "data", "beh2_sto3g_1_5.dat")
+    det = os.path.join(O.REF_ROOT, "tests", "data", "fci_beh2_sto-3gdeterminants.dat")
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for tag, method, nauw in (("fci", O.FCI, 1e-4), ("doci", O.DOCI, -1.0)):
+            r = O.RefCI(method, filename=path)
+            e = meta[tag]["e0"] - meta["econst"]
+            c = arr[f"{tag}_c"]
+            r.print_civec(e, c, nauw, os.path.join(td, "v.txt"))
+            out[f"civec_{tag}"] = open(os.path.join(td, "v.txt")).read()
+            r.print_rdm(e, c, os.path.join(td, "r.txt"))
+            out[f"rdm_{tag}"] = open(os.path.join(td, "r.txt")).read()
+            out[f"nauw_{tag}"] = nauw
+            r.close()
+        # FCI_File over the reference's BeH2 list: its own eigenvector
+        r = O.RefCI(O.FCI, filename=path, det_file=det)
+        m = r.crs()
+        e, c = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
+        r.print_civec(e, c, 1e-4, os.path.join(td, "v.txt"))
+        out["civec_dets"] = open(os.path.join(td, "v.txt")).read()
+        out["nauw_dets"] = 1e-4
+        np.save(os.path.join(OUT, "formats_dets_c.npy"), c)
+        out["e0_dets"] = e + meta["econst"]
+        r.close()
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print(name, {k: (len(v) if isinstance(v, str) else v) for k, v in out.items()})
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets"]
+    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets", "formats"]
     for nm in names:
-        if nm == "orbopt":
+        if nm == "formats":
+            case_formats(nm)
+        elif nm == "orbopt":
             case_orbopt(nm)
         elif nm == "dets":
             case_dets(nm)
