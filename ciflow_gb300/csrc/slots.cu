@@ -42,7 +42,6 @@ namespace {
 constexpr int kSlotThreads = 256;
 constexpr int kRowWarps = kTileRows / 32;                // warps covering the tile's rows
 constexpr int kSplits = kSlotThreads / 32 / kRowWarps;  // quad ranges per row
-constexpr int kQuadsInFlight = 2;  // 16-byte value loads in flight per lane (4 was slower at L=12)
 
 __host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
 
@@ -112,6 +111,20 @@ struct SlotOccupancy<Plain<float>> {
     static constexpr int kMinBlocks = 5;
 };
 
+// 16-byte value loads in flight per lane: 3 for the FP32 matvec (2% over 2 at L=12;
+// 4 spills at the 48-register budget), 2 for the hi/lo variant (two arrays per quad).
+// Measured and dropped: a cp.async ring of 2-5 quads per lane in shared memory
+// (3.0-3.6 TB/s, with or without an evict-first L2 policy) and two or three tiles
+// of one alpha string per block sharing the staged descriptors (4.4 / 2.7 TB/s).
+template <typename F>
+struct SlotInFlight {
+    static constexpr int kQuads = 2;
+};
+template <>
+struct SlotInFlight<Plain<float>> {
+    static constexpr int kQuads = 3;
+};
+
 // ---------------------------------------------------------------------------
 // Matvec. Block = one tile; warp w: rows (w % kRowWarps) * 32 + lane, quad range w / kRowWarps.
 template <typename F>
@@ -135,6 +148,7 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
     const uint32_t *dt = p.b.d_target + ib * p.b.nd;
     const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
     const int64_t qbase = (ia * T + t) * (int64_t)Q;
+    constexpr int kQuadsInFlight = SlotInFlight<F>::kQuads;
     typename F::Acc acc{};
     typename F::Chunk v[kQuadsInFlight];
     // kQuadsInFlight quads in flight per lane; each quad has one beta kind (uniform branch)
