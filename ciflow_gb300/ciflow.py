@@ -423,7 +423,7 @@ class FCI_File(CIMethod):
         return len(self.up) // self.words
 
     def get_density(self):
-        raise NotImplementedError("RDMs of determinant lists are not built (cigpu_rdm returns ENOTSUP)")
+        return DensFILE(self)
 
 
 class CI_Big(FCI_File):
@@ -519,6 +519,10 @@ class CIDens:
             tr2 = float(np.trace(self._aa) + np.trace(self._bb) + np.trace(self._ab))
             if abs(tr2 - N * (N - 1) / 2) > 1e-5:
                 raise AssertionError(f"trace of the 2-RDM {tr2} != {N * (N - 1) / 2}")
+
+
+class DensFILE(CIDens):
+    """RDMs of a determinant list's state (DensFILE, CIDens.h:157-170)."""
 
 
 class DensFCI(CIDens):

@@ -742,7 +742,7 @@ int cigpu_solve(cigpu_crs *crs, double tol, int64_t max_matvec, const double *c0
 
 int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *aa, double *ab, double *bb) {
     if (!crs || !c) return CIGPU_EINVAL;
-    if (crs->method == CIGPU_DETS) return CIGPU_ENOTSUP;
+    if (crs->method == CIGPU_DETS && crs->L > 64) return CIGPU_ENOTSUP;
     CIGPU_TRY
     cudaStream_t s = crs->stream;
     StreamScope scope(s);

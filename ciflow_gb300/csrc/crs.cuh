@@ -55,6 +55,9 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
 int status_from_exception();
 // y = H x of a determinant list without a stored matrix (every pair rescanned).
 void dets_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s);
+// RDMs of a determinant list's state (device vector c); host outputs as cigpu_rdm
+// (the 2-RDM when aa, ab and bb are all given).
+void dets_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s);
 // CIGPU_EINVAL unless h is symmetric and eri 8-fold symmetric (1e-10 relative) and all finite.
 int validate_integrals(int L, const double *h, const double *eri, bool *exact);
 // CIGPU_EINVAL unless U (L x L, row-major) is finite and orthogonal to 1e-10.

@@ -418,7 +418,274 @@ bool parse_line(const std::string &line, int words, uint64_t *up, uint64_t *down
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// RDMs of a list's state (DensFILE::construct_CI_one_dens / construct_CI_two_dens,
+// CIDens.cpp:1468-1529): every pair i <= j contributes c_i c_j through the
+// reference's fill rules (fill_density_matrix_one / fill_density_matrix,
+// CIDens.cpp:676-896) into the symmetric (min, max) storage of CIDens. The sums are
+// accumulated as 64-bit fixed-point integers (value * 2^60, rounded to nearest) with
+// integer atomics: integer addition is associative, so the result does not depend on
+// the order the warps reach an element (bit-identical runs), and two's-complement
+// wrap-around keeps every final sum exact while it lies within +-8 (RDM elements lie
+// within +-1). Each contribution is rounded by at most 2^-61.
+struct RdmAcc {
+    unsigned long long *one, *aa, *ab, *bb;
+    int L, np;
+    bool two;
+};
+
+__device__ __forceinline__ void acc_add(unsigned long long *at, double v) {
+    atomicAdd(at, (unsigned long long)__double2ll_rn(v * 0x1p60));
+}
+__device__ __forceinline__ void rdm_add_one(const RdmAcc &R, int spin, int o1, int o2, double v) {
+    const int a = min(o1, o2), b = max(o1, o2);
+    acc_add(R.one + ((int64_t)spin * R.L + a) * R.L + b, v);
+}
+// add_two_rdm (CIDens.cpp:227-256)
+__device__ __forceinline__ void rdm_add_two(const RdmAcc &R, int spin, int o1, int o2, int o3, int o4, double v) {
+    const int L = R.L;
+    if (spin == 1) {
+        const int64_t A = (int64_t)o1 * L + o2, B = (int64_t)o3 * L + o4;
+        acc_add(R.ab + min(A, B) * (int64_t)L * L + max(A, B), v);
+        return;
+    }
+    if (o1 == o2 || o3 == o4) return;
+    int odd = 0;
+    if (o1 > o2) {
+        const int t = o1;
+        o1 = o2;
+        o2 = t;
+        odd ^= 1;
+    }
+    if (o3 > o4) {
+        const int t = o3;
+        o3 = o4;
+        o4 = t;
+        odd ^= 1;
+    }
+    const int64_t A = o1 * L + o2 - (o1 + 1) * (o1 + 2) / 2, B = o3 * L + o4 - (o3 + 1) * (o3 + 2) / 2;
+    acc_add((spin == 0 ? R.aa : R.bb) + min(A, B) * R.np + max(A, B), negate_if(v, odd));
+}
+
+// fill_one_dense (CIDens.cpp:676-754) for strings b1 -> b2 differing in one orbital;
+// `same` is the other spin's string. alpha: the moved electron is alpha.
+template <int W>
+__device__ void fill_single(const RdmAcc &R, const uint64_t *b1, const uint64_t *b2, const uint64_t *same, double contr,
+                            bool alpha) {
+    uint64_t x[W], c[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        x[w] = b1[w] ^ b2[w];
+        c[w] = b1[w] & b2[w];
+    }
+    const int o0 = pop_lowest<W>(x), o1 = pop_lowest<W>(x);
+    contr = negate_if(contr, nstacked<W>(o0, o1, c) & 1);
+    rdm_add_one(R, alpha ? 0 : 1, o0, o1, contr);
+    if (!R.two) return;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = c[w]; y; y &= y - 1) {
+            const int z = 64 * w + __ffsll((long long)y) - 1;
+            rdm_add_two(R, alpha ? 0 : 2, o0, z, o1, z, contr);
+        }
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = same[w]; y; y &= y - 1) {
+            const int z = 64 * w + __ffsll((long long)y) - 1;
+            if (alpha)
+                rdm_add_two(R, 1, o0, z, o1, z, contr);
+            else
+                rdm_add_two(R, 1, z, o0, z, o1, contr);
+        }
+}
+
+// fill_two_dense (CIDens.cpp:756-779): a same-spin double
+template <int W>
+__device__ void fill_double_same(const RdmAcc &R, const uint64_t *s1, const uint64_t *s2, double contr, int spin) {
+    uint64_t x[W], c[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        x[w] = s1[w] ^ s2[w];
+        c[w] = s1[w] & s2[w];
+    }
+    int o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = pop_lowest<W>(x);
+    int a0, a1, b0, b1;
+    arrange4<W>(o, s1, a0, a1, b0, b1);
+    const int diff = nstacked<W>(a0, a1, c) + nstacked<W>(b0, b1, c);
+    rdm_add_two(R, spin, a0, a1, b0, b1, negate_if(contr, diff & 1));
+}
+
+// fill_two_dense_upanddown (CIDens.cpp:781-806): an alpha-beta double
+template <int W>
+__device__ void fill_double_ab(const RdmAcc &R, const uint64_t *u1, const uint64_t *u2, const uint64_t *d1,
+                               const uint64_t *d2, double contr) {
+    uint64_t xu[W], cu[W], xd[W], cd[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        xu[w] = u1[w] ^ u2[w];
+        cu[w] = u1[w] & u2[w];
+        xd[w] = d1[w] ^ d2[w];
+        cd[w] = d1[w] & d2[w];
+    }
+    int a0 = pop_lowest<W>(xu), a1 = pop_lowest<W>(xu);
+    if (!has_bit<W>(u1, a0)) {
+        const int t = a0;
+        a0 = a1;
+        a1 = t;
+    }
+    int b0 = pop_lowest<W>(xd), b1 = pop_lowest<W>(xd);
+    if (!has_bit<W>(d1, b0)) {
+        const int t = b0;
+        b0 = b1;
+        b1 = t;
+    }
+    const int diff = nstacked<W>(a0, a1, cu) + nstacked<W>(b0, b1, cd);
+    rdm_add_two(R, 1, a0, b0, a1, b1, negate_if(contr, diff & 1));
+}
+
+// fill_diagonal (CIDens.cpp:808-853)
+template <int W>
+__device__ void fill_diag(const RdmAcc &R, const uint64_t *up, const uint64_t *dn, double contr) {
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = up[w]; y; y &= y - 1) rdm_add_one(R, 0, 64 * w + __ffsll((long long)y) - 1, 64 * w + __ffsll((long long)y) - 1, contr);
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = dn[w]; y; y &= y - 1) rdm_add_one(R, 1, 64 * w + __ffsll((long long)y) - 1, 64 * w + __ffsll((long long)y) - 1, contr);
+    if (!R.two) return;
+    for (int spin = 0; spin < 2; ++spin) {
+        const uint64_t *s = spin == 0 ? up : dn;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            for (uint64_t y = s[w]; y; y &= y - 1) {
+                const int i = 64 * w + __ffsll((long long)y) - 1;
+                // partners j > i
+#pragma unroll
+                for (int w2 = 0; w2 < W; ++w2) {
+                    uint64_t y2 = s[w2];
+                    if (w2 == w) y2 &= y & (y - 1);  // bits above i in the same word
+                    else if (w2 < w) y2 = 0;
+                    for (; y2; y2 &= y2 - 1) {
+                        const int j = 64 * w2 + __ffsll((long long)y2) - 1;
+                        rdm_add_two(R, spin == 0 ? 0 : 2, i, j, i, j, contr);
+                    }
+                }
+            }
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        for (uint64_t y = up[w]; y; y &= y - 1) {
+            const int i = 64 * w + __ffsll((long long)y) - 1;
+#pragma unroll
+            for (int w2 = 0; w2 < W; ++w2)
+                for (uint64_t y2 = dn[w2]; y2; y2 &= y2 - 1) {
+                    const int j = 64 * w2 + __ffsll((long long)y2) - 1;
+                    rdm_add_two(R, 1, i, j, i, j, contr);
+                }
+        }
+}
+
+template <int W>
+__global__ void __launch_bounds__(32 * kDetWarps) k_dets_rdm(DetParams p, const double *__restrict__ c, RdmAcc R) {
+    __shared__ uint64_t tile[kDetTile * 2 * W];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t r0 = (int64_t)blockIdx.x * kDetWarps; r0 < p.n; r0 += (int64_t)gridDim.x * kDetWarps) {
+        const int64_t i = r0 + warp;
+        const bool active = i < p.n;
+        uint64_t ui[W], di[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            ui[w] = active ? p.dets[i * 2 * W + w] : 0;
+            di[w] = active ? p.dets[i * 2 * W + W + w] : 0;
+        }
+        const double ci = active ? c[i] : 0.0;
+        // columns j >= i: tiles from the one holding i
+        for (int64_t base = (r0 / kDetTile) * kDetTile; base < p.n; base += kDetTile) {
+            const int tn = (int)(p.n - base < kDetTile ? p.n - base : kDetTile);
+            __syncthreads();
+            for (int t = threadIdx.x; t < tn * 2 * W; t += blockDim.x) tile[t] = p.dets[base * 2 * W + t];
+            __syncthreads();
+            if (!active) continue;
+            for (int jj = lane; jj < tn; jj += 32) {
+                const int64_t j = base + jj;
+                if (j < i) continue;
+                const uint64_t *uj = tile + jj * 2 * W, *dj = uj + W;
+                int nu = 0, nd = 0;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    nu += __popcll(ui[w] ^ uj[w]);
+                    nd += __popcll(di[w] ^ dj[w]);
+                }
+                if (nu + nd > 4) continue;
+                const double contr = ci * c[j];
+                // fill_density_matrix_one / fill_density_matrix (CIDens.cpp:855-896)
+                if (nu == 0 && nd == 0) fill_diag<W>(R, ui, di, contr);
+                else if (nu == 2 && nd == 0) fill_single<W>(R, ui, uj, di, contr, true);
+                else if (nu == 0 && nd == 2) fill_single<W>(R, di, dj, ui, contr, false);
+                else if (R.two && nu == 4 && nd == 0) fill_double_same<W>(R, ui, uj, contr, 0);
+                else if (R.two && nu == 0 && nd == 4) fill_double_same<W>(R, di, dj, contr, 2);
+                else if (R.two && nu == 2 && nd == 2) fill_double_ab<W>(R, ui, uj, di, dj, contr);
+            }
+        }
+    }
+}
+
+// Expands the (min, max) fixed-point storage into the full symmetric output arrays.
+__global__ void k_rdm_expand(RdmAcc R, double *rdm1, double *aa, double *ab, double *bb) {
+    const int L = R.L, np = R.np;
+    const int64_t L2 = (int64_t)L * L, n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;
+    const int64_t total = n1 + (R.two ? 2 * n2 + n3 : 0);
+    auto val = [](unsigned long long q) { return (double)(long long)q * 0x1p-60; };
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        if (t < n1) {
+            const int64_t s = t / L2, ij = t - s * L2;
+            const int i = (int)(ij / L), j = (int)(ij - (int64_t)i * L);
+            rdm1[t] = val(R.one[(s * L + min(i, j)) * L + max(i, j)]);
+        } else if (t < n1 + 2 * n2) {
+            const int64_t u = t - n1, which = u / n2, ij = u - which * n2;
+            const int64_t i = ij / np, j = ij - i * np;
+            const unsigned long long *X = which == 0 ? R.aa : R.bb;
+            (which == 0 ? aa : bb)[ij] = val(X[min(i, j) * np + max(i, j)]);
+        } else {
+            const int64_t ij = t - n1 - 2 * n2, i = ij / L2, j = ij - i * L2;
+            ab[ij] = val(R.ab[min(i, j) * L2 + max(i, j)]);
+        }
+    }
+}
+
 }  // namespace
+
+void dets_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s) {
+    const int L = c.L, np = L * (L - 1) / 2;
+    const int64_t L2 = (int64_t)L * L, n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;
+    const bool two = aa && ab && bb;
+    DevBuf<unsigned long long> acc(n1 + (two ? 2 * n2 + n3 : 0));
+    CIGPU_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes(), s));
+    RdmAcc R{acc.p, two ? acc.p + n1 : nullptr, two ? acc.p + n1 + 2 * n2 : nullptr, two ? acc.p + n1 + n2 : nullptr,
+             L, np, two};
+    DetParams p = params_of(c);
+    if (c.det_words == 1)
+        k_dets_rdm<1><<<rows_grid(c.dim), 32 * kDetWarps, 0, s>>>(p, c_dev, R);
+    else
+        k_dets_rdm<2><<<rows_grid(c.dim), 32 * kDetWarps, 0, s>>>(p, c_dev, R);
+    CIGPU_CUDA(cudaGetLastError());
+    DevBuf<double> out(n1 + (two ? 2 * n2 + n3 : 0));
+    double *o1 = out.p, *oaa = two ? out.p + n1 : nullptr, *obb = two ? out.p + n1 + n2 : nullptr,
+           *oab = two ? out.p + n1 + 2 * n2 : nullptr;
+    const int64_t total = (int64_t)out.n;
+    k_rdm_expand<<<(int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 8), 256, 0, s>>>(R, o1, oaa, oab, obb);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch(2);
+    if (rdm1) CIGPU_CUDA(cudaMemcpyAsync(rdm1, o1, sizeof(double) * n1, cudaMemcpyDeviceToHost, s));
+    if (two) {
+        CIGPU_CUDA(cudaMemcpyAsync(aa, oaa, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(bb, obb, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(ab, oab, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+    }
+    CIGPU_CUDA(cudaStreamSynchronize(s));
+}
 
 void dets_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
     DetParams p = params_of(c);

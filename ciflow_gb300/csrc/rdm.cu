@@ -27,6 +27,9 @@
 //
 // Storage follows CIDens: the 1-RDM and each 2-RDM block are symmetric pair
 // matrices (Vector2d, matrix.cpp:674-690), accumulated on (min, max) and mirrored.
+//
+// Determinant lists (DensFILE) are handled in dets.cu: a pair scan with 64-bit
+// fixed-point integer atomics (order-independent sums, also bit-reproducible).
 #include <algorithm>
 #include <mutex>
 #include <stdexcept>
@@ -469,6 +472,10 @@ DevBuf<T> upload(const std::vector<T> &v, cudaStream_t s) {
 }  // namespace
 
 void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s) {
+    if (c.method == CIGPU_DETS) {
+        dets_rdm(c, c_dev, rdm1, aa, ab, bb, s);
+        return;
+    }
     const int L = c.L, np = L * (L - 1) / 2;
     const int64_t L2 = (int64_t)L * L;
     const int64_t n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;

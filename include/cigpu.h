@@ -247,8 +247,9 @@ int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_d
  * SparseMatrix_CRS_Sym for the list, precision FP64 or MIXED);
  * CIGPU_DETS_ONTHEFLY stores no matrix (FP64 only): every matvec recomputes the
  * elements from the list, as CI_Big does for the part it does not keep. The CRS
- * handle works with cigpu_solve, cigpu_mvprod and (CRS storage) the exports;
- * cigpu_rdm returns CIGPU_ENOTSUP for it. ---- */
+ * handle works with cigpu_solve, cigpu_mvprod, (CRS storage) the exports, and
+ * cigpu_rdm for L <= 64 (DensFILE, CIDens.cpp:1468-1529: every pair of the list
+ * through the reference's fill rules; sums in 64-bit fixed point, bit-reproducible). ---- */
 enum { CIGPU_DETS_CRS = 0, CIGPU_DETS_ONTHEFLY = 1 };
 int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
                      int precision, cigpu_stream stream, cigpu_crs **out);

@@ -1008,3 +1008,27 @@ int orc_build_dets(int L, int nup, int ndown, const double *h, const double *eri
     return 0;
 }
 
+/* DensFILE::construct_CI_one_dens / construct_CI_two_dens (CIDens.cpp:1468-1529): every
+ * pair i <= j of a determinant list (64-bit strings) through fill_density_matrix_one /
+ * fill_density_matrix with contr = c_i c_j. Outputs as orc_rdm_pairs. */
+int orc_rdm_dets(int L, int ndet, const uint64_t *up, const uint64_t *down, const double *c, double *rdm1,
+                 double *aa, double *ab, double *bb) {
+    if (L < 2 || L > 62 || ndet < 1) return 1;
+    rdm_pool_t P;
+    pool_init(&P, L);
+#pragma omp parallel
+    {
+        rdm_t R;
+        rdm_bind(&R, L, P.buf + (size_t)thread_id() * P.sz);
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < ndet; ++i)
+            for (int j = i; j < ndet; ++j) {
+                const double contr = c[i] * c[j];
+                fill_pair_one(&R, up[i], down[i], up[j], down[j], contr);
+                fill_pair_two(&R, up[i], down[i], up[j], down[j], contr);
+            }
+    }
+    pool_reduce(&P, L, rdm1, aa, ab, bb);
+    return 0;
+}
+

@@ -58,6 +58,10 @@ int orc_rdm_excitations(int method, int L, int nup, int ndown, const double *c, 
 int orc_build_dets(int L, int nup, int ndown, const double *h, const double *eri, int64_t ndet, int words,
                    const uint64_t *up, const uint64_t *down, int64_t *row, uint32_t *col, double *val);
 
+/* RDMs of a determinant list's state (DensFILE: every pair i <= j, 64-bit strings). */
+int orc_rdm_dets(int L, int ndet, const uint64_t *up, const uint64_t *down, const double *c, double *rdm1,
+                 double *aa, double *ab, double *bb);
+
 /* Bounded samples for the CPU baseline: rows [r0, r1) of the upper CRS (see the .c file). */
 int64_t orc_build_rows(int method, int L, int nup, int ndown, const double *h, const double *eri, int64_t r0,
                        int64_t r1, int64_t *counts, uint32_t *col, double *val);

@@ -405,3 +405,21 @@ def build_dets(ints, up: np.ndarray, down: np.ndarray, words: int = 1) -> UpperC
                        _ptr(col), _ptr(val))
     return UpperCRS(row, col, val)
 
+
+def rdm_dets(L: int, up: np.ndarray, down: np.ndarray, c: np.ndarray):
+    """DensFILE RDMs of a determinant list's state, CIDens conventions (64-bit strings)."""
+    lib = port()
+    lib.orc_rdm_dets.restype = ctypes.c_int
+    lib.orc_rdm_dets.argtypes = [ctypes.c_int, ctypes.c_int] + [_P] * 7
+    np_ = L * (L - 1) // 2
+    up = np.ascontiguousarray(up, dtype=np.uint64)
+    down = np.ascontiguousarray(down, dtype=np.uint64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    r1 = np.zeros((2, L, L))
+    aa = np.zeros((np_, np_))
+    ab = np.zeros((L * L, L * L))
+    bb = np.zeros((np_, np_))
+    if lib.orc_rdm_dets(L, len(up), _ptr(up), _ptr(down), _ptr(c), _ptr(r1), _ptr(aa), _ptr(ab), _ptr(bb)) != 0:
+        raise ValueError("oracle rejected the list")
+    return r1, aa, ab, bb
+

@@ -193,8 +193,12 @@ def case_dets(name: str):
             m = r.crs()
             ru, rd = r.dets()
             assert np.array_equal(ru, up) and np.array_equal(rd, dn), "reference list differs from the parse"
-            e, _ = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
+            e, c = O.lowest_eigenpair(m, v0=np.random.default_rng(12345).standard_normal(m.n))
             rec.update({"crs_sha256_reference": crs_sha256(m), "e0_reference": e + ints.econst})
+            if tag == "beh2":  # DensFILE RDMs of the reference (TestDensity.cpp compares them with DensFCI)
+                (r1, aa, ab, bb), ed = r.density(ints.L, e, c)
+                out.update({f"{tag}_c": c, f"{tag}_rdm1": r1, f"{tag}_aa": aa, f"{tag}_ab": ab, f"{tag}_bb": bb})
+                rec["dens_energy_reference"] = ed
             r.close()
         meta[tag] = rec
         out.update({f"{tag}_up": up, f"{tag}_down": dn})

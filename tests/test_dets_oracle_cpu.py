@@ -81,3 +81,14 @@ def test_reader_errors(tmp_path):
     assert lib.cigpu_dets_read(str(long).encode(), 1, 0, None, None, ctypes.byref(n), ctypes.byref(nb)) == A.EINVAL
     assert lib.cigpu_dets_read(str(long).encode(), 2, 0, None, None, ctypes.byref(n), ctypes.byref(nb)) == A.OK
     assert (n.value, nb.value) == (1, 70)
+
+
+def test_oracle_densfile_matches_reference():
+    """The oracle's DensFILE restatement against the reference's DensFILE RDMs of the
+    BeH2 list (tests/golden/dets.npz)."""
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dets.npz"))
+    ints, up, down, words, meta = dets_case("beh2")
+    got = O.rdm_dets(ints.L, up, down, g["beh2_c"])
+    for x, k in zip(got, ("rdm1", "aa", "ab", "bb")):
+        assert np.max(np.abs(x - g[f"beh2_{k}"])) < 1e-14, k
+

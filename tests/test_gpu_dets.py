@@ -105,7 +105,46 @@ def test_dets_rejections():
                                 ctypes.byref(out)) == A.EINVAL  # orbital 9 of a 7-orbital space
     assert lib.cigpu_build_dets(ham.device(), len(up), 1, A.ptr(up), A.ptr(down), A.DETS_ONTHEFLY, A.MIXED, None,
                                 ctypes.byref(out)) == A.ENOTSUP
-    cim = FCI_File(ham, up=up, down=down)
-    c = np.zeros(len(up))
-    c[0] = 1.0
-    assert lib.cigpu_rdm(cim.get_mat().handle, A.ptr(c), None, None, None, None) == A.ENOTSUP
+
+
+def rdms(cim_handle, L, c):
+    np_ = L * (L - 1) // 2
+    one, aa = np.zeros((2, L, L)), np.zeros((np_, np_))
+    ab, bb = np.zeros((L * L, L * L)), np.zeros((np_, np_))
+    c = np.ascontiguousarray(c)
+    A.check(A.lib().cigpu_rdm(cim_handle, A.ptr(c), A.ptr(one), A.ptr(aa), A.ptr(ab), A.ptr(bb)))
+    return one, aa, ab, bb
+
+
+def test_dets_rdm_matches_reference_densfile():
+    """The device DensFILE RDMs of the BeH2 list equal the reference's DensFILE
+    (tests/golden/dets.npz) to 1e-13 and, as TestDensity.cpp checks, DensFCI's to
+    1e-11; two runs are bit-identical (order-independent fixed-point sums)."""
+    import json, os
+    from .helpers import GOLDEN, beh2_integrals
+    ints, up, down, words, meta = dets_case("beh2")
+    g = np.load(os.path.join(GOLDEN, "dets.npz"))
+    cim = FCI_File(Hamiltonian.from_integrals(ints), up=up, down=down, words=words)
+    got = rdms(cim.get_mat().handle, ints.L, g["beh2_c"])
+    for x, k in zip(got, ("rdm1", "aa", "ab", "bb")):
+        assert np.max(np.abs(x - g[f"beh2_{k}"])) < 1e-13, k
+    again = rdms(cim.get_mat().handle, ints.L, g["beh2_c"])
+    assert all(np.array_equal(x, y) for x, y in zip(got, again))
+    _, _, arr = beh2_integrals()
+    for x, k in zip(got, ("rdm1", "aa", "ab", "bb")):
+        assert np.max(np.abs(x - arr[f"fci_{k}"])) < 1e-11, k
+    cim.solve(tol=1e-10)
+    cim.construct_density()
+    assert cim.cid.get_dens_energy() == pytest.approx(cim.get_ci_energy(), abs=1e-9)
+
+
+def test_dets_rdm_matches_oracle_gkci():
+    ints, up, down, words, meta = dets_case("be_gkci")
+    cim = FCI_File(Hamiltonian.from_integrals(ints), up=up, down=down, words=words)
+    cim.solve(tol=1e-10)
+    c = cim.get_eigvec()
+    got = rdms(cim.get_mat().handle, ints.L, c)
+    ref = O.rdm_dets(ints.L, up, down, c)
+    for x, y in zip(got, ref):
+        assert np.max(np.abs(x - y)) < 1e-13
+
