@@ -10,6 +10,9 @@
 //   SparseMatrix_CRS_Sym: getn/getm/datasize/operator()/mvprod (SparseMatrix_CRS.h:33-130)
 //   CIDens / DensFCI / DensDOCI: construct_density, get_one_rdm, get_two_rdm,
 //       get_one/two_electron_energy, get_dens_energy, test_invariants (CIDens.h:29-174)
+//   Hamiltonian(filename) / save_file (psi4 integral text), FCI_File / CI_Big (determinant
+//       lists, CIMethod.h:164-189), print_ci_vec / print_rdm (the reference's text dumps)
+//   SimulatedAnnealing / LocalMinimizer (orbital optimisers over cigpu_orbopt)
 // Differences by design: errors throw ciflow_gb300::Error (with the cigpu status)
 // instead of calling exit(1); solve keeps the CRS resident; FCI/DOCI take an
 // optional precision (CIGPU_FP64 = the plain method, CIGPU_MIXED).
@@ -56,6 +59,29 @@ class Hamiltonian {
           h_((size_t)Norbitals * Norbitals, 0.0), eri_((size_t)Norbitals * Norbitals * Norbitals * Norbitals, 0.0) {
         if (nGroup != 0) throw Error(CIGPU_ENOTSUP, "Hamiltonian: only point group 0 (C1)");
     }
+    // Hamiltonian(filename) for a psi4 integral text dump (Hamiltonian.cpp:157-171, 707-885).
+    explicit Hamiltonian(const std::string &filename) : L_(0), nup_(0), ndown_(0), econst_(0) {
+        check(cigpu_ham_read_psi4(filename.c_str(), &L_, &nup_, &ndown_, &econst_, nullptr, nullptr, nullptr, nullptr),
+              "cigpu_ham_read_psi4");
+        h_.assign((size_t)L_ * L_, 0.0);
+        eri_.assign((size_t)L_ * L_ * L_ * L_, 0.0);
+        check(cigpu_ham_read_psi4(filename.c_str(), &L_, &nup_, &ndown_, &econst_, h_.data(), eri_.data(), nullptr,
+                                  &hf_energy_),
+              "cigpu_ham_read_psi4");
+    }
+    // Takes ownership of a device Hamiltonian (e.g. an optimiser's rotated one) and reads its integrals.
+    explicit Hamiltonian(cigpu_ham *owned, int L, int nup, int ndown, double econst)
+        : L_(L), nup_(nup), ndown_(ndown), econst_(econst), h_((size_t)L * L), eri_((size_t)L * L * L * L) {
+        dev_.reset(owned);
+        check(cigpu_ham_export(owned, h_.data(), eri_.data()), "cigpu_ham_export");
+        dirty_ = false;
+    }
+    // Hamiltonian::save_file's format (C1, 17 significant digits).
+    void save_file(const std::string &filename) const {
+        check(cigpu_ham_write_psi4(filename.c_str(), L_, nup_, ndown_, econst_, h_.data(), eri_.data(), hf_energy_),
+              "cigpu_ham_write_psi4");
+    }
+    double get_hf_energy() const { return hf_energy_; }
     int getL() const { return L_; }
     int getnup() const { return nup_; }
     int getndown() const { return ndown_; }
@@ -96,6 +122,7 @@ class Hamiltonian {
     };
     int L_, nup_, ndown_;
     double econst_;
+    double hf_energy_ = 0;
     std::vector<double> h_, eri_;
     std::unique_ptr<cigpu_ham, Del> dev_;
     bool dirty_ = true;
@@ -175,6 +202,7 @@ class CIDens {
     std::pair<bool, bool> is_constructed() const { return solved_; }
 
    protected:
+    friend class CIMethod;
     CIMethod *cim_;
     unsigned state_;
     std::pair<bool, bool> solved_{false, false};
@@ -189,6 +217,10 @@ class DensDOCI : public CIDens {
    public:
     using CIDens::CIDens;
 };
+class DensFILE : public CIDens {
+   public:
+    using CIDens::CIDens;
+};
 
 class CIMethod {
    public:
@@ -198,7 +230,7 @@ class CIMethod {
     virtual std::string get_name() = 0;
     virtual std::unique_ptr<CIDens> get_density() = 0;
 
-    void build_ci() {
+    virtual void build_ci() {
         cigpu_crs *c = nullptr;
         check(cigpu_build(ham_->device(), method_, precision_, nullptr, &c), "cigpu_build");
         mat_.reset(new SparseMatrix_CRS_Sym(c));
@@ -240,6 +272,17 @@ class CIMethod {
         if (!cid_->is_constructed().first || (trdm && !cid_->is_constructed().second)) cid_->construct_density(trdm);
     }
     CIDens *density() { return cid_.get(); }
+    int get_method() const { return method_; }
+    int get_precision() const { return precision_; }
+    double get_tolerance() const { return tol_; }
+    // The CI-vector block of the reference's output (Output.cpp:135-263).
+    virtual void print_ci_vec(const std::string &path, double nauw = -1.0) {
+        check(cigpu_write_civec(path.c_str(), method_, get_l(), gNup(), gNdown(), (int64_t)eigvec_.size(),
+                                eigvec_.data(), get_ci_energy(), get_econst(), nauw, nullptr, nullptr, 1, nullptr),
+              "cigpu_write_civec");
+    }
+    // CIMethod::print_one_rdm / print_two_rdm (CIMethod.cpp:184-195) into a file.
+    void print_rdm(const std::string &path, bool trdm = true);
     Hamiltonian *get_ham() { return ham_; }
     SparseMatrix_CRS_Sym &get_mat() {
         if (!mat_) build_ci();
@@ -283,6 +326,180 @@ class DOCI : public CIMethod {
     std::unique_ptr<CIDens> get_density() override { return std::unique_ptr<CIDens>(new DensDOCI(this)); }
 };
 
+// FCI_File / CI_Big (CIMethod.h:164-189): CI over the determinant list of a file
+// (Permutator_File format) in list order; CI_Big keeps no matrix (every matvec
+// recomputes the elements).
+class FCI_File : public CIMethod {
+   public:
+    FCI_File(Hamiltonian *ham, const std::string &permfile, int precision = CIGPU_FP64)
+        : CIMethod(ham, CIGPU_DETS, precision), permfile_(permfile) {
+        words_ = ham->getL() <= 64 ? 1 : 2;
+        int64_t n = 0;
+        int nb = 0;
+        check(cigpu_dets_read(permfile.c_str(), words_, 0, nullptr, nullptr, &n, &nb), "cigpu_dets_read");
+        up_.resize((size_t)n * words_);
+        down_.resize((size_t)n * words_);
+        check(cigpu_dets_read(permfile.c_str(), words_, n, up_.data(), down_.data(), &n, &nb), "cigpu_dets_read");
+        build_ci();
+    }
+    void build_ci() override {
+        cigpu_crs *c = nullptr;
+        check(cigpu_build_dets(ham_->device(), get_dim(), words_, up_.data(), down_.data(), storage(), precision_,
+                               nullptr, &c),
+              "cigpu_build_dets");
+        mat_.reset(new SparseMatrix_CRS_Sym(c));
+    }
+    int get_dim() override { return (int)(up_.size() / words_); }
+    std::string get_name() override { return "FCI_File"; }
+    std::unique_ptr<CIDens> get_density() override { return std::unique_ptr<CIDens>(new DensFILE(this)); }
+    // Permutator::get_clean_detfile (Permutator.cpp:88-100)
+    std::string get_clean_detfile() const {
+        std::string f = permfile_.substr(permfile_.find_last_of("/\\") + 1);
+        f = f.substr(0, f.find_last_of('.'));
+        std::string out;
+        for (char ch : f)
+            if (std::string("_()-./\\").find(ch) == std::string::npos) out += ch;
+        return out;
+    }
+    void print_ci_vec(const std::string &path, double nauw = -1.0) override {
+        const std::string name = get_clean_detfile();
+        check(cigpu_write_civec(path.c_str(), CIGPU_DETS, get_l(), gNup(), gNdown(), (int64_t)eigvec_.size(),
+                                eigvec_.data(), get_ci_energy(), get_econst(), nauw, up_.data(), down_.data(), words_,
+                                name.c_str()),
+              "cigpu_write_civec");
+    }
+
+   protected:
+    virtual int storage() const { return CIGPU_DETS_CRS; }
+    std::string permfile_;
+    int words_ = 1;
+    std::vector<uint64_t> up_, down_;
+};
+
+class CI_Big : public FCI_File {
+   public:
+    CI_Big(Hamiltonian *ham, const std::string &permfile) : FCI_File(ham, permfile, CIGPU_FP64) {}
+    std::string get_name() override { return "CI_Big"; }
+
+   protected:
+    int storage() const override { return CIGPU_DETS_ONTHEFLY; }
+};
+
+// ---- orbital optimisers (SimulatedAnnealing.cpp, LocalMinimizer.cpp) over cigpu_orbopt ----
+// The optimiser owns the rotated Hamiltonians (as OrbitalOptimization owns _optham);
+// update_cim() hands the current one to the CIMethod and solves it there.
+class OrbitalOptimization {
+   public:
+    explicit OrbitalOptimization(CIMethod *cim, uint64_t seed = 0) : cim_(cim) {
+        if (!cim->is_solved()) cim->solve();
+        cigpu_orbopt_config cfg{};
+        cfg.method = cim->get_method();
+        cfg.precision = cim->get_precision();
+        cfg.tol = cim->get_tolerance();
+        cfg.warm_start = 1;
+        cfg.seed = seed;
+        cigpu_orbopt *o = nullptr;
+        check(cigpu_orbopt_create(cim->get_ham()->device(), &cfg, &o), "cigpu_orbopt_create");
+        opt_.reset(o);
+    }
+    virtual ~OrbitalOptimization() = default;
+    double get_opt_ci_energy() const { return stats().e_opt; }
+    std::vector<double> get_opt_unitary() const {
+        std::vector<double> u((size_t)cim_->get_l() * cim_->get_l());
+        check(cigpu_orbopt_get(opt_.get(), nullptr, u.data(), nullptr, nullptr), "cigpu_orbopt_get");
+        return u;
+    }
+    cigpu_orbopt_stats stats() const {
+        cigpu_orbopt_stats st{};
+        check(cigpu_orbopt_get(opt_.get(), nullptr, nullptr, nullptr, &st), "cigpu_orbopt_get");
+        return st;
+    }
+    // OrbitalOptimization::update_cim (SimulatedAnnealing.cpp:83-87)
+    void update_cim() {
+        cigpu_ham *h = nullptr;
+        check(cigpu_orbopt_ham(opt_.get(), &h), "cigpu_orbopt_ham");
+        Hamiltonian *ham = cim_->get_ham();
+        optham_.reset(new Hamiltonian(h, ham->getL(), ham->getnup(), ham->getndown(), ham->getEconst()));
+        cim_->set_ham(optham_.get());
+        cim_->solve();
+    }
+    // set_cim_optimal (SimulatedAnnealing.cpp:69-74)
+    void set_cim_optimal() {
+        check(cigpu_orbopt_set_optimal(opt_.get()), "cigpu_orbopt_set_optimal");
+        update_cim();
+    }
+    double get_cim_no() {
+        double e = 0;
+        check(cigpu_orbopt_natural(opt_.get(), cim_->get_method(), &e), "cigpu_orbopt_natural");
+        return e;
+    }
+    double get_fci_no() {
+        double e = 0;
+        check(cigpu_orbopt_natural(opt_.get(), CIGPU_FCI, &e), "cigpu_orbopt_natural");
+        return e;
+    }
+
+   protected:
+    struct Del {
+        void operator()(cigpu_orbopt *o) const { cigpu_orbopt_destroy(o); }
+    };
+    CIMethod *cim_;
+    std::unique_ptr<cigpu_orbopt, Del> opt_;
+    std::unique_ptr<Hamiltonian> optham_;
+};
+
+class SimulatedAnnealing : public OrbitalOptimization {
+   public:
+    SimulatedAnnealing(CIMethod *cim, double temp, double change_temp, double angle, double change_angle,
+                       uint64_t seed = 0)
+        : OrbitalOptimization(cim, seed) {
+        p_.temp = temp;
+        p_.change_temp = change_temp;
+        p_.max_angle = angle;
+        p_.change_angle = change_angle;
+        p_.steps = 20000;
+        p_.max_unaccept = 2000;
+        p_.min_angle = 1e-7;
+        p_.speculate = 1;
+    }
+    void set_steps(int64_t steps) { p_.steps = steps; }
+    void set_speculate(int k) { p_.speculate = k; }
+    // SimulatedAnnealing::optimize (SimulatedAnnealing.cpp:306-391)
+    double optimize() {
+        double e = 0;
+        check(cigpu_orbopt_anneal(opt_.get(), &p_, &e), "cigpu_orbopt_anneal");
+        update_cim();
+        return e;
+    }
+
+   private:
+    cigpu_anneal_params p_{};
+};
+
+class LocalMinimizer : public OrbitalOptimization {
+   public:
+    explicit LocalMinimizer(CIMethod *cim, uint64_t seed = 0) : OrbitalOptimization(cim, seed) {
+        if (cim->get_method() != CIGPU_DOCI) throw Error(CIGPU_ENOTSUP, "LocalMinimizer: DOCI only");
+        p_.conv_crit = 1e-6;
+        p_.conv_steps = 25;
+        p_.max_iters = 1000;
+    }
+    void set_conv_crit(double crit) { p_.conv_crit = crit; }
+    void set_conv_steps(int steps) { p_.conv_steps = steps; }
+    double get_conv_crit() const { return p_.conv_crit; }
+    // LocalMinimizer::optimize (LocalMinimizer.cpp:130-235)
+    double optimize(bool dist_choice = false) {
+        p_.dist_choice = dist_choice ? 1 : 0;
+        double e = 0;
+        check(cigpu_orbopt_local(opt_.get(), &p_, &e), "cigpu_orbopt_local");
+        update_cim();
+        return e;
+    }
+
+   private:
+    cigpu_local_params p_{};
+};
+
 // ---- CIDens members that need CIMethod ----
 inline unsigned CIDens::dim() const { return (unsigned)cim_->get_l(); }
 
@@ -297,6 +514,14 @@ inline void CIDens::construct_density(bool twordm) {
                     twordm ? ab_.data() : nullptr, twordm ? bb_.data() : nullptr),
           "cigpu_rdm");
     solved_ = {true, twordm};
+}
+
+inline void CIMethod::print_rdm(const std::string &path, bool trdm) {
+    construct_density(0, trdm);
+    const CIDens &d = *cid_;
+    check(cigpu_write_rdm(path.c_str(), get_l(), d.one_.data(), trdm ? d.aa_.data() : nullptr,
+                          trdm ? d.ab_.data() : nullptr, trdm ? d.bb_.data() : nullptr),
+          "cigpu_write_rdm");
 }
 
 inline double CIDens::get_one_electron_energy() const {

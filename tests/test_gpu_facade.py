@@ -28,7 +28,7 @@ def test_cpp_facade_driver(tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "test_facade.cpp"), "-o", str(exe), "-L", lib, "-lcigpu",
                     f"-Wl,-rpath,{lib}"], check=True)
-    out = subprocess.run([str(exe), str(data)], check=True, capture_output=True, text=True).stdout
+    out = subprocess.run([str(exe), str(data), str(tmp_path)], check=True, capture_output=True, text=True).stdout
     r = json.loads(out.strip().splitlines()[-1])
     # reference tests/src/TestDOCI.cpp:31
     assert abs(r["e_doci"] - (-15.225362047972723)) < 1e-10
@@ -40,3 +40,13 @@ def test_cpp_facade_driver(tmp_path):
     assert r["h00"] == ref.val[0]
     ysum = float(np.sum(O.sym_mvprod(ref, np.ones(ref.n))))
     assert abs(r["ysum"] - ysum) < 1e-9 * max(1.0, abs(ysum))
+    # psi4 dump round trip, FCI_File / CI_Big over the full list, text dumps, optimisers
+    assert r["psi4_round_trip"] == 1
+    assert r["dim_file"] == meta["fci"]["dim"]
+    assert abs(r["e_file"] - r["e_fci"]) < 1e-9 and abs(r["e_big"] - r["e_fci"]) < 1e-9
+    assert abs(r["e_file_dens"] - r["e_fci"]) < 1e-9  # DensFILE, as TestDensity.cpp
+    assert (tmp_path / "fci_vec.txt").read_text().count("\n") > 10
+    assert "#THE 2RDM:" in (tmp_path / "fci_rdm.txt").read_text()
+    assert r["e_sa_opt"] <= r["e_opt_start"] + 1e-10 and abs(r["e_sa"] - r["e_sa_opt"]) < 1e-8
+    assert r["e_lm"] <= r["e_sa"] + 1e-8 and abs(r["e_lm_cim"] - r["e_lm"]) < 1e-8
+
