@@ -313,6 +313,11 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
             c.val32.alloc(slots_count(p));
             c.val32lo.alloc(slots_count(p));
             fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
+            c.slot_desc.alloc(std::max<int64_t>(slot_desc_count(p), 1));
+            c.slot_st.alloc(std::max<int64_t>(slot_st_count(p), 4));
+            slot_tables_launch(p, c.slot_desc.p, c.slot_st.p, s);
+            p.desc_tab = c.slot_desc.p;
+            p.st_tab = c.slot_st.p;
             tr.mark("slot fill");
         } else {
             fci_launch(kCount, p, s);

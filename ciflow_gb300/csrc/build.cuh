@@ -34,6 +34,10 @@ struct FciParams {
     double *val64;
     float *val32;
     float *val32lo;  // v - (double)hi, rounded to FP32 (FP32 fill only)
+    // slot-tile matvecs: each alpha string's slot descriptors [Da][Wp] and each
+    // beta tile's single targets [tiles][ns_b][kTileRows] (slot_tables_launch)
+    const uint64_t *desc_tab = nullptr;
+    const uint32_t *st_tab = nullptr;
 };
 
 struct DociParams {

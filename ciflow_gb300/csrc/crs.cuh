@@ -27,6 +27,8 @@ struct cigpu_crs {
     // MIXED FCI: values-only slot tiles (val32/val32lo hold slots_count(fp) values,
     // no col); row_ptr/upper_off/nnz still describe the explicit matrix for export
     bool slots = false;
+    cigpu::DevBuf<uint64_t> slot_desc;  // the slot matvecs' staging tables (slot_tables_launch)
+    cigpu::DevBuf<uint32_t> slot_st;
     cigpu::DevBuf<float> x32;  // MIXED: FP32 copy of x for the FP64 product from hi + lo
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};

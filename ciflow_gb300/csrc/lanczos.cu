@@ -50,10 +50,22 @@ constexpr int kMaxKeep = 32;
 constexpr int kStartSteps = 4;  // FP32 Lanczos steps of the mixed solver's Krylov start
 
 int vec_grid() { return sm_count() * 4; }
-// blocks for an n-element vector kernel: about 4 elements per thread, at most vec_grid()
+// blocks for an n-element basis kernel (dots, updates, combinations): one element
+// per thread up to 8 resident blocks per SM. These kernels read many basis vectors
+// per element, so a thread's loads, not the bytes, set their time on small vectors
+// (tens of thousands of elements): spreading them over every SM instead of a few
+// elements per thread on a quarter of the SMs cut a 30-vector update from ~19 us to
+// a few us at n = 63,504.
 int vec_grid_for(int64_t n) {
+    const int64_t b = (n + kVecThreads - 1) / kVecThreads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * 8, b));
+}
+// blocks per chunk of the dot kernels: about four elements per thread (the grid has
+// one row of blocks per chunk of eight vectors, and fewer partials shorten the
+// reduction that ends the kernel)
+int dot_grid_for(int64_t n) {
     const int64_t b = (n + kVecThreads * 4 - 1) / (kVecThreads * 4);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(vec_grid(), b));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * 4, b));
 }
 
 // Ends a kernel that wrote per-block partial sums partial[v*G + b] (G = gridDim.x):
@@ -79,22 +91,72 @@ __device__ __forceinline__ void reduce_in_last_block(const double *partial, int 
     if (threadIdx.x == 0) *ticket = 0;
 }
 
-// Per-block partial dots V_i . w (i < nvec, chunks of kDotChunk on blockIdx.y).
-// AT is the arithmetic type of the products and of the per-thread sums (float for
-// FP32 vectors: GB300 issues FP64 at 1/64 of the FP32 rate); block partials are
-// reduced in FP64.
+// The last of the gridDim.x blocks of one chunk (blockIdx.y) reduces the chunk's nv
+// rows of block partials partial[i * G + b] into out[i], warp i for row i (a fixed
+// order: lanes over b, four running sums, then the warp tree), and resets the
+// chunk's ticket. A ticket per chunk keeps the atomics spread and puts each chunk's
+// reduction on its own block instead of one block reducing every vector.
+__device__ __forceinline__ void reduce_chunk_in_last_block(const double *partial, int nv, double *out,
+                                                           unsigned *ticket) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int G = gridDim.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < nv) {
+        const double *p = partial + (int64_t)warp * G;
+        double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        int b = lane;
+        for (; b + 96 < G; b += 128) {
+            s0 += __ldcg(p + b);
+            s1 += __ldcg(p + b + 32);
+            s2 += __ldcg(p + b + 64);
+            s3 += __ldcg(p + b + 96);
+        }
+        for (; b < G; b += 32) s0 += __ldcg(p + b);
+        double s = (s0 + s1) + (s2 + s3);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[warp] = s;
+    }
+    if (threadIdx.x == 0) *ticket = 0;
+}
+
+// Per-block partial dots V_i . w (i < nvec, chunks of kDotChunk on blockIdx.y, one
+// ticket per chunk). AT is the arithmetic type of the products and of the
+// per-thread sums (float for FP32 vectors: GB300 issues FP64 at 1/64 of the FP32
+// rate); block partials are reduced in FP64. Each thread walks its elements two at
+// a time, so 18 loads are in flight per step of the loop.
 template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__ V, int64_t ld, int nvec,
                                                           const WT *__restrict__ w, int64_t n,
                                                           double *__restrict__ partial, double *__restrict__ out,
-                                                          unsigned *__restrict__ ticket) {
+                                                          unsigned *__restrict__ tickets) {
+    static_assert(kDotChunk <= kVecThreads / 32, "one warp per vector of a chunk");
     const int G = gridDim.x;
     const int v0 = blockIdx.y * kDotChunk;
     const int nv = min(kDotChunk, nvec - v0);
     AT acc[kDotChunk];
 #pragma unroll
     for (int i = 0; i < kDotChunk; ++i) acc[i] = 0;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; r + stride < n; r += 2 * stride) {
+        const AT wa = (AT)w[r], wb = (AT)w[r + stride];
+        AT va[kDotChunk], vb[kDotChunk];
+#pragma unroll
+        for (int i = 0; i < kDotChunk; ++i)
+            if (i < nv) {
+                va[i] = (AT)V[(int64_t)(v0 + i) * ld + r];
+                vb[i] = (AT)V[(int64_t)(v0 + i) * ld + r + stride];
+            }
+#pragma unroll
+        for (int i = 0; i < kDotChunk; ++i)
+            if (i < nv) acc[i] += va[i] * wa + vb[i] * wb;
+    }
+    if (r < n) {
         const AT wr = (AT)w[r];
 #pragma unroll
         for (int i = 0; i < kDotChunk; ++i)
@@ -116,7 +178,7 @@ __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__
         for (int k = 0; k < kVecThreads / 32; ++k) s += sh[threadIdx.x][k];
         partial[(int64_t)(v0 + threadIdx.x) * G + blockIdx.x] = s;
     }
-    reduce_in_last_block(partial, nvec, out, ticket);
+    reduce_chunk_in_last_block(partial + (int64_t)v0 * G, nv, out + v0, tickets + blockIdx.y);
 }
 
 // w -= sum_{i<nvec} V_i coef_i (arithmetic in AT); partial ||w||^2 per block when nrm != nullptr.
@@ -131,7 +193,15 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
     AT acc = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         AT x = (AT)w[r];
-        for (int i = 0; i < nvec; ++i) x -= (AT)V[(int64_t)i * ld + r] * c[i];
+        int i = 0;
+        for (; i + 8 <= nvec; i += 8) {  // eight loads in flight, products subtracted in order
+            AT v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = (AT)V[(int64_t)(i + q) * ld + r];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) x -= v[q] * c[i + q];
+        }
+        for (; i < nvec; ++i) x -= (AT)V[(int64_t)i * ld + r] * c[i];
         const WT xv = (WT)x;
         w[r] = xv;
         acc += (AT)xv * (AT)xv;
@@ -180,8 +250,20 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__r
     float acc = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         float ru = fa0 * r32[r] + fa0de * c32[r];
-        for (int i = 0; i < k; ++i) {
-            const int64_t o = (int64_t)(i + 1) * ld + r;  // corrections live in slots 1..k
+        int i = 0;
+        for (; i + 4 <= k; i += 4) {  // eight loads in flight, terms added in order
+            float hv[4], vv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t o = (int64_t)(i + q + 1) * ld + r;  // corrections live in slots 1..k
+                hv[q] = HV[o];
+                vv[q] = V[o];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ru += ys[i + q] * (hv[q] - fth * vv[q]);
+        }
+        for (; i < k; ++i) {
+            const int64_t o = (int64_t)(i + 1) * ld + r;
             ru += ys[i] * (HV[o] - fth * V[o]);
         }
         acc += ru * ru;
@@ -300,7 +382,18 @@ __global__ void __launch_bounds__(kVecThreads) k_combine(const VT *__restrict__ 
         double acc[KMAX];
 #pragma unroll
         for (int i = 0; i < KMAX; ++i) acc[i] = 0;
-        for (int l = 0; l < m; ++l) {
+        int l = 0;
+        for (; l + 4 <= m; l += 4) {  // four loads in flight, terms added in order
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = (double)V[(int64_t)(l + q) * ld + r];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int i = 0; i < KMAX; ++i)
+                    if (i < k) acc[i] += v[q] * y[l + q + m * i];
+        }
+        for (; l < m; ++l) {
             const double v = (double)V[(int64_t)l * ld + r];
 #pragma unroll
             for (int i = 0; i < KMAX; ++i)
@@ -400,16 +493,19 @@ void pinned_put(double *p) {
 }
 
 struct VecOps {
+    static constexpr int kTickets = (kMaxBasis + 2 + kDotChunk - 1) / kDotChunk;
     cudaStream_t s;
-    int G;                   // blocks of every vector kernel: sized to n, at most vec_grid()
-    DevBuf<double> partial;  // [(kMaxBasis+2) * G]
+    int G;                   // blocks of the elementwise and update kernels: one element per thread
+    int Gd;                  // blocks (per chunk) of the dot kernels: about four elements per thread
+    DevBuf<double> partial;  // [(kMaxBasis+2) * max(G, Gd)]
     DevBuf<double> out;      // [4 * (kMaxBasis+2)]
-    DevBuf<unsigned> ticket; // last-block counter of the fused reductions
+    DevBuf<unsigned> ticket; // last-block counters of the fused reductions (one per dot chunk)
     double *h_out = nullptr; // pinned
     VecOps(cudaStream_t st, int64_t n)
-        : s(st), G(vec_grid_for(n)), partial((size_t)(kMaxBasis + 2) * vec_grid_for(n)), out(4 * (kMaxBasis + 2)),
-          ticket(1) {
-        CIGPU_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
+        : s(st), G(vec_grid_for(n)), Gd(dot_grid_for(n)),
+          partial((size_t)(kMaxBasis + 2) * std::max(vec_grid_for(n), dot_grid_for(n))), out(4 * (kMaxBasis + 2)),
+          ticket(kTickets) {
+        CIGPU_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned) * kTickets, s));
         h_out = pinned_get();
     }
     ~VecOps() {
@@ -420,7 +516,7 @@ struct VecOps {
     // out[dst .. dst+nvec) = V_i . w   (AT: arithmetic type of the products)
     template <typename VT, typename WT, typename AT = double>
     void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst) {
-        dim3 grid(G, (nvec + kDotChunk - 1) / kDotChunk);
+        dim3 grid(Gd, (nvec + kDotChunk - 1) / kDotChunk);
         k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, out.p + dst, ticket.p);
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
@@ -742,7 +838,14 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     //   the correction size |y_v|, so once ru approaches eps32 |H| |y_v| (or the basis is
     //   full) the correction is folded into the anchor and the residual is recomputed
     //   exactly with an FP64 matvec (residual-correction restart).
-    // Basis slots: 0 = fp32(c) (orthogonalisation only), 1..k = corrections, k+1 = new.
+    //   A fold keeps one direction besides the new anchor: the previous step's Ritz
+    //   vector, orthogonalised against the current one (a "GD+1" restart). Its
+    //   image under H is the same combination of H c (kept in FP32) and the H v_i,
+    //   so it costs no matvec, and the restarted basis keeps the recurrence that a
+    //   collapse to the anchor alone loses: on an L=11 4a4b problem whose 30-vector
+    //   cycles only halved the residual this cut the matvecs from ~250 to ~105.
+    // Basis slots: 0 = fp32(c) (orthogonalisation; HV slot 0 = fp32(H c)),
+    // 1..k = corrections, k+1 = new.
     const int64_t n = P.n;
     const int64_t budget = o.max_matvec > 0 ? o.max_matvec : 3 * n;
     cudaStream_t s = P.stream;
@@ -757,7 +860,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     const int mmax = (int)std::min<int64_t>(std::min(o.dav_basis, kMaxBasis - 2), n - 2);
     DevBuf<float> V((size_t)(mmax + 2) * n), HV((size_t)(mmax + 2) * n), cr32((size_t)2 * n), diag32(n);
     dev_convert(P.diag, diag32.p, n, s);  // FP32 diagonal for the preconditioner
-    DevBuf<double> yd(kMaxBasis + 1);
+    DevBuf<double> yd(kMaxBasis + 1), dd(kMaxBasis + 2);
     int64_t mv32 = 0, mv64 = 0;
     if (!have_start) {
         // Krylov start. Davidson from the lowest-diagonal determinant alone can settle
@@ -819,13 +922,17 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         E = er.first;
         rho = er.second;
         dev_convert(c_dev, V.p, n, s);          // slot 0
+        dev_convert(ref.w.p, HV.p, n, s);       // H c, for the restart direction
         dev_convert(c_dev, cr32.p, n, s);       // c32, r32 for the couplings
         dev_convert(ref.r.p, cr32.p + n, n, s);
     };
     anchor();
     int k = 0;  // corrections in the basis
     double theta = E, a0 = 1.0, yv = 0;
-    std::vector<double> y(kMaxBasis + 1, 0.0);
+    std::vector<double> y(kMaxBasis + 1, 0.0), yp(kMaxBasis + 1, 0.0), d(kMaxBasis + 1, 0.0);
+    int ky = -1, kp = -1;  // corrections behind y and yp (-1: not of the current basis)
+    double a0p = 0;
+    int kept = 0;
     const int SLOT_R = 3 * (kMaxBasis + 1), SLOT_N = SLOT_R + 1;
     while (rho > o.tol && mv32 + mv64 < budget) {
         float *vnew = V.p + (size_t)(k + 1) * n;
@@ -875,11 +982,17 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         for (int i = 0; i < k; ++i)
             for (int j = 0; j < k; ++j) G[(size_t)(i + 1) * q + (j + 1)] = A[(size_t)i * kMaxBasis + j];
         small_eigh(q, G, wv, zv);
+        if (ky >= 0) {  // the previous Ritz vector, for a restart
+            std::copy(y.begin(), y.begin() + ky + 1, yp.begin());
+            a0p = a0;
+        }
+        kp = ky;
         theta = wv[0];
         if (q > 1) gap = wv[1] - wv[0];
         for (int i = 0; i < q; ++i) y[i] = zv[(size_t)i * q];
         a0 = y[0];
         for (int i = 1; i <= k; ++i) a0 -= y[i] * eta[i - 1];
+        ky = k;
         // fold when the previous approximate residual reached the FP32 floor of the
         // correction (the new solution, with one more vector, is at least as good),
         // when the basis is full, or on breakdown
@@ -889,18 +1002,80 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         for (int i = 1; i <= k; ++i) yv += y[i] * y[i];
         yv = std::sqrt(yv);
         if (fold) {
+            // restart direction: the previous Ritz vector p minus its component along
+            // the current one u, in the basis [c, v_1..v_k] (coefficients (a0, y_i)),
+            // formed with its H image in the spare slot k+1 before the anchor moves
+            bool keep = false;
+            if (kp >= 0 && kp <= k && !(rho_u <= 0.5 * o.tol) && tn2 > 1e-28) {
+                double uu = a0 * a0, up = a0 * a0p;
+                for (int i = 1; i <= k; ++i) {
+                    uu += y[i] * y[i];
+                    if (i <= kp) up += y[i] * yp[i];
+                }
+                const double f = up / uu;
+                double dn = 0;
+                for (int i = 0; i <= k; ++i) {
+                    const double pi = i == 0 ? a0p : (i <= kp ? yp[i] : 0.0);
+                    d[i] = pi - f * (i == 0 ? a0 : y[i]);
+                    dn += d[i] * d[i];
+                }
+                dn = std::sqrt(dn);
+                if (dn > 1e-8) {
+                    for (int i = 0; i <= k; ++i) d[i] /= dn;
+                    CIGPU_CUDA(cudaMemcpyAsync(dd.p, d.data(), sizeof(double) * (k + 1), cudaMemcpyHostToDevice, s));
+                    float *vs = V.p + (size_t)(k + 1) * n, *hs = HV.p + (size_t)(k + 1) * n;
+                    k_combine<float, float, 1><<<ops.G, kVecThreads, 0, s>>>(V.p, n, k + 1, dd.p, 1, vs, n, n);
+                    k_combine<float, float, 1><<<ops.G, kVecThreads, 0, s>>>(HV.p, n, k + 1, dd.p, 1, hs, n, n);
+                    CIGPU_CUDA(cudaGetLastError());
+                    count_launch(2);
+                    keep = true;
+                }
+            }
             // c <- a0 c + sum_i y_i v_i  (FP64)
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
             k_combine<float, double, 1><<<ops.G, kVecThreads, 0, s>>>(V.p + n, n, k, yd.p, 1, ref.t.p, n, n);
             k_axpby64<<<ops.G, kVecThreads, 0, s>>>(1.0, ref.t.p, a0, c_dev, n);
             CIGPU_CUDA(cudaGetLastError());
             count_launch(2);
+            const int kf = k;
             anchor();
             ++collapses;
             k = 0;
             yv = 0;
+            ky = kp = -1;
             if (rho > 0.7 * last_rho && collapses > 3) break;  // no progress between folds
             last_rho = rho;
+            if (keep && rho > o.tol) {
+                // the kept direction becomes v_1: one projection against the new
+                // anchor (H v_1 follows with H c), normalised, then its couplings
+                float *v1 = V.p + n, *h1 = HV.p + n;
+                CIGPU_CUDA(cudaMemcpyAsync(v1, V.p + (size_t)(kf + 1) * n, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+                CIGPU_CUDA(cudaMemcpyAsync(h1, HV.p + (size_t)(kf + 1) * n, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+                ops.dots<float, float, float>(V.p, n, 1, v1, n, 0);
+                ops.update<float, float, float>(V.p, n, 1, 0, v1, n, SLOT_N);
+                ops.update<float, float, float>(HV.p, n, 1, 0, h1, n, -1);
+                ops.scale(v1, n, SLOT_N);
+                ops.scale(h1, n, SLOT_N);
+                ops.dots<float, float, float>(v1, n, 1, h1, n, 1);
+                ops.dots<float, float, float>(cr32.p, n, 2, v1, n, 2);
+                const double *hr = ops.fetch(4);
+                if (hr[1] == hr[1] && hr[2] == hr[2] && hr[3] == hr[3]) {
+                    A[0] = hr[1];
+                    eta[0] = hr[2];
+                    bvec[0] = hr[3];
+                    k = 1;
+                    std::vector<double> G2 = {E, bvec[0], bvec[0], A[0]}, w2, z2;
+                    small_eigh(2, G2, w2, z2);
+                    theta = w2[0];
+                    gap = w2[1] - w2[0];
+                    y[0] = z2[0];
+                    y[1] = z2[2];
+                    a0 = y[0] - y[1] * eta[0];
+                    yv = std::fabs(y[1]);
+                    ky = 1;
+                    ++kept;
+                }
+            }
         }
     }
     info.e0 = E;
@@ -909,7 +1084,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     info.error_bound = gap > 0 ? rho * rho / gap : rho;
     info.matvecs_fp64 = mv64;
     info.matvecs_fp32 = mv32;
-    info.restarts = 0;
+    info.restarts = kept;
     info.corrections = collapses;
     info.converged = rho <= o.tol;
     trace_report("mixed davidson", info, tstart);

@@ -31,7 +31,6 @@
 // the CRS generator (build.cu), in slot order, and counts each row's stored
 // nonzeros and lower-triangle nonzeros on the way (the CRS row pointers of export).
 #include <algorithm>
-
 #include "slots.cuh"
 #include "spmv_formats.cuh"
 
@@ -40,6 +39,7 @@ namespace cigpu {
 namespace {
 
 constexpr int kSlotThreads = 256;
+constexpr int kPrefetchQuads = 4;  // quads (1 KB of FP32 values each) of a range prefetched to L2 at the start
 constexpr int kRowWarps = kTileRows / 32;                // warps covering the tile's rows
 constexpr int kSplits = kSlotThreads / 32 / kRowWarps;  // quad ranges per row
 
@@ -99,6 +99,40 @@ __device__ __forceinline__ void stage_tile(const FciParams &p, const SlotMap &m,
     }
 }
 
+// The matvec's staging from the precomputed tables (the tile's slot descriptors
+// and beta single targets) with 16-byte loads: a few independent loads per thread
+// where computing them took ~10 dependent table reads.
+__device__ __forceinline__ void stage_tile_tab(const FciParams &p, const SlotMap &m, int64_t ia, int64_t t,
+                                               uint64_t *desc, uint32_t *st) {
+    const uint4 *ds = reinterpret_cast<const uint4 *>(p.desc_tab + ia * m.wp);
+    uint4 *dd = reinterpret_cast<uint4 *>(desc);
+    for (int i = threadIdx.x; i < m.wp / 2; i += blockDim.x) dd[i] = __ldg(ds + i);
+    const int n4 = p.b.ns * kTileRows / 4;
+    const uint4 *ss = reinterpret_cast<const uint4 *>(p.st_tab + t * p.b.ns * kTileRows);
+    uint4 *sd = reinterpret_cast<uint4 *>(st);
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) sd[i] = __ldg(ss + i);
+}
+
+__global__ void k_slot_desc_table(const FciParams p, uint64_t *__restrict__ tab) {
+    const SlotMap m = slot_map(p);
+    const int64_t total = p.a.D * m.wp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ia = i / m.wp;
+        tab[i] = slot_desc(p, m, ia, (int)(i - ia * m.wp));
+    }
+}
+
+__global__ void k_slot_st_table(const FciParams p, uint32_t *__restrict__ tab) {
+    const int nsb = p.b.ns;
+    const int64_t T = (p.Db + kTileRows - 1) / kTileRows, per = (int64_t)nsb * kTileRows, total = T * per;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = i / per;
+        const int rem = (int)(i - t * per), xb = rem / kTileRows, r = rem - xb * kTileRows;
+        const int64_t ib = t * kTileRows + r;
+        tab[i] = ib < p.Db ? __ldg(p.b.s_target + ib * nsb + xb) : 0u;
+    }
+}
+
 // Blocks per SM the register budget is set for (measured at L=10..12): 5 for the
 // FP32 matvec (48 registers; forcing 6 blocks at 40 registers lost ILP and ran 5%
 // slower); the hi/lo variant runs 2% faster held to 4 blocks (64 registers).
@@ -127,6 +161,11 @@ struct SlotInFlight<Plain<float>> {
 
 // ---------------------------------------------------------------------------
 // Matvec. Block = one tile; warp w: rows (w % kRowWarps) * 32 + lane, quad range w / kRowWarps.
+// Measured and dropped: a tile split over a cluster of 2-4 blocks whose row sums
+// meet through distributed shared memory (for matrices of few tiles, 1.33 waves
+// at L=10): every block carries a fixed ~7-9 us (ramp, staging, drain), which
+// costs more than the emptier last wave (L=10: 63 us at two blocks per tile
+// against 66 us at one; L=11: 287 against 250 us).
 template <typename F>
 __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_spmv_slots(const FciParams p, const F f,
                                                              typename F::X *__restrict__ y) {
@@ -137,17 +176,21 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
     uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
     uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
-    stage_tile(p, m, ia, t, desc, st);
-    __syncthreads();
+    const int64_t tile = blockIdx.x;
+    const int64_t ia = tile / T, t = tile - ia * T;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = (warp % kRowWarps) * 32 + lane, ks = warp / kRowWarps;
+    const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
+    const int64_t qbase = tile * (int64_t)Q;
+    // the first values of each quad range head for L2 while the tables are staged
+    if (lane == 0 && warp % kRowWarps == 0 && c1 > c0)
+        f.prefetch((qbase + c0) * kTileRows * 4, (int64_t)min(c1 - c0, kPrefetchQuads) * kTileRows * 4);
+    stage_tile_tab(p, m, ia, t, desc, st);
+    __syncthreads();
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;
     const uint32_t *dt = p.b.d_target + ib * p.b.nd;
-    const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
-    const int64_t qbase = (ia * T + t) * (int64_t)Q;
     constexpr int kQuadsInFlight = SlotInFlight<F>::kQuads;
     typename F::Acc acc{};
     typename F::Chunk v[kQuadsInFlight];
@@ -373,6 +416,17 @@ void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *coun
     k_fill_slots<<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, hi, lo, count, lower);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
+}
+
+int64_t slot_desc_count(const FciParams &p) { return p.a.D * (int64_t)slot_map(p).wp; }
+int64_t slot_st_count(const FciParams &p) { return ((p.Db + kTileRows - 1) / kTileRows) * p.b.ns * kTileRows; }
+
+void slot_tables_launch(const FciParams &p, uint64_t *desc, uint32_t *st, cudaStream_t s) {
+    const int g = sm_count() * 8;
+    k_slot_desc_table<<<g, 256, 0, s>>>(p, desc);
+    if (slot_st_count(p) > 0) k_slot_st_table<<<g, 256, 0, s>>>(p, st);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch(slot_st_count(p) > 0 ? 2 : 1);
 }
 
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s) {

@@ -15,6 +15,13 @@ int64_t slots_count(const FciParams &p);
 // Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p) and
 // each row's stored-nonzero count and lower-triangle count (count, lower: [dim]).
 void fill_slots_launch(const FciParams &p, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s);
+// Sizes (elements) of the matvecs' staging tables: slot descriptors per alpha
+// string (uint64) and beta single targets per tile (uint32).
+int64_t slot_desc_count(const FciParams &p);
+int64_t slot_st_count(const FciParams &p);
+// Fills both tables (p needs the string tables); the matvecs stage a tile's
+// descriptors and targets from them with 16-byte loads.
+void slot_tables_launch(const FciParams &p, uint64_t *desc, uint32_t *st, cudaStream_t s);
 // y = H x from FP32 slot values, FP32 x/y and accumulation.
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s);
 // FP64 y = H x from the split slot values hi + lo; x32 is an FP32 copy of x.

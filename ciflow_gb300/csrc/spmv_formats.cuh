@@ -15,6 +15,12 @@ namespace cigpu {
 //     the term, so it accumulates in FP32 from an FP32 copy of x (x32), adding below
 //     2^-48 relative error while keeping FP64 instructions to one per element
 //     (GB300 issues FP64 at 1/64 of the FP32 rate).
+// Starts an L2 prefetch of `bytes` (a multiple of 16) at the 16-byte aligned `p`: a
+// bulk hint with nothing to wait for.
+__device__ __forceinline__ void l2_prefetch_bulk(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 template <typename VT>
 struct Plain {
     using X = VT;
@@ -27,6 +33,10 @@ struct Plain {
         VT v[4];
     };
     __device__ __forceinline__ void load4(int64_t at, Chunk &c) const;
+    // L2 prefetch of the values [at, at + n) (at and n multiples of 16 bytes' worth)
+    __device__ __forceinline__ void prefetch(int64_t at, int64_t n) const {
+        l2_prefetch_bulk(val + at, (uint32_t)(n * sizeof(VT)));
+    }
     __device__ __forceinline__ void zero(Chunk &c) const { c.v[0] = c.v[1] = c.v[2] = c.v[3] = 0; }
     __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
         a.s += c.v[j] * __ldg(x + col);
@@ -89,6 +99,10 @@ struct HiLo {
     __device__ __forceinline__ void load4(int64_t at, Chunk &c) const {
         c.h = __ldcs(reinterpret_cast<const float4 *>(hi + at));
         c.l = __ldcs(reinterpret_cast<const float4 *>(lo + at));
+    }
+    __device__ __forceinline__ void prefetch(int64_t at, int64_t n) const {
+        l2_prefetch_bulk(hi + at, (uint32_t)(n * sizeof(float)));
+        l2_prefetch_bulk(lo + at, (uint32_t)(n * sizeof(float)));
     }
     __device__ __forceinline__ void zero(Chunk &c) const { c.h = c.l = make_float4(0, 0, 0, 0); }
     __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
