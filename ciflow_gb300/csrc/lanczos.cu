@@ -233,20 +233,27 @@ __global__ void k_scale_to(const IT *__restrict__ t, int64_t n, const double *__
 // next basis slot as the preconditioned direction:
 //   ru = a0 r + a0 (E - theta) c + sum_i y_i (HV_i - theta V_i)   (FP32 arithmetic;
 //        r = H c - E c is the exact FP64 anchor residual)
-//   t  = ru / (theta - H_ii)                                      (guarded)
-// and the partial ||ru||^2 (FP64 block sums).
+//   t  = ru / (sigma - H_ii), sigma = min(theta, min_i H_ii)       (guarded)
+// and the partial ||ru||^2 (FP64 block sums). The shift is held at or below the
+// lowest diagonal element (*dmin) so that sigma - H_ii keeps one sign: with a start
+// far above the ground state (a warm start after a large orbital rotation, theta
+// 14 Eh high on a DOCI L=16 problem) theta - H_ii passes through zero on the
+// determinants whose diagonal lies near theta, the directions pile onto them, and
+// Davidson crawled (117 matvecs, residual 0.3); held, the same start converged in
+// 15. Near convergence theta lies below every H_ii and the shift is theta.
 __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__restrict__ r32,
                                                                 const float *__restrict__ c32,
                                                                 const float *__restrict__ V, const float *__restrict__ HV,
                                                                 int64_t ld, int k, const double *__restrict__ y,
                                                                 double a0, double a0_de, double theta,
+                                                                const double *__restrict__ dmin,
                                                                 const float *__restrict__ diag32, float *__restrict__ t,
                                                                 int64_t n, double *__restrict__ nrm,
                                                                 double *__restrict__ nrm_out, unsigned *__restrict__ ticket) {
     __shared__ float ys[kMaxBasis + 1];
     for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = (float)y[i];
     __syncthreads();
-    const float fa0 = (float)a0, fa0de = (float)a0_de, fth = (float)theta;
+    const float fa0 = (float)a0, fa0de = (float)a0_de, fth = (float)theta, fsig = (float)fmin(theta, *dmin);
     float acc = 0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         float ru = fa0 * r32[r] + fa0de * c32[r];
@@ -267,7 +274,7 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__r
             ru += ys[i] * (HV[o] - fth * V[o]);
         }
         acc += ru * ru;
-        float d = fth - diag32[r];  // FP32 (no per-element FP64 or conversion work)
+        float d = fsig - diag32[r];  // FP32 (no per-element FP64 or conversion work)
         if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
         t[r] = ru / d;
     }
@@ -284,11 +291,13 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__r
     reduce_in_last_block(nrm, 1, nrm_out, ticket);
 }
 
-// t = r / (E - H_ii) in FP32 (first direction after an anchor update).
+// t = r / (sigma - H_ii) in FP32 (first direction after an anchor update), sigma =
+// min(E, min_i H_ii) (*dmin): see the shift of k_dav_residual32.
 __global__ void k_precond32(const double *__restrict__ r, const double *__restrict__ diag, double E,
-                            float *__restrict__ t, int64_t n) {
+                            const double *__restrict__ dmin, float *__restrict__ t, int64_t n) {
+    const double sig = fmin(E, *dmin);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float d = (float)(E - diag[i]);
+        float d = (float)(sig - diag[i]);
         if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
         t[i] = (float)r[i] / d;
     }
@@ -331,8 +340,8 @@ __global__ void k_argmin_partial(const double *__restrict__ d, int64_t n, double
 }
 
 // One warp: the (value, index) minimum over the G block partials, ties to the lower
-// index; the index goes to pi[0].
-__global__ void k_argmin_final(const double *__restrict__ pv, int64_t *__restrict__ pi, int G) {
+// index; the index goes to pi[0] and the value to pv[0] (after every read of pv).
+__global__ void k_argmin_final(double *__restrict__ pv, int64_t *__restrict__ pi, int G) {
     double best = 1e308;
     int64_t bi = INT64_MAX;
     for (int b = threadIdx.x; b < G; b += 32)
@@ -348,7 +357,10 @@ __global__ void k_argmin_final(const double *__restrict__ pv, int64_t *__restric
             bi = oi;
         }
     }
-    if (threadIdx.x == 0) pi[0] = bi;
+    if (threadIdx.x == 0) {
+        pi[0] = bi;
+        pv[0] = best;
+    }
 }
 
 // v = e_at + keep * v with at = *pi (v holds a random vector on entry).
@@ -862,20 +874,25 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     dev_convert(P.diag, diag32.p, n, s);  // FP32 diagonal for the preconditioner
     DevBuf<double> yd(kMaxBasis + 1), dd(kMaxBasis + 2);
     int64_t mv32 = 0, mv64 = 0;
+    // the lowest diagonal element (value in pv[0], index in pi[0]): the preconditioner's
+    // shift bound and the cold start's determinant
+    DevBuf<double> pv(ops.G);
+    DevBuf<int64_t> pi(ops.G);
+    k_argmin_partial<<<ops.G, kVecThreads, 0, s>>>(P.diag, n, pv.p, pi.p);
+    k_argmin_final<<<1, 32, 0, s>>>(pv.p, pi.p, ops.G);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch(2);
+    const double *dmin = pv.p;
     if (!have_start) {
         // Krylov start. Davidson from the lowest-diagonal determinant alone can settle
         // on an excited state when that determinant overlaps the ground state weakly
         // (few electrons in many orbitals, strong two-electron terms). Instead take
         // q0 = e_argmin + g (g uniform random, |g| ~ 1), run kStartSteps FP32 Lanczos
         // steps with full reorthogonalisation, and start from the lowest Ritz vector.
-        DevBuf<double> pv(ops.G);
-        DevBuf<int64_t> pi(ops.G);
         dev_fill_random(c_dev, n, o.seed, s);
-        k_argmin_partial<<<ops.G, kVecThreads, 0, s>>>(P.diag, n, pv.p, pi.p);
-        k_argmin_final<<<1, 32, 0, s>>>(pv.p, pi.p, ops.G);
         k_add_unit_at<<<ops.G, kVecThreads, 0, s>>>(pi.p, std::sqrt(3.0 / (double)n), c_dev, n);
         CIGPU_CUDA(cudaGetLastError());
-        count_launch(3);
+        count_launch(1);
         const int m0 = (int)std::min<int64_t>(kStartSteps, std::min<int64_t>(n - 1, mmax + 1));
         constexpr int kCol = 44, kNrm = 100;  // out[] slots: T columns, norms (coefficients at 0)
         dev_convert(c_dev, V.p, n, s);
@@ -939,12 +956,12 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         float *hvnew = HV.p + (size_t)(k + 1) * n;
         // preconditioned direction into slot k+1 (and ||ru||^2 into SLOT_R)
         if (k == 0) {
-            k_precond32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, vnew, n);
+            k_precond32<<<ops.G, kVecThreads, 0, s>>>(ref.r.p, P.diag, E, dmin, vnew, n);
             count_launch();
         } else {
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
             k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(cr32.p + n, cr32.p, V.p, HV.p, n, k, yd.p, a0,
-                                                            a0 * (E - theta), theta, diag32.p, vnew, n, ops.partial.p,
+                                                            a0 * (E - theta), theta, dmin, diag32.p, vnew, n, ops.partial.p,
                                                             ops.out.p + SLOT_R, ops.ticket.p);
             count_launch();
         }
@@ -1005,8 +1022,11 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
             // restart direction: the previous Ritz vector p minus its component along
             // the current one u, in the basis [c, v_1..v_k] (coefficients (a0, y_i)),
             // formed with its H image in the spare slot k+1 before the anchor moves
+            // only a fold of a full basis keeps it: a fold at the FP32 floor of the
+            // correction restarts clean (the kept direction would carry that floor
+            // into the next cycle, and at tight tolerances the cycles then stall)
             bool keep = false;
-            if (kp >= 0 && kp <= k && !(rho_u <= 0.5 * o.tol) && tn2 > 1e-28) {
+            if (kp >= 0 && kp <= k && k >= mmax && !(rho_u <= std::max(0.5 * o.tol, floor)) && tn2 > 1e-28) {
                 double uu = a0 * a0, up = a0 * a0p;
                 for (int i = 1; i <= k; ++i) {
                     uu += y[i] * y[i];

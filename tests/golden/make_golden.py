@@ -137,6 +137,49 @@ def case_orbopt(name: str):
     print(name, json.dumps(meta))
 
 
+def case_warm_chain(name: str):
+    """A warm start far above the ground state: the oracle's annealing chain (the
+    reference's SimulatedAnnealing loop restated, DOCI L=16 8 pairs, seeded
+    integrals 4, chain seed 11, parameters 0.4/0.99/1.4/0.999) run to its 78th
+    decided step, whose proposal (a 73-degree rotation of orbitals 9 and 11) leaves
+    the current ground state 14 Eh above the new one. Saves the accepted rotations
+    before it, the proposal and the oracle's energies."""
+    import math
+    import orbopt as OO
+    from ciflow_gb300.synthetic import make_integrals
+    ints = make_integrals(16, 8, 8, nchol=16, seed=4)
+    opt = OO.Optimizer(ints, OO.O.DOCI, seed=11)
+    p = OO.AnnealParams()
+    prop = OO.SplitMix64(OO.stream_seed(opt.seed, 2 * opt.calls + 1))
+    temp, max_angle, e_old, decided, accepted = p.temp, p.max_angle, opt.e, 0, []
+    while True:
+        i, j = prop.below(opt.L), prop.below(opt.L)
+        if i == j:
+            continue
+        u1, u2 = prop.uniform(), prop.uniform()
+        angle = max_angle * (u1 - u2)
+        h2, e2 = OO.jacobi(opt.h, opt.eri, i, j, angle)
+        e_new, c_new = opt._solve(h2, e2)
+        if decided == 77:
+            meta = {"L": 16, "pairs": 8, "seed": 4, "nchol": 16, "accepted": accepted,
+                    "proposal": [i, j, angle], "e_current": e_old, "e_proposal": e_new}
+            break
+        accept = e_new < e_old
+        if not accept:
+            cost = math.exp((e_old - e_new) / temp)
+            accept = not (opt.acc.uniform() * (1 + cost) > cost)
+        if accept:
+            e_old = e_new
+            opt.h, opt.eri, opt.e, opt.c = h2, e2, e_new, c_new
+            accepted.append([i, j, angle])
+        decided += 1
+        temp *= p.change_temp
+        max_angle *= p.change_angle
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta)[:300])
+
+
 # Determinant-list CI (FCI_File): the reference's own test cases. BeH2 STO-3G with
 # the full 1225-determinant list of tests/data/fci_beh2_sto-3gdeterminants.dat
 # (TestDensity.cpp), Be cc-pVDZ with the 100-determinant GKCI list (TestDetFile.cpp:
@@ -246,12 +289,14 @@ def case_formats(name: str):
 
 
 if __name__ == "__main__":
-    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets", "formats"]
+    names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets", "formats", "warm_chain"]
     for nm in names:
         if nm == "formats":
             case_formats(nm)
         elif nm == "orbopt":
             case_orbopt(nm)
+        elif nm == "warm_chain":
+            case_warm_chain(nm)
         elif nm == "dets":
             case_dets(nm)
         elif nm == "beh2_sto3g":

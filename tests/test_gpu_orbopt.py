@@ -259,3 +259,30 @@ def test_python_mirror_and_current_hamiltonian():
     assert e_loc <= cim.get_ci_energy() + 1e-9 and cim.get_ci_energy() == pytest.approx(e_loc, abs=1e-9)
     with pytest.raises(ValueError):
         LocalMinimizer(FCI(Hamiltonian.from_integrals(make_integrals(6, 3, 3, nchol=8, seed=2))))
+
+
+def test_warm_start_far_above_the_ground_state():
+    """Step 78 of an annealing chain (tests/golden/warm_chain.json, made by the
+    oracle's chain): a 73-degree rotation leaves the current ground state 14 Eh
+    above the proposal's. Warm-started from it, both methods reach the proposal's
+    ground state (the oracle's energy) with converged residuals; the mixed method
+    keeps its preconditioner's shift at or below the lowest diagonal element, without
+    which its Davidson crawled to a stall at an excited energy."""
+    with open(os.path.join(GOLD, "warm_chain.json")) as f:
+        g = json.load(f)
+    H = Hamiltonian.from_integrals(make_integrals(g["L"], g["pairs"], g["pairs"], nchol=g["nchol"], seed=g["seed"]))
+    for i, j, a in g["accepted"]:
+        H = H.jacobi(int(i), int(j), float(a))
+    cur = DOCI(H, precision=A.FP64)
+    cur.solve(tol=1e-10)
+    assert abs(cur.get_ci_energy() - g["e_current"]) < 1e-8
+    c0 = cur.get_eigvec()
+    i, j, a = g["proposal"]
+    Hp = H.jacobi(int(i), int(j), float(a))
+    for prec in (A.MIXED, A.FP64):
+        m = DOCI(Hp, precision=prec)
+        m.solve(tol=1e-8, c0=c0)
+        assert m.info["status"] == A.OK, (prec, m.info)
+        assert abs(m.get_ci_energy() - g["e_proposal"]) < 1e-8, (prec, m.get_ci_energy(), g["e_proposal"])
+        # the start lies far above: a solver that settles near it has not found the ground state
+        assert m.info["matvecs_fp32"] + m.info["matvecs_fp64"] < 150
