@@ -133,16 +133,18 @@ __global__ void k_slot_st_table(const FciParams p, uint32_t *__restrict__ tab) {
     }
 }
 
-// Blocks per SM the register budget is set for (measured at L=10..12): 5 for the
-// FP32 matvec (48 registers; forcing 6 blocks at 40 registers lost ILP and ran 5%
-// slower); the hi/lo variant runs 2% faster held to 4 blocks (64 registers).
+// Blocks per SM the register budget is set for (measured at L=10..12): 6 for the
+// FP32 matvec (40 registers once its staging reads the precomputed tables; 2.4%
+// over 5 blocks at L=12, equal at L=11, 2% slower at L=10, and with 4 quads in
+// flight 5% slower everywhere); the hi/lo variant runs 2% faster held to 4 blocks
+// (64 registers).
 template <typename F>
 struct SlotOccupancy {
     static constexpr int kMinBlocks = 4;
 };
 template <>
 struct SlotOccupancy<Plain<float>> {
-    static constexpr int kMinBlocks = 5;
+    static constexpr int kMinBlocks = 6;
 };
 
 // 16-byte value loads in flight per lane: 3 for the FP32 matvec (2% over 2 at L=12;
