@@ -65,7 +65,7 @@ typedef struct {
     double gap;              /* estimated gap to the next Ritz value */
     int64_t matvecs_fp64;    /* FP64 matrix-vector products */
     int64_t matvecs_fp32;    /* FP32 matrix-vector products */
-    int32_t restarts;        /* thick restarts */
+    int32_t restarts;        /* thick restarts (FP64); MIXED: folds that kept the previous Ritz direction */
     int32_t corrections;     /* FP64 residual-correction cycles (MIXED) */
     int32_t converged;       /* 1 when residual <= tol */
     int32_t reserved;
