@@ -292,7 +292,7 @@ def run_cigpu(args, rank: int, world: int, dist):
     def summary(ms, tot, infos):
         srt = sorted(ms)
         de = [abs(i.e0 - golden["e0"]) for i in infos] if golden else []
-        return {"solves_per_s": world * len(ms) / tot, "ms_per_solve": statistics.mean(ms),
+        return {"solves_per_s": world * len(ms) / tot, "ms_per_solve": statistics.mean(ms), "step_ms": [round(x, 3) for x in ms],
                 "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(round(0.99 * (len(srt) - 1))))],
                 "max_abs_dE0": max(de) if de else None, "residual": max(i.residual for i in infos),
                 "matvecs_fp64": infos[-1].matvecs_fp64, "matvecs_fp32": infos[-1].matvecs_fp32,

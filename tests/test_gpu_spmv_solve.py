@@ -155,3 +155,20 @@ def test_solver_finds_the_ground_state(case, precision):
     cim = build(FCI, ints, precision)
     cim.solve(tol=1e-6)
     assert abs(cim.get_ci_energy() - ints.econst - e_ref) <= 1e-6
+
+
+def test_mixed_restart_keeps_the_previous_ritz_direction():
+    """L=11 4a4b (seeded integrals 1114, a request of the served mix): its Davidson
+    cycles of 30 vectors only halve the residual. Folds of the full basis keep the
+    previous Ritz direction (restarts > 0), and the mixed solve reaches the FP64
+    energy in fewer FP32 matvecs than the 165 it took restarting from the anchor
+    alone (plain Lanczos takes ~107 FP64 matvecs)."""
+    H = Hamiltonian.from_integrals(make_integrals(11, 4, 4, nchol=16, seed=1114))
+    ref = FCI(H, precision=A.FP64)
+    ref.solve(tol=1e-8)
+    m = FCI(H, precision=A.MIXED)
+    m.solve(tol=1e-5)  # the served stream's tolerance
+    assert m.info["status"] == A.OK and m.info["converged"] == 1
+    assert abs(m.get_ci_energy() - ref.get_ci_energy()) < 1e-6
+    assert m.info["restarts"] >= 1
+    assert m.info["matvecs_fp32"] < 150, m.info
