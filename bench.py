@@ -46,6 +46,8 @@ def parse_args():
                     help="served-stream requests per form (0 skips the served stream)")
     ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
+    ap.add_argument("--served-low-rates", type=float, nargs="*", default=[30.0, 100.0],
+                    help="further arrival rates (1/s) for latencies below saturation")
     ap.add_argument("--dets-orbitals", type=int, default=32,
                     help="orbitals of the CISD determinant-list section (0: skip); electrons per spin = L/4")
     ap.add_argument("--orbopt-steps", type=int, default=600,
@@ -373,7 +375,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         from ciflow_gb300.serve_bench import served as run_served
         barrier()
         served = run_served(args.served_requests, args.served_rate, args.served_inflight, tol_mixed=args.tol,
-                            tol_fp64=args.tol, seed=4 + rank)
+                            tol_fp64=args.tol, seed=4 + rank, extra_rates=tuple(args.served_low_rates))
         if dist is not None:
             tm, tp = reduce_over_ranks([served["mixed"]["solves_per_s"], served["plain_fp64"]["solves_per_s"]],
                                        dist, "sum")

@@ -121,8 +121,10 @@ def summarise(stream, results, wall):
 
 def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed: float = 1e-5,
            tol_fp64: float = 1e-5, tol_ref: float = 1e-8, every_big: int = 100, seed: int = 4,
-           ref_results=None):
-    """Both forms over the same stream; the tighter FP64 pass gives each request's E0."""
+           ref_results=None, extra_rates=()):
+    """Both forms over the same stream; the tighter FP64 pass gives each request's E0.
+    `extra_rates`: further arrival rates at which both forms run the same stream
+    again, for latencies below saturation (summaries under "by_rate")."""
     stream = make_stream(n, seed=seed, every_big=every_big)
     res_m, wall_m = run_stream(stream, A.MIXED, rate, tol_mixed, max_inflight, seed=seed)
     res_p, wall_p = run_stream(stream, A.FP64, rate, tol_fp64, max_inflight, seed=seed)
@@ -145,6 +147,18 @@ def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed:
         "plain_fp64": summarise(stream, res_p, wall_p) | {"max_abs_dE0": float(dp.max()), "tol": tol_fp64},
     }
     out["mixed_over_plain_solves_per_s"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    by_rate = {}
+    for r in extra_rates:
+        row = {}
+        for prec, tol, name in ((A.MIXED, tol_mixed, "mixed"), (A.FP64, tol_fp64, "plain_fp64")):
+            res, wall = run_stream(stream, prec, r, tol, max_inflight, seed=seed)
+            de = np.abs(np.array([x["e0"] for x in res]) - e_ref)
+            sm = summarise(stream, res, wall)
+            row[name] = {"solves_per_s": sm["solves_per_s"], "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"],
+                         "max_abs_dE0": float(de.max()), "failures": len(failures(res, de))}
+        by_rate[str(r)] = row
+    if by_rate:
+        out["by_rate"] = by_rate
     return out
 
 
