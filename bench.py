@@ -50,6 +50,7 @@ def parse_args():
                     help="further arrival rates (1/s) for latencies below saturation")
     ap.add_argument("--dets-orbitals", type=int, default=32,
                     help="orbitals of the CISD determinant-list section (0: skip); electrons per spin = L/4")
+    ap.add_argument("--doci", type=int, default=1, help="1: the DOCI L=24 12-pair section (0 skips it)")
     ap.add_argument("--orbopt-steps", type=int, default=600,
                     help="simulated-annealing steps of the orbital-optimisation section (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=512,
@@ -404,6 +405,13 @@ def run_cigpu(args, rank: int, world: int, dist):
         dets = run_dets(args.dets_orbitals, args.dets_orbitals // 4,
                         cpu_rows=20000 if (rank == 0 and world == 1) else 0)
 
+    # DOCI pair space, L=24 12 pairs: both forms' build + solve, matvec roofline and 1-RDM
+    doci = None
+    if args.doci:
+        from ciflow_gb300.doci_bench import run as run_doci
+        barrier()
+        doci = run_doci(args.tol, peak_gbs=peaks["hbm_gbs"])
+
     cpu = None
     if rank == 0 and world == 1:
         cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
@@ -429,6 +437,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "gpu_launches_plain": launches_plain,
         "clocks": clk.summary(),
         "served": served,
+        "doci": doci,
         "batched": batched,
         "orbopt": orbopt,
         "dets": dets,

@@ -44,46 +44,75 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+    // a row's bounds are loaded one row ahead, and its unaligned ends (at most 3
+    // elements each side, one per lane) with its first body chunks: short rows
+    // (DOCI: 145 elements) were a chain of dependent loads, bounds -> head ->
+    // body -> tail
+    int64_t s = 0, e = 0;
+    if (gid < n) {
+        s = __ldg(row_ptr + gid);
+        e = __ldg(row_ptr + gid + 1);
+    }
     for (int64_t r = gid; r < n; r += ng) {
-        if (m.skip(r)) continue;  // the same for the G lanes of the row
-        const int64_t s = row_ptr[r], e = row_ptr[r + 1];
-        typename F::Acc acc{};
-        // scalar head up to a 16-byte boundary of both arrays (4 elements)
-        const int64_t s4 = (s + 3) & ~(int64_t)3;
-        const int64_t head_end = s4 < e ? s4 : e;
-        if (s + lane < head_end) f.term1(s + lane, __ldcs(col + s + lane), acc);
-        const int64_t nb = (e > s4) ? ((e - s4) >> 2) : 0;
-        const uint4 *c4 = reinterpret_cast<const uint4 *>(col + s4);
-        for (int64_t b0 = 0; b0 < nb; b0 += G * U) {
-            uint4 c[U];
-            typename F::Chunk v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int64_t idx = b0 + u * G + lane;
-                if (idx < nb) {
-                    c[u] = __ldcs(c4 + idx);
-                    f.load4(s4 + (idx << 2), v[u]);
-                } else {
-                    c[u] = make_uint4(0, 0, 0, 0);
-                    f.zero(v[u]);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (b0 + u * G + lane < nb) {
-                    f.term(v[u], 0, c[u].x, acc);
-                    f.term(v[u], 1, c[u].y, acc);
-                    f.term(v[u], 2, c[u].z, acc);
-                    f.term(v[u], 3, c[u].w, acc);
-                }
-            }
+        const int64_t rn = r + ng;
+        int64_t sn = 0, en = 0;
+        if (rn < n) {
+            sn = __ldg(row_ptr + rn);
+            en = __ldg(row_ptr + rn + 1);
         }
-        // scalar tail (< 4 elements)
-        const int64_t t0 = s4 + (nb << 2);
-        if (e > s4 && t0 + lane < e) f.term1(t0 + lane, __ldcs(col + t0 + lane), acc);
+        if (!m.skip(r)) {  // the same for the G lanes of the row
+            typename F::Acc acc{};
+            const int64_t s4 = (s + 3) & ~(int64_t)3;
+            const int64_t head_end = s4 < e ? s4 : e;
+            const int64_t nb = (e > s4) ? ((e - s4) >> 2) : 0;
+            const int64_t t0 = s4 + (nb << 2);
+            const bool has_h = lane < 4 && s + lane < head_end;
+            const bool has_t = lane < 4 && e > s4 && t0 + lane < e;
+            uint32_t ch = 0, ct = 0;
+            typename F::Chunk vh, vt;
+            f.zero(vh);
+            f.zero(vt);
+            if (has_h) {
+                ch = __ldcs(col + s + lane);
+                f.load1(s + lane, vh);
+            }
+            if (has_t) {
+                ct = __ldcs(col + t0 + lane);
+                f.load1(t0 + lane, vt);
+            }
+            const uint4 *c4 = reinterpret_cast<const uint4 *>(col + s4);
+            for (int64_t b0 = 0; b0 < nb; b0 += G * U) {
+                uint4 c[U];
+                typename F::Chunk v[U];
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) f.reduce(acc, gmask, o);
-        if (lane == 0) y[r] = f.result(acc);
+                for (int u = 0; u < U; ++u) {
+                    const int64_t idx = b0 + u * G + lane;
+                    if (idx < nb) {
+                        c[u] = __ldcs(c4 + idx);
+                        f.load4(s4 + (idx << 2), v[u]);
+                    } else {
+                        c[u] = make_uint4(0, 0, 0, 0);
+                        f.zero(v[u]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (b0 + u * G + lane < nb) {
+                        f.term(v[u], 0, c[u].x, acc);
+                        f.term(v[u], 1, c[u].y, acc);
+                        f.term(v[u], 2, c[u].z, acc);
+                        f.term(v[u], 3, c[u].w, acc);
+                    }
+                }
+            }
+            if (has_h) f.term(vh, 0, ch, acc);
+            if (has_t) f.term(vt, 0, ct, acc);
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) f.reduce(acc, gmask, o);
+            if (lane == 0) y[r] = f.result(acc);
+        }
+        s = sn;
+        e = en;
     }
 }
 
@@ -101,14 +130,15 @@ int sm_count_spmv() {
     return sms;
 }
 
-// lanes per row from the mean row length (in 4-element chunks); the grid covers
+// lanes per row from the mean row length (in 4-element chunks: 32 lanes for FCI
+// rows of hundreds, 8 for the DOCI rows of ~36); the grid covers
 // the rows once (at most a full persistent grid), so a small matrix leaves SMs
 // free for the kernels of concurrent solves on other streams.
 template <typename F>
 static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const F &f,
                         typename F::X *y, cudaStream_t s) {
     const double chunks = n > 0 ? (double)nnz / n / 4.0 : 0;
-    const int G = chunks >= 48 ? 32 : chunks >= 20 ? 16 : 8;
+    const int G = chunks >= 48 ? 32 : 8;  // DOCI L=24 (36 chunks): 8 lanes 19% over 16
     const int64_t need = (n * G + kSpmvThreads - 1) / kSpmvThreads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(spmv_grid(), need));
     if (G == 32)

@@ -33,6 +33,8 @@ struct Plain {
         VT v[4];
     };
     __device__ __forceinline__ void load4(int64_t at, Chunk &c) const;
+    // one value into slot 0 of a chunk (the unaligned ends of a CRS row)
+    __device__ __forceinline__ void load1(int64_t at, Chunk &c) const { c.v[0] = __ldcs(val + at); }
     // L2 prefetch of the values [at, at + n) (at and n multiples of 16 bytes' worth)
     __device__ __forceinline__ void prefetch(int64_t at, int64_t n) const {
         l2_prefetch_bulk(val + at, (uint32_t)(n * sizeof(VT)));
@@ -99,6 +101,10 @@ struct HiLo {
     __device__ __forceinline__ void load4(int64_t at, Chunk &c) const {
         c.h = __ldcs(reinterpret_cast<const float4 *>(hi + at));
         c.l = __ldcs(reinterpret_cast<const float4 *>(lo + at));
+    }
+    __device__ __forceinline__ void load1(int64_t at, Chunk &c) const {
+        c.h.x = __ldcs(hi + at);
+        c.l.x = __ldcs(lo + at);
     }
     __device__ __forceinline__ void prefetch(int64_t at, int64_t n) const {
         l2_prefetch_bulk(hi + at, (uint32_t)(n * sizeof(float)));
