@@ -101,6 +101,8 @@ CONFIGS = {
     "c4": dict(method="FCI", L=10, nup=5, ndown=5, nchol=16, seed=4),
     # profiling size: same construction, CRS of a few GB (x larger than L1, CRS larger than L2)
     "p11": dict(method="FCI", L=11, nup=5, ndown=5, nchol=16, seed=11),
+    # DOCI profiling size: 184,756 pair determinants, an FP64 CRS of ~224 MB (larger than L2)
+    "p20": dict(method="DOCI", L=20, nup=10, ndown=10, nchol=24, seed=20),
 }
 
 
