@@ -53,7 +53,7 @@ bool parse_indices(const std::string &line, int nidx, int *idx, double *value) {
 
 void write_g(FILE *f, double v, int digits) { std::fprintf(f, "%.*g", digits, v); }
 
-std::string bits(const uint64_t *s, int words, int L) {
+std::string bits(const uint64_t *s, int L) {
     std::string out((size_t)L, '0');
     for (int o = 0; o < L; ++o)
         if ((s[o >> 6] >> (o & 63)) & 1) out[(size_t)(L - 1 - o)] = '1';
@@ -190,7 +190,7 @@ int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, i
     std::fprintf(f, "\n");
     int64_t count = 0;
     auto entry2 = [&](int64_t idx, const uint64_t *u, const uint64_t *d, int w, double v) {
-        std::fprintf(f, "%lld\t%s\t%s\t", (long long)idx, bits(u, w, L).c_str(), bits(d, w, L).c_str());
+        std::fprintf(f, "%lld\t%s\t%s\t", (long long)idx, bits(u, L).c_str(), bits(d, L).c_str());
         write_g(f, v, 16);
         std::fprintf(f, "\n");
     };
@@ -236,7 +236,7 @@ int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, i
         uint64_t s = nup ? (((uint64_t)1 << nup) - 1) : 0;
         for (int64_t idx = 0; idx < dim; ++idx) {
             if (std::fabs(c[idx]) >= threshold) {
-                std::fprintf(f, "%lld\t%s\t", (long long)idx, bits(&s, 1, L).c_str());
+                std::fprintf(f, "%lld\t%s\t", (long long)idx, bits(&s, L).c_str());
                 write_g(f, c[idx], 16);
                 std::fprintf(f, "\n");
                 ++count;

@@ -440,16 +440,6 @@ __global__ void __launch_bounds__(kVecThreads) k_residual(const double *__restri
     reduce_in_last_block(nrm, 1, nrm_out, ticket);
 }
 
-// Davidson-type diagonal preconditioner t = r / (E - H_ii), guarded away from 0.
-__global__ void k_precond(const double *__restrict__ r, const double *__restrict__ diag, double E,
-                          double *__restrict__ t, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double d = E - diag[i];
-        if (fabs(d) < 1e-2) d = d < 0 ? -1e-2 : 1e-2;
-        t[i] = r[i] / d;
-    }
-}
-
 __global__ void k_axpby64(double a, const double *__restrict__ x, double b, double *__restrict__ y, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = a * x[i] + b * y[i];
