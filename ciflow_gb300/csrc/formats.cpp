@@ -189,7 +189,7 @@ int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, i
     write_g(f, e0, 16);
     std::fprintf(f, "\n");
     int64_t count = 0;
-    auto entry2 = [&](int64_t idx, const uint64_t *u, const uint64_t *d, int w, double v) {
+    auto entry2 = [&](int64_t idx, const uint64_t *u, const uint64_t *d, double v) {
         std::fprintf(f, "%lld\t%s\t%s\t", (long long)idx, bits(u, L).c_str(), bits(d, L).c_str());
         write_g(f, v, 16);
         std::fprintf(f, "\n");
@@ -224,7 +224,7 @@ int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, i
         for (size_t a = 0; a < ua.size(); ++a)
             for (size_t b = 0; b < db.size(); ++b, ++idx)
                 if (std::fabs(c[idx]) >= threshold) {
-                    entry2(idx, &ua[a], &db[b], 1, c[idx]);
+                    entry2(idx, &ua[a], &db[b], c[idx]);
                     ++count;
                 }
         std::fprintf(f, "#Significant determinants: %lld of %lld\n#End vecoutput\n", (long long)count, (long long)dim);
@@ -257,7 +257,7 @@ int cigpu_write_civec(const char *path, int method, int L, int nup, int ndown, i
                      (long long)dim);
         for (int64_t idx = 0; idx < dim; ++idx)
             if (std::fabs(c[idx]) >= threshold) {
-                entry2(idx, up + idx * words, down + idx * words, words, c[idx]);
+                entry2(idx, up + idx * words, down + idx * words, c[idx]);
                 ++count;
             }
         std::fprintf(f, "#Significant determinants: %lld of %lld\n#End vecoutput\n", (long long)count, (long long)dim);
