@@ -55,3 +55,21 @@ def test_single_process_needs_no_group():
     import bench
     assert bench.reduce_over_ranks([4.0], None) == [4.0]
     assert bench.job_throughput(3, 1.5, 1, None) == (2.0, 1.5)
+
+
+def test_reference_arm_prints_its_line():
+    """`bench.py --impl reference` times the oracle's restatement of the reference
+    build and serial matvec on the host cores and prints one JSON line with the
+    contract's keys (the c0 workload and a one-second sample keep this short)."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--config", "c0",
+                          "--steps", "1", "--warmup", "0", "--cpu-seconds", "1"],
+                         capture_output=True, text=True, timeout=600, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([x for x in out.stdout.splitlines() if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["unit"] == "solves/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
