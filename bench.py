@@ -375,7 +375,7 @@ def run_cigpu(args, rank: int, world: int, dist):
     # problems, Poisson arrivals into the continuous-batching server, both forms
     served = None
     if args.served_requests > 0:
-        from ciflow_gb300.serve_bench import served as run_served
+        from benchmarks.serve_bench import served as run_served
         barrier()
         served = run_served(args.served_requests, args.served_rate, args.served_inflight, tol_mixed=args.tol,
                             tol_fp64=args.tol, seed=4 + rank, extra_rates=tuple(args.served_low_rates))
@@ -388,21 +388,21 @@ def run_cigpu(args, rank: int, world: int, dist):
     # batched uneven solves: one cigpu_solve_batch call against the same problems one at a time
     batched = None
     if args.batched_problems > 0:
-        from ciflow_gb300.batch_bench import run as run_batched
+        from benchmarks.batch_bench import run as run_batched
         barrier()
         batched = run_batched(args.batched_problems, seed=rank)
 
     # orbital optimisation: the optimisers' set_ham -> solve loop on the device
     orbopt = None
     if args.orbopt_steps > 0:
-        from ciflow_gb300.orbopt_bench import bench_section
+        from benchmarks.orbopt_bench import bench_section
         barrier()
         orbopt = bench_section(args.orbopt_steps, cpu_steps=20 if (rank == 0 and world == 1) else 0)
 
     # determinant lists (FCI_File / CI_Big): a CISD list, stored CRS and on-the-fly matvecs
     dets = None
     if args.dets_orbitals > 0:
-        from ciflow_gb300.dets_bench import run as run_dets
+        from benchmarks.dets_bench import run as run_dets
         barrier()
         dets = run_dets(args.dets_orbitals, args.dets_orbitals // 4,
                         cpu_rows=20000 if (rank == 0 and world == 1) else 0)
@@ -410,7 +410,7 @@ def run_cigpu(args, rank: int, world: int, dist):
     # DOCI pair space, L=24 12 pairs: both forms' build + solve, matvec roofline and 1-RDM
     doci = None
     if args.doci:
-        from ciflow_gb300.doci_bench import run as run_doci
+        from benchmarks.doci_bench import run as run_doci
         barrier()
         doci = run_doci(args.tol, peak_gbs=peaks["hbm_gbs"])
 

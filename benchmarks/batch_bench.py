@@ -6,7 +6,7 @@ The batch: L uniform in 6..12; FCI with 1..L/2 electrons per spin or DOCI with
 paths use the plain FP64 method, so they compute the same quantity; every result
 carries |dE0| between the two.
 
-    python -m ciflow_gb300.batch_bench --count 512
+    python -m benchmarks.batch_bench --count 512
 """
 from __future__ import annotations
 
@@ -18,8 +18,8 @@ from math import comb
 
 import numpy as np
 
-from . import _abi as A
-from .batch import random_problems, solve_batch
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.batch import random_problems, solve_batch
 
 
 def one_at_a_time(problems, tol: float):

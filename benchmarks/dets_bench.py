@@ -9,7 +9,7 @@ solves, and the CPU baseline: the oracle's restatement of the reference build
 (get_ham_element for every pair, OpenMP) timed on a bounded sample of rows and
 extrapolated.
 
-    python -m ciflow_gb300.dets_bench --L 32 --n 8
+    python -m benchmarks.dets_bench --L 32 --n 8
 """
 from __future__ import annotations
 
@@ -23,9 +23,9 @@ import time
 
 import numpy as np
 
-from . import _abi as A
-from .ciflow import CI_Big, FCI_File, Hamiltonian
-from .synthetic import make_integrals
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.ciflow import CI_Big, FCI_File, Hamiltonian
+from ciflow_gb300.synthetic import make_integrals
 
 
 def cisd_list(L: int, nup: int, ndown: int):

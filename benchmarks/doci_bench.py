@@ -6,7 +6,7 @@ and lowest-eigenpair solve (wall time through the C ABI, second of two runs), th
 matvec timed alone with CUDA events against its algorithmic bytes, the 1-RDM, and
 |dE0| against the reference's E0 (tests/golden/c2.json, from the reference CRS).
 
-    python -m ciflow_gb300.doci_bench
+    python -m benchmarks.doci_bench
 """
 from __future__ import annotations
 
@@ -17,8 +17,8 @@ import time
 
 import numpy as np
 
-from . import _abi as A
-from .synthetic import config_integrals
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.synthetic import config_integrals
 
 GOLDEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden", "c2.json")
 

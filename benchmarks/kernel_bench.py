@@ -1,7 +1,7 @@
 """Kernel microbenchmark: launch one hot kernel of the CI path a few times on a
 named configuration (used for profiler captures and roofline timing).
 
-    python -m ciflow_gb300.kernel_bench --config c4 --kernel spmv_f32 --reps 3
+    python -m benchmarks.kernel_bench --config c4 --kernel spmv_f32 --reps 3
 
 Kernels: spmv_f32, spmv_f64 (CRS matvec), build_f64, build_f32 (CRS build:
 count + fill passes), matvec_hilo (FP64 product from the FP32 hi + lo values of a mixed CRS),
@@ -31,8 +31,8 @@ def main() -> None:
 
     import torch
 
-    from . import _abi as A
-    from .synthetic import CONFIGS, config_integrals
+    from ciflow_gb300 import _abi as A
+    from ciflow_gb300.synthetic import CONFIGS, config_integrals
 
     lib = A.lib()
     cfg = CONFIGS[args.config]

@@ -12,7 +12,7 @@ build + eigensolve, LocalMinimizer.cpp:130-235). Arms:
 * ``warm``: every solve from the current eigenvector;
 * ``speculate=K``: warm, K proposals solved concurrently on K streams (same chain).
 
-    python -m ciflow_gb300.orbopt_bench --L 16 --pairs 8 --steps 200
+    python -m benchmarks.orbopt_bench --L 16 --pairs 8 --steps 200
 """
 from __future__ import annotations
 
@@ -21,9 +21,9 @@ import ctypes
 import json
 import time
 
-from . import _abi as A
-from .ciflow import Hamiltonian
-from .synthetic import make_integrals
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.ciflow import Hamiltonian
+from ciflow_gb300.synthetic import make_integrals
 
 
 def _create(ints, precision, warm, tol, seed):

@@ -11,7 +11,7 @@ requests. The same request list runs through the mixed FP32/FP64 form and the
 plain FP64 form; every mixed result carries |dE0| against the plain FP64 result
 of the same request, solved to a tighter tolerance.
 
-    python -m ciflow_gb300.serve_bench --rate 1000 --requests 300
+    python -m benchmarks.serve_bench --rate 1000 --requests 300
 """
 from __future__ import annotations
 
@@ -22,10 +22,10 @@ import time
 
 import numpy as np
 
-from . import _abi as A
-from .server import Server
-from .ciflow import unitary_exp
-from .synthetic import make_integrals
+from ciflow_gb300 import _abi as A
+from ciflow_gb300.server import Server
+from ciflow_gb300.ciflow import unitary_exp
+from ciflow_gb300.synthetic import make_integrals
 
 
 def rotation(L: int, sigma: float, seed: int) -> np.ndarray:

@@ -28,7 +28,7 @@ _D = ctypes.c_double
 class SolveInfo(ctypes.Structure):
     _fields_ = [("e0", _D), ("residual", _D), ("error_bound", _D), ("gap", _D),
                 ("matvecs_fp64", _I64), ("matvecs_fp32", _I64), ("restarts", ctypes.c_int32),
-                ("corrections", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("corrections", ctypes.c_int32), ("converged", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("seconds", _D)]
 
     def as_dict(self) -> dict:
@@ -98,7 +98,7 @@ SIGNATURES = {
     "cigpu_crs_layout": (_I, [_P, _P, _P]),
     "cigpu_crs_export_upper": (_I, [_P, _P, _P, _P]),
     "cigpu_crs_export_full": (_I, [_P, _P, _P, _P]),
-    "cigpu_mvprod": (_I, [_P, _P, _P]),
+    "cigpu_mvprod": (_I, [_P, _P, _P, _P]),
     "cigpu_mvprod_device": (_I, [_P, _P, _P, _I, _P]),
     "cigpu_solve": (_I, [_P, _D, _I64, _P, _P, _P]),
     "cigpu_rdm": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -214,7 +214,7 @@ class SparseMatrix_CRS_Sym:
         x = np.ascontiguousarray(x, dtype=np.float64)
         if y is None:
             y = np.empty(self.n)
-        A.check(A.lib().cigpu_mvprod(self.handle, A.ptr(x), A.ptr(y)), "cigpu_mvprod")
+        A.check(A.lib().cigpu_mvprod(self.handle, A.ptr(x), A.ptr(y), None), "cigpu_mvprod")
         return y
 
     def mvprod_device(self, x, y, stream=None) -> None:

@@ -209,11 +209,10 @@ static int64_t binom64(int n, int k) { return d_binom(n, k); }
 
 size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     int64_t dim, W;
+    dim = std::max<int64_t>(space_dim(method, L, nup, ndown), 0);
     if (method == CIGPU_DOCI) {
-        dim = binom64(L, nup);
         W = 1 + (int64_t)nup * (L - nup);
     } else {
-        dim = binom64(L, nup) * binom64(L, ndown);
         const int64_t sa = (int64_t)nup * (L - nup), sb = (int64_t)ndown * (L - ndown);
         W = 1 + sa + sb + sa * sb + binom64(nup, 2) * binom64(L - nup, 2) + binom64(ndown, 2) * binom64(L - ndown, 2);
     }
@@ -273,6 +272,7 @@ struct ExplicitFp32 {
 
 void build_crs(cigpu_crs &c, cudaStream_t s) {
     const auto t0 = std::chrono::steady_clock::now();
+    CIGPU_CUDA(cudaGetDevice(&c.device));
     Trace tr("build", s);
     cigpu_ham &h = *c.ham;
     const int64_t dim = c.dim;
@@ -476,6 +476,7 @@ int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, boo
     const int st = crs.precision == CIGPU_MIXED ? solve_mixed(P, o, c_dev, have_start, info)
                                                 : solve_fp64(P, o, c_dev, have_start, info);
     info.e0 += crs.ham->econst;
+    info.precision = crs.precision;
     return st;
 }
 
@@ -591,8 +592,7 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
     if (method == CIGPU_DOCI && ham->nup != ham->ndown) return CIGPU_EINVAL;
     if (method == CIGPU_DOCI && ham->nup > 32) return CIGPU_ENOTSUP;
     if (ham->L > kMaxL) return CIGPU_ENOTSUP;  // 64-bit strings; determinant lists go up to 128 orbitals
-    const int64_t dim = method == CIGPU_DOCI ? binom64(ham->L, ham->nup)
-                                             : binom64(ham->L, ham->nup) * binom64(ham->L, ham->ndown);
+    const int64_t dim = space_dim(method, ham->L, ham->nup, ham->ndown);
     if (dim < 1 || dim > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     CIGPU_TRY
     std::unique_ptr<cigpu_crs> c(new cigpu_crs);
@@ -698,10 +698,10 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
     CIGPU_CATCH
 }
 
-int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y) {
+int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y, cigpu_stream stream) {
     if (!crs || !x || !y) return CIGPU_EINVAL;
     CIGPU_TRY
-    cudaStream_t s = crs->stream;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : crs->stream;
     StreamScope scope(s);
     DevBuf<double> dx(crs->dim), dy(crs->dim);
     CIGPU_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * crs->dim, cudaMemcpyHostToDevice, s));

@@ -698,6 +698,7 @@ void solve_lockstep(std::vector<Item *> &items, double tol, cudaStream_t s, doub
             in.matvecs_fp64 = hmv[p] + 1;
             in.restarts = hrs[p];
             in.converged = hres[p] <= tol;
+            in.precision = CIGPU_FP64;
         }
         it.status = hres[p] <= tol ? CIGPU_OK : CIGPU_ENOCONV;
     }
@@ -730,13 +731,14 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 (q.precision != CIGPU_FP64 && q.precision != CIGPU_MIXED))
                 return CIGPU_EINVAL;
             if (q.method == CIGPU_DOCI && q.nup != q.ndown) return CIGPU_EINVAL;
+            if (q.L < 1 || q.L > kMaxL || q.nup < 0 || q.ndown < 0 || q.nup > q.L || q.ndown > q.L) return CIGPU_EINVAL;
             if (q.rot && (q.L < 1 || q.L > kMaxL || validate_rotation(q.L, q.rot) != CIGPU_OK)) return CIGPU_EINVAL;
             items[i].idx = i;
         }
         std::vector<int> small_idx, big_idx;
         for (int i = 0; i < count; ++i) {
             const cigpu_request &q = req[i];
-            items[i].dim = q.method == CIGPU_DOCI ? d_binom(q.L, q.nup) : d_binom(q.L, q.nup) * d_binom(q.L, q.ndown);
+            items[i].dim = space_dim(q.method, q.L, q.nup, q.ndown);
             (items[i].dim <= max_batched_dim ? small_idx : big_idx).push_back(i);
         }
         int hw = (int)std::thread::hardware_concurrency();

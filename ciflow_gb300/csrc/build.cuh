@@ -57,12 +57,38 @@ struct DociParams {
     float *val32lo;
 };
 
+// C(n, k) exactly while it fits in int64, else INT64_MAX (saturated). Each step
+// r <- r (n-k+i) / i is carried out as (r/g) ((n-k+i)/(i/g)) with g = gcd(r, i),
+// which is exact (i divides r (n-k+i)) and has no intermediate larger than the
+// result, so nothing overflows for any n (Hamiltonians go up to 128 orbitals).
 __host__ __device__ inline int64_t d_binom(int n, int k) {
     if (k < 0 || k > n) return 0;
     if (k > n - k) k = n - k;
-    int64_t r = 1;
-    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
-    return r;
+    uint64_t r = 1;
+    for (int i = 1; i <= k; ++i) {
+        uint64_t g = r, b = (uint64_t)i;
+        while (b) {
+            const uint64_t t = g % b;
+            g = b;
+            b = t;
+        }
+        const uint64_t a = r / g, m = (uint64_t)(n - k + i) / ((uint64_t)i / g);
+        if (a > (uint64_t)INT64_MAX / m) return INT64_MAX;
+        r = a * m;
+    }
+    return (int64_t)r;
+}
+
+// Determinants of an FCI space (alpha x beta strings) or a DOCI space (pair
+// strings); -1 for impossible electron counts or a count beyond int64.
+__host__ __device__ inline int64_t space_dim(int method, int L, int nup, int ndown) {
+    if (L < 0 || nup < 0 || ndown < 0 || nup > L || ndown > L) return -1;
+    const int64_t a = d_binom(L, nup);
+    if (a == INT64_MAX) return -1;
+    if (method == 1 /* CIGPU_DOCI */) return a;
+    const int64_t b = d_binom(L, ndown);
+    if (b == INT64_MAX || (b != 0 && a > INT64_MAX / b)) return -1;
+    return a * b;
 }
 
 // Position of the a-th (0-based) set bit of x.

@@ -10,6 +10,7 @@ struct cigpu_crs {
     int method = CIGPU_FCI, precision = CIGPU_FP64;
     int L = 0, nup = 0, ndown = 0;
     int64_t dim = 0, nnz_full = 0, nnz_upper = 0;
+    int device = -1;  // CUDA device the matrix lives on
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // FCI string tables (host copies kept for the RDM code)

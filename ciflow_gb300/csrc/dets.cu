@@ -766,6 +766,7 @@ int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up
     c->dim = ndet;
     c->det_words = W;
     c->onthefly = storage == CIGPU_DETS_ONTHEFLY;
+    CIGPU_CUDA(cudaGetDevice(&c->device));
     if (stream) {
         c->stream = static_cast<cudaStream_t>(stream);
     } else {

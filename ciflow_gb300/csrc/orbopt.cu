@@ -248,13 +248,6 @@ __global__ void __launch_bounds__(32 * kScanWarps) k_doci_pair_scan(int L, int N
 
 int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(sm_count() * 8, (n + kJacThreads - 1) / kJacThreads)); }
 
-int64_t binom_i64(int n, int k) {
-    if (k < 0 || k > n) return 0;
-    int64_t r = 1;
-    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
-    return r;
-}
-
 double seconds_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -779,8 +772,7 @@ int cigpu_orbopt_create(const cigpu_ham *ham, const cigpu_orbopt_config *cfg, ci
     if (cfg->method == CIGPU_DOCI && (ham->nup != ham->ndown || ham->L > 32)) return CIGPU_ENOTSUP;
     if (cfg->method == CIGPU_FCI && !ham->host_valid) return CIGPU_EINVAL;
     if (ham->L > kMaxL) return CIGPU_ENOTSUP;
-    const int64_t dim = cfg->method == CIGPU_DOCI ? binom_i64(ham->L, ham->nup)
-                                                  : binom_i64(ham->L, ham->nup) * binom_i64(ham->L, ham->ndown);
+    const int64_t dim = space_dim(cfg->method, ham->L, ham->nup, ham->ndown);
     if (dim < 1 || dim > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     try {
         const auto t0 = std::chrono::steady_clock::now();
@@ -896,7 +888,7 @@ int cigpu_orbopt_natural(cigpu_orbopt *opt, int density_method, double *e) {
             c.L = L;
             c.nup = c.ham->nup;
             c.ndown = c.ham->ndown;
-            c.dim = density_method == CIGPU_DOCI ? binom_i64(L, c.nup) : binom_i64(L, c.nup) * binom_i64(L, c.ndown);
+            c.dim = space_dim(density_method, L, c.nup, c.ndown);
             c.stream = opt->s;
             build_crs(c, opt->s);
             DevBuf<double> v(c.dim);

@@ -622,8 +622,11 @@ void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, doub
 // holds it (4 MiB) until the process exits. Host code must not take its name as
 // a device address; the address is looked up once per device with
 // cudaGetSymbolAddress (on the first call on that device, which should therefore
-// come before any stream capture). Every call shares the array and leaves its
-// contents behind: calls that overlap on the GPU race on it.
+// come before any stream capture) and kept for the life of the process, so it
+// does not survive a cudaDeviceReset of that device. The call runs on the current
+// device, which must be the one the CRS was built on (CIGPU_EINVAL otherwise).
+// Every call shares the array and leaves its contents behind: calls that overlap
+// on the GPU race on it.
 namespace cigpu {
 namespace {
 
@@ -667,6 +670,9 @@ extern "C" int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *r
     if (L2 > 1024) return CIGPU_ENOTSUP;
     const int G = (int)std::min<int64_t>(kNoAllocMaxBlocks, kNoAllocScratchBytes / (sizeof(double) * 2 * L2));
     if (G < 1) return CIGPU_ENOTSUP;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CIGPU_ECUDA;
+    if (dev != crs->device) return CIGPU_EINVAL;  // the matrix and the scratch must share a device
     double *scratch = nullptr;
     cudaError_t e = scratch_address(&scratch);
     if (e != cudaSuccess) {

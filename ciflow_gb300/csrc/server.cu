@@ -48,7 +48,7 @@ struct Request {
 };
 
 int64_t dim_of(int L, int nup, int ndown, int method) {
-    return method == CIGPU_DOCI ? cigpu::d_binom(L, nup) : cigpu::d_binom(L, nup) * cigpu::d_binom(L, ndown);
+    return cigpu::space_dim(method, L, nup, ndown);
 }
 
 // Host validation of a request at submit: sizes, and the same integral checks as
@@ -85,10 +85,18 @@ struct cigpu_server {
     std::vector<std::thread> workers;
 
     // Moves admissible requests from the queue to the ready list (mu held).
+    // A request that does not fit counts one bypass each time a later request is
+    // admitted ahead of it; once one has been passed kMaxBypass times, nothing
+    // behind it is admitted until it fits.
     void admit_locked() {
+        std::vector<Request *> waiting;  // earlier requests of this pass that did not fit
         for (auto it = queue.begin(); it != queue.end() && inflight < max_inflight;) {
             auto &q = *it;
             if (in_use + q->bytes <= budget) {
+                bool held = false;
+                for (Request *w : waiting) held = held || w->bypassed >= kMaxBypass;
+                if (held) break;
+                for (Request *w : waiting) ++w->bypassed;
                 in_use += q->bytes;
                 ++inflight;
                 ++admitted;
@@ -97,7 +105,7 @@ struct cigpu_server {
                 it = queue.erase(it);
                 cv_work.notify_one();
             } else {
-                if (++q->bypassed > kMaxBypass) break;  // let it drain to fit before others pass
+                waiting.push_back(q.get());
                 ++it;
             }
         }

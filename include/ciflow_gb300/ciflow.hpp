@@ -138,7 +138,7 @@ class SparseMatrix_CRS_Sym {
     int datasize() const { return (int)nnz_upper_; }
     int64_t nnz_full() const { return nnz_full_; }
     // y = H x with host buffers (SparseMatrix_CRS_Sym::mvprod, SparseMatrix_CRS.cpp:700-723)
-    void mvprod(const double *x, double *y) const { check(cigpu_mvprod(crs_.get(), x, y), "cigpu_mvprod"); }
+    void mvprod(const double *x, double *y) const { check(cigpu_mvprod(crs_.get(), x, y, nullptr), "cigpu_mvprod"); }
     // Element (i, j) of the symmetric matrix (SparseMatrix_CRS_Sym::operator()).
     double operator()(unsigned i, unsigned j) const {
         if (i > j) std::swap(i, j);

@@ -68,7 +68,8 @@ typedef struct {
     int32_t restarts;        /* thick restarts (FP64); MIXED: folds that kept the previous Ritz direction */
     int32_t corrections;     /* FP64 residual-correction cycles (MIXED) */
     int32_t converged;       /* 1 when residual <= tol */
-    int32_t reserved;
+    int32_t precision;       /* cigpu_precision the solve ran in (cigpu_solve_batch may
+                                run a problem in FP64 although MIXED was requested) */
     double seconds;          /* wall time of the solve */
 } cigpu_solve_info;
 
@@ -129,8 +130,9 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
  * (SparseMatrix_CRS.cpp:700-723; virtual at SparseMatrix_CRS.h:126).
  * Host buffers x, y of length dim; FP64 arithmetic (for a MIXED CRS the FP64
  * product uses the stored FP32 split of each value, v = hi + lo, exact to
- * 2^-48 relative). ---- */
-int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y);
+ * 2^-48 relative). The copies and the product run on `stream` (NULL: the CRS
+ * stream); the call returns when y is filled. ---- */
+int cigpu_mvprod(cigpu_crs *crs, const double *x, double *y, cigpu_stream stream);
 /* Device-buffer form on the given stream. dtype 0: FP64 x/y (FP64 matvec);
  * dtype 1: FP32 x/y (FP32 values, FP32 accumulation; MIXED CRS only). */
 int cigpu_mvprod_device(cigpu_crs *crs, const void *x, void *y, int dtype, cigpu_stream stream);
@@ -162,9 +164,11 @@ int cigpu_rdm(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa, do
  * library, so this call allocates nothing. crs must be a DOCI CRS with L <= 32
  * (CIGPU_ENOTSUP otherwise). c (dim) and the outputs, laid out as in cigpu_rdm,
  * are DEVICE buffers; the work is queued on `stream` (NULL: the CRS stream) and
- * the call returns without waiting. The first call on a device looks up the
- * array's device address; make it before any stream capture. Calls share the
- * array: calls that overlap on the GPU race, so serialise them. ---- */
+ * the call returns without waiting. Call it with the CRS's device current
+ * (CIGPU_EINVAL otherwise). The first call on a device looks up the array's
+ * device address and keeps it for the life of the process (it does not survive
+ * a cudaDeviceReset); make that first call before any stream capture. Calls
+ * share the array: calls that overlap on the GPU race, so serialise them. ---- */
 int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *rdm1, double *rdm2_aa, double *rdm2_ab,
                            double *rdm2_bb, cigpu_stream stream);
 

@@ -25,7 +25,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libcigpu_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libciflow_ref.so")
-REF_ROOT = os.environ.get("CIGPU_REFERENCE_ROOT", "/root/reference")
+# The CIFlow source tree the reference library is compiled from: CIGPU_REFERENCE_ROOT,
+# else the checkout location used where the fixtures were made. Only build_ref()
+# and the fixture generator read it; nothing on a GPU host needs it.
+REF_ROOT = os.environ.get("CIGPU_REFERENCE_ROOT") or "/root/reference"
 
 FCI, DOCI = 0, 1
 _P = ctypes.c_void_p

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the CIFlow reference.
 
-Run in a checkout where the reference tree is available (default
-/root/reference, override with CIGPU_REFERENCE_ROOT):
+Run where the reference tree is available (its location comes from
+oracle.REF_ROOT, i.e. CIGPU_REFERENCE_ROOT):
 
     python tests/golden/make_golden.py [names...]
 
@@ -288,10 +288,80 @@ def case_formats(name: str):
     print(name, {k: (len(v) if isinstance(v, str) else v) for k, v in out.items()})
 
 
+# CPU baseline calibration: the reference (oracle/_ref) against the oracle's
+# restatement (the port that runs on hosts without the reference tree), on the same
+# host with the same thread count, and ARPACK's matvec count at the reference's
+# settings (SparseMatrix_CRS::arpackDiagonalize, SparseMatrix_CRS.cpp:360-481:
+# which='SA', ncv=42, tol=0, maxiter=3n) driving the reference's own serial
+# Sym::mvprod. For c0/c4/c2 the whole reference solve (constructor + ARPACK loop) is
+# also timed end to end.
+def _median_time(f, reps: int) -> float:
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        f()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+def case_calibration(name: str, cfgs=("c0", "c4", "c2", "c1")):
+    import platform
+
+    import scipy.sparse.linalg as sla
+    threads = len(os.sched_getaffinity(0))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    path = os.path.join(OUT, f"{name}.json")
+    meta = json.load(open(path)) if os.path.exists(path) else {}
+    meta.update({"host": platform.machine(), "cpu": platform.processor() or platform.machine(), "threads": threads})
+    for cfg_name in cfgs:
+        cfg = CONFIGS[cfg_name]
+        method = O.FCI if cfg["method"] == "FCI" else O.DOCI
+        ints = config_integrals(cfg_name)
+        t0 = time.perf_counter()
+        r = O.RefCI(method, ints=ints)
+        t_ref_build = time.perf_counter() - t0
+        n = int(r.lib.ref_ci_dim(r.h))
+        t0 = time.perf_counter()
+        off, col, val = O.build_rows(method, ints, 0, n)
+        t_port_build = time.perf_counter() - t0
+        x = np.random.default_rng(0).standard_normal(n)
+        y = np.zeros(n)
+        reps = 3 if n > 200000 else 10
+        t_port_mv = _median_time(lambda: O.sym_mvprod_rows(0, off, col, val, x, y), reps)
+        del off, col, val
+        t_ref_mv = _median_time(lambda: r.mvprod(x), reps)
+        count = [0]
+
+        def mv(v):
+            count[0] += 1
+            return r.mvprod(v)
+
+        v0 = np.random.default_rng(12345).standard_normal(n)
+        op = sla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+        t0 = time.perf_counter()
+        w, _ = sla.eigsh(op, k=1, which="SA", ncv=min(42, n - 1), tol=0, maxiter=3 * n, v0=v0)
+        t_eig = time.perf_counter() - t0
+        r.close()
+        rec = {"dim": n, "ref_build_s": t_ref_build, "port_build_s": t_port_build,
+               "ref_mvprod_s": t_ref_mv, "port_mvprod_s": t_port_mv,
+               "build_ratio_ref_over_port": t_ref_build / t_port_build,
+               "mvprod_ratio_ref_over_port": t_ref_mv / t_port_mv,
+               "arpack_matvecs": count[0], "arpack_s": t_eig, "e0": float(w[0]) + ints.econst,
+               "ref_solve_s": t_ref_build + t_eig}
+        meta[cfg_name] = rec
+        with open(path, "w") as f:
+            json.dump(meta, f, indent=1)
+        print(cfg_name, json.dumps(rec), flush=True)
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets", "formats", "warm_chain"]
     for nm in names:
-        if nm == "formats":
+        if nm == "calibration":
+            case_calibration(nm)
+        elif nm.startswith("calibration:"):
+            case_calibration("calibration", tuple(nm.split(":", 1)[1].split(",")))
+        elif nm == "formats":
             case_formats(nm)
         elif nm == "orbopt":
             case_orbopt(nm)
