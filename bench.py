@@ -42,6 +42,8 @@ def parse_args():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--tol", type=float, default=1e-5, help="FP64 residual target (|dE0| ~ tol^2/gap)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--cpu-full-solve", type=int, default=1,
+                    help="1: also time one whole CPU solve of L=10 5a5b end to end (about 20 s)")
     ap.add_argument("--served-requests", type=int, default=200,
                     help="served-stream requests per form (0 skips the served stream)")
     ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
@@ -51,6 +53,8 @@ def parse_args():
     ap.add_argument("--dets-orbitals", type=int, default=32,
                     help="orbitals of the CISD determinant-list section (0: skip); electrons per spin = L/4")
     ap.add_argument("--doci", type=int, default=1, help="1: the DOCI L=24 12-pair section (0 skips it)")
+    ap.add_argument("--rdm", type=int, default=1,
+                    help="1: RDMs of the mixed ground state, timed, with their errors against the oracle (0 skips)")
     ap.add_argument("--orbopt-steps", type=int, default=600,
                     help="simulated-annealing steps of the orbital-optimisation section (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=512,
@@ -153,10 +157,30 @@ def job_throughput(units_per_rank: float, seconds: float, world: int, dist, devi
     return world * units_per_rank / slowest, slowest
 
 
-def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float, n_matvec: int) -> dict:
-    """The CPU implementation of the path (the oracle's restatement of the reference
-    build and serial Sym::mvprod), timed on a bounded sample of rows and
-    extrapolated to one full solve: t = t_build + n_matvec * t_mvprod."""
+def calibration(cfg_name: str) -> dict | None:
+    """The committed calibration of the oracle port against the reference itself
+    (tests/golden/calibration.json, made by tests/golden/make_golden.py on a host
+    with the reference tree): reference/port time ratios of the build and of the
+    serial Sym::mvprod at the same thread count, and ARPACK's matvec count at the
+    reference's settings (which='SA', ncv=42, tol=0) driving the reference mvprod."""
+    p = os.path.join(ROOT, "tests", "golden", "calibration.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    if cfg_name not in d:
+        return None
+    rec = dict(d[cfg_name])
+    rec.update({"host": d.get("host"), "threads": d.get("threads")})
+    return rec
+
+
+def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float) -> dict:
+    """The reference CPU solve of the workload, estimated from the oracle port (the
+    restatement of the reference build and serial Sym::mvprod) timed on a bounded
+    sample of rows on these host cores and calibrated by the committed
+    reference/port ratios: t = k_build t_build + n_arpack k_mv t_mvprod, with
+    n_arpack the reference ARPACK run's matvec count."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
@@ -164,6 +188,7 @@ def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float, n_matvec: i
     method = O.DOCI if CONFIGS[cfg_name]["method"] == "DOCI" else O.FCI
     n = O.dim(method, ints.L, ints.nup, ints.ndown)
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    t_start = time.perf_counter()
     # size the sample from a short probe
     probe = max(200, min(n, 2000))
     t0 = time.perf_counter()
@@ -182,13 +207,187 @@ def cpu_baseline(cfg_name: str, ints, threads: int, target_s: float, n_matvec: i
     frac = rows / n
     full_build = t_build / frac
     full_mv = t_mv / frac
-    t_solve = full_build + n_matvec * full_mv
+    cal = calibration(cfg_name)
+    if cal:
+        n_mv, k_b, k_mv = cal["arpack_matvecs"], cal["build_ratio_ref_over_port"], cal["mvprod_ratio_ref_over_port"]
+    else:  # no calibration: the port as measured and ARPACK's count unknown
+        n_mv, k_b, k_mv = 105, 1.0, 1.0
+    t_solve = k_b * full_build + n_mv * k_mv * full_mv
     return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": threads, "kind": "port",
-            "sample": (f"rows {stride_start}..{stride_start + rows} of {n} ({100 * frac:.2f}%): build "
-                       f"{t_build:.2f}s with {threads} threads (reference build_parallel algorithm, sorted "
-                       f"row insertion), serial Sym::mvprod {t_mv:.3f}s; extrapolated full build "
-                       f"{full_build:.1f}s + {n_matvec} matvecs x {full_mv:.2f}s"),
-            "extrapolated_build_s": full_build, "extrapolated_mvprod_s": full_mv}
+            "sample": (f"rows {stride_start}..{stride_start + rows} of {n} ({100 * frac:.2f}%): port build "
+                       f"{t_build:.2f}s with {threads} threads (the reference build_parallel algorithm with sorted "
+                       f"row insertion), serial Sym::mvprod {t_mv:.3f}s; full solve = {k_b:.2f} x {full_build:.1f}s "
+                       f"build + {n_mv} ARPACK matvecs x {k_mv:.3f} x {full_mv:.2f}s"),
+            "extrapolated_build_s": full_build, "extrapolated_mvprod_s": full_mv,
+            "solve_s_estimate": t_solve, "port_uncalibrated_solve_s": full_build + n_mv * full_mv,
+            "arpack_matvecs": n_mv,
+            "calibration": ({"build_ratio_ref_over_port": k_b, "mvprod_ratio_ref_over_port": k_mv,
+                             "measured_on": f"{cal['host']}, {cal['threads']} threads",
+                             "source": "tests/golden/calibration.json"} if cal else None),
+            "sample_wall_s": time.perf_counter() - t_start}
+
+
+def cpu_full_solve(cfg_name: str, threads: int) -> dict:
+    """One whole CPU solve, measured end to end, not extrapolated: the oracle port's
+    build (all threads) and ARPACK (scipy eigsh, which='SA', ncv=42, tol=0, as
+    SparseMatrix_CRS::arpackDiagonalize) driving the port's serial Sym::mvprod."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import scipy.sparse.linalg as sla
+    import oracle as O
+    from ciflow_gb300.synthetic import CONFIGS, config_integrals
+    cfg = CONFIGS[cfg_name]
+    method = O.DOCI if cfg["method"] == "DOCI" else O.FCI
+    ints = config_integrals(cfg_name)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    m = O.build_upper(method, ints)
+    t_build = time.perf_counter() - t0
+    count = [0]
+
+    def mv(v):
+        count[0] += 1
+        return O.sym_mvprod(m, v)
+
+    n = m.n
+    op = sla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+    t1 = time.perf_counter()
+    w, _ = sla.eigsh(op, k=1, which="SA", ncv=min(42, n - 1), tol=0, maxiter=3 * n,
+                     v0=np.random.default_rng(12345).standard_normal(n))
+    t_eig = time.perf_counter() - t1
+    out = {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b ({n} determinants)",
+           "solve_s": t_build + t_eig, "build_s": t_build, "eigensolve_s": t_eig, "matvecs": count[0],
+           "cores": threads, "kind": "port", "e0": float(w[0]) + ints.econst}
+    gpath = os.path.join(ROOT, "tests", "golden", f"{cfg_name}.json")
+    if os.path.exists(gpath):
+        with open(gpath) as f:
+            out["abs_dE0_vs_reference"] = abs(out["e0"] - json.load(f)["e0"])
+    cal = calibration(cfg_name)
+    if cal:
+        out["reference_solve_s_measured_at_calibration"] = cal["ref_solve_s"]
+        out["port_solve_s_at_calibration"] = cal["port_build_s"] + cal["arpack_matvecs"] * cal["port_mvprod_s"]
+    return out
+
+
+def small_solves(lib, cfg_name: str, tol: float, reps: int = 5) -> dict:
+    """Whole solves of a small configuration on the GPU through the C ABI with host
+    buffers (create + build + solve + eigenvector to the host), both forms, median of
+    `reps` after one warm-up: the GPU side of the measured whole CPU solve."""
+    import numpy as np
+
+    from ciflow_gb300 import _abi as A
+    from ciflow_gb300.synthetic import CONFIGS, config_integrals
+    cfg = CONFIGS[cfg_name]
+    ints = config_integrals(cfg_name)
+    method = A.DOCI if cfg["method"] == "DOCI" else A.FCI
+    h, eri = np.ascontiguousarray(ints.h), np.ascontiguousarray(ints.eri)
+    golden = load_golden(cfg_name)
+    out = {}
+    for prec, name in ((A.MIXED, "mixed"), (A.FP64, "plain_fp64")):
+        ts, e = [], None
+        for i in range(reps + 1):
+            t0 = time.perf_counter()
+            ham, crs = ctypes.c_void_p(), ctypes.c_void_p()
+            A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri),
+                                         ctypes.byref(ham)))
+            A.check(lib.cigpu_build(ham, method, prec, None, ctypes.byref(crs)))
+            dim = ctypes.c_int64()
+            lib.cigpu_crs_dims(crs, ctypes.byref(dim), None, None)
+            c = np.empty(dim.value)
+            info = A.SolveInfo()
+            st = lib.cigpu_solve(crs, tol, 0, None, A.ptr(c), ctypes.byref(info))
+            lib.cigpu_crs_destroy(crs)
+            lib.cigpu_ham_destroy(ham)
+            if st not in (A.OK, A.ENOCONV):
+                A.check(st, "cigpu_solve")
+            if i:
+                ts.append(time.perf_counter() - t0)
+            e = info.e0
+        out[name] = {"solve_s": statistics.median(ts), "e0": e,
+                     "abs_dE0_vs_reference": abs(e - golden["e0"]) if golden else None}
+    return out
+
+
+def config_dict(args, cfg: dict, golden: dict | None, world: int) -> dict:
+    """The workload description both arms print (identical for the same config)."""
+    return {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b "
+                        f"({golden['dim'] if golden else '?'} determinants)",
+            "name": args.config, **cfg, "tol_residual": args.tol,
+            "l2": "inputs larger than L2 (CRS of ~1.55e9 nonzeros, 12-19 GB)" if args.config == "c1" else "n/a",
+            "parallelism": f"replicas x{world}"}
+
+
+def load_golden(name: str) -> dict | None:
+    gpath = os.path.join(ROOT, "tests", "golden", f"{name}.json")
+    if os.path.exists(gpath):
+        with open(gpath) as f:
+            return json.load(f)
+    return None
+
+
+def rdm_section(lib, ham, method: int, ints, cfg_name: str, tol: float, stream, reps: int = 3,
+                check: bool = True) -> dict:
+    """1-RDM and 2-RDM of the mixed ground state through cigpu_rdm (host c in, host
+    RDMs out), timed with CUDA events on the CRS stream, and their errors against the
+    oracle: the oracle's restatement of DensFCI/DensDOCI on the same vector (kernel
+    parity) and, where the fixture holds them, the RDMs of the reference's own FP64
+    ARPACK ground state (error of the mixed state), with |E_dens - E_CI|."""
+    import numpy as np
+    import torch
+
+    from ciflow_gb300 import _abi as A
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    crs = ctypes.c_void_p()
+    A.check(lib.cigpu_build(ham, method, A.MIXED, sh, ctypes.byref(crs)))
+    dim = ctypes.c_int64()
+    lib.cigpu_crs_dims(crs, ctypes.byref(dim), None, None)
+    c = np.empty(dim.value)
+    info = A.SolveInfo()
+    st = lib.cigpu_solve(crs, tol, 0, None, A.ptr(c), ctypes.byref(info))
+    if st not in (A.OK, A.ENOCONV):
+        A.check(st, "cigpu_solve")
+    L = ints.L
+    np_ = L * (L - 1) // 2
+    two = method == A.FCI or L <= 32
+    r1 = np.empty((2, L, L))
+    aa, ab, bb = np.empty((np_, np_)), np.empty((L * L, L * L)), np.empty((np_, np_))
+    outs = (A.ptr(r1), A.ptr(aa), A.ptr(ab), A.ptr(bb)) if two else (A.ptr(r1), None, None, None)
+    ms = []
+    for i in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        A.check(lib.cigpu_rdm(crs, A.ptr(c), *outs), "cigpu_rdm")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i:  # the first call warms the allocator cache
+            ms.append(e0.elapsed_time(e1))
+    lib.cigpu_crs_destroy(crs)
+    out = {"state": "mixed ground state", "e0": info.e0, "residual": info.residual,
+           "rdms": "1-RDM + 2-RDM (aa, ab, bb)" if two else "1-RDM",
+           "ms_per_call": statistics.median(ms), "ms_all": [round(x, 3) for x in ms],
+           "path": "cigpu_rdm with host c and host outputs (H2D of c and D2H of the RDMs included)"}
+    if not check:
+        return out
+    # the oracle as the checker (after the timed calls)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    t0 = time.perf_counter()
+    ref = O.rdm(O.FCI if method == A.FCI else O.DOCI, L, ints.nup, ints.ndown, c)
+    out["oracle_s"] = time.perf_counter() - t0
+    got = (r1, aa, ab, bb)
+    names = ("rdm1", "rdm2_aa", "rdm2_ab", "rdm2_bb") if two else ("rdm1",)
+    out["max_abs_err_vs_oracle_same_vector"] = {n: float(np.abs(g - r).max()) for n, g, r in zip(names, got, ref)}
+    if two:
+        out["abs_E_dens_minus_E_ci"] = abs(O.dens_energy(ints, r1, aa, ab, bb) - info.e0)
+    npz = os.path.join(ROOT, "tests", "golden", f"{cfg_name}.npz")
+    if os.path.exists(npz):
+        g = np.load(npz)
+        keys = {"rdm1": "rdm1", "rdm2_aa": "aa", "rdm2_ab": "ab", "rdm2_bb": "bb"}
+        errs = {n: float(np.abs(x - g[keys[n]]).max()) for n, x in zip(names, got) if keys[n] in g}
+        if errs:
+            out["max_abs_err_vs_reference_fp64_state"] = errs
+    return out
 
 
 def host_threads() -> int:
@@ -201,29 +400,36 @@ def host_threads() -> int:
 # ---------------------------------------------------------------------------
 def run_reference(args, rank: int, world: int):
     """--impl reference: the reference CPU implementation of the path on the host
-    cores (the oracle port of the reference build + serial matvec, all threads),
-    rank 0 only."""
+    cores, rank 0 only. Each step is a bounded sample of the workload (the oracle
+    port's build of a slice of rows with all threads, and the serial matvec over
+    it); the value is the full solve those samples give, calibrated against the
+    reference itself (ARPACK's matvec count and the reference/port time ratios,
+    tests/golden/calibration.json). One whole L=10 5a5b solve is also measured end
+    to end without extrapolation."""
     if rank != 0:
         return
     from ciflow_gb300.synthetic import CONFIGS, config_integrals
     ints = config_integrals(args.config)
     threads = host_threads()
-    # matvec count of a Lanczos solve of this problem to the same residual target (1e-5):
-    # the plain FP64 arm's count on the GPU (the reference's ARPACK runs to tol=0,
-    # machine precision, and needs more)
-    n_mv = {"c1": 105, "c4": 62, "c2": 120}.get(args.config, 105)
-    vals = []
+    vals, walls = [], []
     for _ in range(args.warmup):
-        cpu_baseline(args.config, ints, threads, min(args.cpu_seconds, 4.0), n_mv)
+        cpu_baseline(args.config, ints, threads, min(args.cpu_seconds, 4.0) / 2)
     for _ in range(args.steps):
-        vals.append(cpu_baseline(args.config, ints, threads, args.cpu_seconds / 2, n_mv))
+        t0 = time.perf_counter()
+        vals.append(cpu_baseline(args.config, ints, threads, args.cpu_seconds / 2))
+        walls.append(time.perf_counter() - t0)
     v = statistics.median([b["value"] for b in vals])
+    full = cpu_full_solve("c4", threads) if args.cpu_full_solve else None
     cfg = CONFIGS[args.config]
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(walls),
+           "ms_per_solve_estimate": 1000.0 / v, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals)",
-           "config": {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b", **cfg},
+           "config": config_dict(args, cfg, load_golden(args.config), world),
+           "step": "one bounded sample of the solve (build of a slice of rows + serial matvec over it); "
+                   "value = the full solve the sample gives, calibrated against the reference",
            "cpu_baseline": {**vals[-1], "value": v},
+           "cpu_full_solve_c4": full,
            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -371,6 +577,12 @@ def run_cigpu(args, rank: int, world: int, dist):
            "h2d_bytes_per_step": int(h.nbytes + eri.nbytes), "d2h_bytes_per_step": int(c_host.nbytes),
            "path": "cigpu_ham_create + cigpu_build(MIXED) + cigpu_solve(c_out host), pageable host buffers"}
 
+    # RDMs of the mixed ground state: time through the C ABI, errors against the oracle
+    rdm = None
+    if args.rdm:
+        barrier()
+        rdm = rdm_section(lib, ham, method, ints, args.config, args.tol, stream, check=(rank == 0))
+
     # served stream: L=10 5a5b FCI under random orbital rotations mixed with uneven
     # problems, Poisson arrivals into the continuous-batching server, both forms
     served = None
@@ -412,11 +624,22 @@ def run_cigpu(args, rank: int, world: int, dist):
     if args.doci:
         from benchmarks.doci_bench import run as run_doci
         barrier()
-        doci = run_doci(args.tol, peak_gbs=peaks["hbm_gbs"])
+        checker = None
+        if rank == 0:  # RDM errors against the oracle, after the timed calls
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle as O
+            checker = O.rdm
+        doci = run_doci(args.tol, peak_gbs=peaks["hbm_gbs"], rdm_checker=checker)
+
+    # the same L=10 5a5b problem the CPU solves whole below, on the GPU (C ABI, host buffers)
+    small = small_solves(lib, "c4", args.tol) if args.cpu_full_solve else None
 
     cpu = None
     if rank == 0 and world == 1:
-        cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds, plain["matvecs_fp64"])
+        cpu = cpu_baseline(args.config, ints, host_threads(), args.cpu_seconds)
+        if args.cpu_full_solve:
+            cpu["full_solve_c4"] = cpu_full_solve("c4", host_threads())
+            cpu["full_solve_c4"]["gpu_same_problem"] = small
 
     lib.cigpu_ham_destroy(ham)
     if rank != 0:
@@ -426,11 +649,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["ms_per_solve"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)",
         "data": "synthetic (seeded integrals, no dataset)",
-        "config": {"workload": f"{cfg['method']} L={cfg['L']} {cfg['nup']}a{cfg['ndown']}b "
-                               f"({golden['dim'] if golden else '?'} determinants)",
-                   "name": args.config, **cfg, "tol_residual": args.tol,
-                   "l2": "inputs larger than L2 (CRS of ~1.55e9 nonzeros, 12-19 GB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": config_dict(args, cfg, golden, world),
         "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"],
         "mixed": mixed, "plain_fp64": plain,
         "mixed_over_plain": mixed["solves_per_s"] / plain["solves_per_s"],
@@ -438,6 +657,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "e2e": e2e, "gpu_launches": launches_mixed,
         "gpu_launches_plain": launches_plain,
         "clocks": clk.summary(),
+        "rdm": rdm,
         "served": served,
         "doci": doci,
         "batched": batched,

@@ -23,7 +23,10 @@ from ciflow_gb300.synthetic import config_integrals
 GOLDEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden", "c2.json")
 
 
-def run(tol: float = 1e-5, reps: int = 20, peak_gbs: float | None = None) -> dict:
+def run(tol: float = 1e-5, reps: int = 20, peak_gbs: float | None = None, rdm_checker=None) -> dict:
+    """rdm_checker(method, L, nup, ndown, c) -> (rdm1, aa, ab, bb): the oracle's RDMs,
+    given by the caller; the 1-RDM of each form is then compared with it on the
+    same vector and with the reference's own 1-RDM of its FP64 ground state."""
     import torch  # device buffers and CUDA events for the matvec timing
 
     lib = A.lib()
@@ -86,10 +89,24 @@ def run(tol: float = 1e-5, reps: int = 20, peak_gbs: float | None = None) -> dic
             if peak_gbs:
                 row["matvec"]["frac_of_peak"] = nbytes / t / 1e9 / peak_gbs
             rdm1 = np.empty((2, ints.L, ints.L))
-            t0 = time.perf_counter()
-            A.check(lib.cigpu_rdm(crs, A.ptr(c), A.ptr(rdm1), None, None, None), "cigpu_rdm")
-            row["rdm1_s"] = time.perf_counter() - t0
+            ms = []
+            for i in range(4):  # the first call warms the allocator cache
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                A.check(lib.cigpu_rdm(crs, A.ptr(c), A.ptr(rdm1), None, None, None), "cigpu_rdm")
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                if i:
+                    ms.append(ev0.elapsed_time(ev1))
+            row["rdm1_ms"] = float(np.median(ms))
             row["rdm1_trace"] = float(rdm1[0].trace() + rdm1[1].trace())
+            if rdm_checker is not None:
+                ref = rdm_checker(1, ints.L, ints.nup, ints.ndown, c)
+                row["rdm1_max_abs_err_vs_oracle_same_vector"] = float(np.abs(rdm1 - ref[0]).max())
+            gnpz = GOLDEN[:-5] + ".npz"
+            if os.path.exists(gnpz):
+                row["rdm1_max_abs_err_vs_reference_fp64_state"] = float(np.abs(rdm1 - np.load(gnpz)["rdm1"]).max())
             lib.cigpu_crs_destroy(crs)
             out[name] = row
         m, p = out["mixed"], out["plain_fp64"]

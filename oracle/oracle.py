@@ -388,6 +388,22 @@ def ref_jacobi(ints, rotations):
     return h, eri, U
 
 
+def ref_rotate(ints, U):
+    """OrbitalTransform::fillHamCI with the unitary U (row-major, U[a, p]): the
+    rotated (h, eri chemist) of the reference."""
+    lib = ref()
+    lib.ref_rotate.restype = ctypes.c_int
+    lib.ref_rotate.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [_P] * 5
+    L = ints.L
+    hh = np.ascontiguousarray(ints.h, dtype=np.float64)
+    ee = np.ascontiguousarray(ints.eri, dtype=np.float64)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    h = np.zeros((L, L))
+    eri = np.zeros((L,) * 4)
+    lib.ref_rotate(L, ints.nup, ints.ndown, ints.econst, _ptr(hh), _ptr(ee), _ptr(U), _ptr(h), _ptr(eri))
+    return h, eri
+
+
 def build_dets(ints, up: np.ndarray, down: np.ndarray, words: int = 1) -> UpperCRS:
     """The oracle's FCI_File CRS of a determinant list (strings of `words` 64-bit words)."""
     lib = port()

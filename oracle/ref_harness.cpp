@@ -261,6 +261,33 @@ int ref_jacobi(int L, int nup, int ndown, double econst, const double *h, const 
     return 0;
 }
 
+// OrbitalTransform::fillHamCI (OrbitalTransform.cpp:64-135) with the unitary set to
+// U (row-major, U[a*L + p]: row a is the new orbital a in the old orbitals; the
+// reference block is column-major, element (a, p) at a + L*p). Outputs the
+// rotated h (L*L) and eri (L^4, chemist) the reference Hamiltonian holds.
+int ref_rotate(int L, int nup, int ndown, double econst, const double *h, const double *eri, const double *U,
+               double *h_out, double *eri_out) {
+    Hamiltonian *ham = make_ham(L, nup, ndown, econst, h, eri);
+    Hamiltonian *rot = make_ham(L, nup, ndown, econst, h, eri);
+    {
+        OrbitalTransform tr(ham);
+        double *blk = tr.get_unitary().getBlock(0);
+        for (int a = 0; a < L; ++a)
+            for (int p_ = 0; p_ < L; ++p_) blk[a + (size_t)L * p_] = U[a * L + p_];
+        tr.fillHamCI(*rot);
+    }
+    const size_t L1 = L, L2 = L1 * L1, L3 = L2 * L1;
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j) h_out[i * L + j] = rot->getTmat(i, j);
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j)
+            for (int k_ = 0; k_ < L; ++k_)
+                for (int l_ = 0; l_ < L; ++l_) eri_out[i * L3 + j * L2 + k_ * L1 + l_] = rot->getVmat(i, k_, j, l_);
+    delete rot;
+    delete ham;
+    return 0;
+}
+
 // DOCI pair scan with the reference density of the installed eigenpair (as in
 // ref_ci_density). For pair index P of k < l: theta/energy/found as
 // LocalMinimizer::scan_orbitals decides them (start 0.3, then 0.01 on a maximum;

@@ -288,6 +288,61 @@ def case_formats(name: str):
     print(name, {k: (len(v) if isinstance(v, str) else v) for k, v in out.items()})
 
 
+# RDMs of the FP64 ground state where the reference's DensFCI (O(dim^2) pair loop)
+# is out of reach (c1: 853,776 determinants): the lowest eigenpair of the CRS
+# (the oracle's, bit-identical to the reference CRS by the SHA-256 of case_config)
+# from ARPACK at the reference's settings, and its RDMs from the oracle's
+# restatement of DensFCI (pinned to the reference's DensFCI on BeH2, c0 and c4).
+def case_state_rdm(name: str):
+    import scipy.sparse.linalg as sla
+    cfg = CONFIGS[name]
+    method = O.FCI if cfg["method"] == "FCI" else O.DOCI
+    ints = config_integrals(name)
+    meta = json.load(open(os.path.join(OUT, f"{name}.json")))
+    m = O.build_upper(method, ints)
+    assert crs_sha256(m) == meta["crs_sha256"], "oracle CRS differs from the reference CRS"
+    n = m.n
+    op = sla.LinearOperator((n, n), matvec=lambda x: O.sym_mvprod(m, x, threaded=True), dtype=np.float64)
+    w, v = sla.eigsh(op, k=1, which="SA", ncv=42, tol=0, maxiter=3 * n,
+                     v0=np.random.default_rng(12345).standard_normal(n))
+    del m
+    c = v[:, 0] / np.linalg.norm(v[:, 0])
+    r1, aa, ab, bb = O.rdm(method, ints.L, ints.nup, ints.ndown, c)
+    meta["state_rdm"] = {"e0": float(w[0]) + ints.econst,
+                         "source": "ARPACK (which='SA', ncv=42, tol=0) on the reference CRS; oracle DensFCI"}
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), rdm1=r1, aa=aa, ab=ab, bb=bb)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta["state_rdm"]))
+
+
+# Orbital rotation: the reference's OrbitalTransform::fillHamCI (with the real
+# dgemm of oracle/ref_shims) applied to seeded integrals with U = exp(kappa),
+# kappa antisymmetric with N(0, sigma) entries (the served stream's rotation is
+# sigma = 0.05; sigma = 0.6 mixes the orbitals strongly). Cases: L=8 (the 4a4b
+# FCI integrals) and L=10 (the 5a5b served-stream base integrals).
+ROTATE_CASES = {"L8": ("c0", 0.6, 21), "L10": ("c4", 0.05, 22), "L10_strong": ("c4", 0.6, 23)}
+
+
+def case_rotate(name: str):
+    import scipy.linalg as sl
+    out, meta = {}, {}
+    for tag, (cfg_name, sigma, seed) in ROTATE_CASES.items():
+        ints = config_integrals(cfg_name)
+        L = ints.L
+        rng = np.random.default_rng(seed)
+        k = np.triu(rng.normal(0.0, sigma, (L, L)), 1)
+        U = sl.expm(k - k.T)
+        h, eri = O.ref_rotate(ints, U)
+        out.update({f"{tag}_U": U, f"{tag}_h": h, f"{tag}_eri": eri})
+        meta[tag] = {"config": cfg_name, "sigma": sigma, "seed": seed, "L": L,
+                     "integrals_sha": ints.checksum()}
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    with open(os.path.join(OUT, f"{name}.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, json.dumps(meta))
+
+
 # CPU baseline calibration: the reference (oracle/_ref) against the oracle's
 # restatement (the port that runs on hosts without the reference tree), on the same
 # host with the same thread count, and ARPACK's matvec count at the reference's
@@ -357,7 +412,11 @@ def case_calibration(name: str, cfgs=("c0", "c4", "c2", "c1")):
 if __name__ == "__main__":
     names = sys.argv[1:] or ["beh2_sto3g", "c0", "c4", "orbopt", "dets", "formats", "warm_chain"]
     for nm in names:
-        if nm == "calibration":
+        if nm == "c1_state":
+            case_state_rdm("c1")
+        elif nm == "rotate":
+            case_rotate(nm)
+        elif nm == "calibration":
             case_calibration(nm)
         elif nm.startswith("calibration:"):
             case_calibration("calibration", tuple(nm.split(":", 1)[1].split(",")))

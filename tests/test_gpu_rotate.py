@@ -6,10 +6,16 @@ Checks: the rotated integrals equal the numpy four-index transform to 1e-13
 energy does not change under a rotation (FCI is invariant) while the DOCI
 energy does, and matches DOCI on host-rotated integrals; a served request with
 a rotation gives the same energy as the request with pre-rotated integrals.
+Pinned to the reference: the rotated integrals equal those the reference's own
+OrbitalTransform::fillHamCI produces for the same U (tests/golden/rotate.*,
+made by tests/golden/make_golden.py from the compiled reference) to 1e-12 of
+the largest integral.
 """
 import numpy as np
 import pytest
 import scipy.linalg
+
+from .helpers import load_golden
 
 from ciflow_gb300 import _abi as A
 from ciflow_gb300.ciflow import DOCI, FCI, Hamiltonian
@@ -77,3 +83,16 @@ def test_served_rotation_matches_prerotated_integrals():
         with pytest.raises(A.CigpuError) as e:
             srv.submit(ints, rot=2.0 * U)  # not orthogonal
         assert e.value.status == A.EINVAL
+
+
+@pytest.mark.parametrize("tag", ["L8", "L10", "L10_strong"])
+def test_rotation_matches_reference_fillhamci(tag):
+    from ciflow_gb300.synthetic import config_integrals
+    meta, g = load_golden("rotate")
+    m = meta[tag]
+    ints = config_integrals(m["config"])
+    assert ints.checksum() == m["integrals_sha"]
+    H = Hamiltonian.from_integrals(ints).rotated(g[f"{tag}_U"])
+    scale = np.abs(g[f"{tag}_eri"]).max()
+    assert np.abs(H.eri - g[f"{tag}_eri"]).max() <= 1e-12 * scale
+    assert np.abs(H.h - g[f"{tag}_h"]).max() <= 1e-12 * np.abs(g[f"{tag}_h"]).max()

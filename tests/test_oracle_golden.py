@@ -104,3 +104,19 @@ def test_oracle_rejects_bad_sizes():
     lib = O.port()
     assert lib.orc_build_upper(O.FCI, 70, 3, 3, None, None, None, None, None) != 0
     assert lib.orc_build_upper(O.DOCI, 8, 3, 2, None, None, None, None, None) != 0
+
+
+def test_rotation_fixture_is_the_four_index_transform():
+    """The reference fillHamCI fixture (tests/golden/rotate.*) is U h U^T and the
+    four-index transform of the ERIs: checks the fixture and the dgemm shim."""
+    from .helpers import load_golden
+    from ciflow_gb300.synthetic import config_integrals
+    meta, g = load_golden("rotate")
+    for tag, m in meta.items():
+        ints = config_integrals(m["config"])
+        U = g[f"{tag}_U"]
+        np.testing.assert_allclose(U @ U.T, np.eye(ints.L), atol=1e-13)
+        h = U @ ints.h @ U.T
+        eri = np.einsum("ap,bq,cr,ds,pqrs->abcd", U, U, U, U, ints.eri, optimize=True)
+        assert np.abs(g[f"{tag}_h"] - h).max() <= 1e-12 * np.abs(h).max()
+        assert np.abs(g[f"{tag}_eri"] - eri).max() <= 1e-12 * np.abs(eri).max()
