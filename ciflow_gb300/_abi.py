@@ -17,7 +17,7 @@ OK, EINVAL, ENOMEM, EAGAIN, ECANCELED, ETIMEDOUT, ENOTSUP, ENOCONV, ECUDA, ENOTF
 FCI, DOCI, DETS = 0, 1, 2
 DETS_CRS, DETS_ONTHEFLY = 0, 1
 FP64, MIXED = 0, 1
-LAYOUT_CRS, LAYOUT_SLOTS, LAYOUT_ONTHEFLY = 0, 1, 2
+LAYOUT_CRS, LAYOUT_SLOTS, LAYOUT_ONTHEFLY, LAYOUT_PAIRS = 0, 1, 2, 3
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -193,8 +193,10 @@ def matvec_bytes(handle, fp32: bool) -> tuple[int, str]:
     check(lib().cigpu_crs_layout(handle, ctypes.byref(lay), ctypes.byref(stored)))
     n, m = dim.value, stored.value
     sx = 4 if fp32 else 8
+    if lay.value == LAYOUT_PAIRS:  # matrix-free DOCI: strings, diagonal, x, y (hop gathers hit x in L2)
+        return n * (8 + 3 * sx), "doci-pairs-fp32" if fp32 else "doci-pairs-fp64"
     if lay.value == LAYOUT_SLOTS:
-        sv = 4 if fp32 else 8
-        return m * sv + 2 * n * sx, "slots-fp32" if fp32 else "slots-hilo"
+        sv = 4 if fp32 else 8  # FP32 values, or FP64 values / FP32 hi + lo
+        return m * sv + 2 * n * sx, "slots-fp32" if fp32 else "slots-fp64"
     sv = 4 if fp32 else 8
     return m * (sv + 4) + 8 * (n + 1) + 2 * n * sx, "crs-fp32" if fp32 else "crs-fp64"

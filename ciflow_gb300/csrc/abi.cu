@@ -221,6 +221,8 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     size_t b = (size_t)dim * W * 12;
     if (method == CIGPU_FCI && precision == CIGPU_MIXED)  // slot tiles of kTileRows beta strings, hi + lo
         b = (size_t)binom64(L, nup) * ((binom64(L, ndown) + kTileRows - 1) / kTileRows * kTileRows) * (W + 16) * 8;
+    if (method == CIGPU_DOCI)  // matrix-free: strings and the FP32 diagonal
+        b = (size_t)dim * (8 + 4);
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
     b += (size_t)dim * vbytes * (42 + 1 + 14);   // Krylov basis + restart buffer
     b += (size_t)dim * 8 * 5;                    // c, refinement vectors
@@ -252,21 +254,62 @@ struct RowSingles {
 };
 
 // Explicit FP32 CRS (columns + hi values) of a values-only CRS, for export.
-struct ExplicitFp32 {
+// The explicit CRS (columns and values) of a matrix stored as slot tiles, made by
+// the CRS generator for export: FP32 hi/lo values for MIXED, FP64 for FP64.
+struct ExplicitCrs {
     DevBuf<uint32_t> col;
     DevBuf<float> hi, lo;
+    DevBuf<double> v64;
     void make(cigpu_crs &c, cudaStream_t s) {
+        if (c.pairs) {
+            make_doci(c, s);
+            return;
+        }
         FciParams q = c.fp;
         RowSingles rs;
         rs.make(c, q, s);
         col.alloc(std::max<int64_t>(c.nnz_full, 1));
-        hi.alloc(std::max<int64_t>(c.nnz_full, 1));
-        lo.alloc(std::max<int64_t>(c.nnz_full, 1));
         q.row_ptr = c.row_ptr.p;
         q.col = col.p;
-        q.val32 = hi.p;
-        q.val32lo = lo.p;
-        fci_launch(kFill32, q, s);
+        if (c.precision == CIGPU_FP64) {
+            v64.alloc(std::max<int64_t>(c.nnz_full, 1));
+            q.val64 = v64.p;
+            fci_launch(kFill64, q, s);
+        } else {
+            hi.alloc(std::max<int64_t>(c.nnz_full, 1));
+            lo.alloc(std::max<int64_t>(c.nnz_full, 1));
+            q.val32 = hi.p;
+            q.val32lo = lo.p;
+            fci_launch(kFill32, q, s);
+        }
+    }
+    // DOCI without a stored matrix: the row structure (count pass + scan, kept in
+    // the handle) and the explicit rows from the CRS generator.
+    void make_doci(cigpu_crs &c, cudaStream_t s) {
+        DociParams q = c.dp;
+        if (!c.rows_ready) {
+            DevBuf<uint32_t> count(c.dim);
+            q.row_count = count.p;
+            q.upper_off = c.upper_off.p;
+            doci_launch(kCount, q, s);
+            exclusive_scan_u32(count.p, c.row_ptr.p, c.dim, s);
+            CIGPU_CUDA(cudaStreamSynchronize(s));
+            c.rows_ready = true;
+        }
+        col.alloc(std::max<int64_t>(c.nnz_full, 1));
+        q.row_ptr = c.row_ptr.p;
+        q.col = col.p;
+        if (c.precision == CIGPU_FP64) {
+            v64.alloc(std::max<int64_t>(c.nnz_full, 1));
+            q.val64 = v64.p;
+            doci_launch(kFill64, q, s);
+        } else {
+            hi.alloc(std::max<int64_t>(c.nnz_full, 1));
+            lo.alloc(std::max<int64_t>(c.nnz_full, 1));
+            q.val32 = hi.p;
+            q.val32lo = lo.p;
+            doci_launch(kFill32, q, s);
+        }
     }
 };
 
@@ -304,15 +347,21 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
         singles.make(c, p, s);
-        c.slots = c.precision == CIGPU_MIXED && slots_supported(p);
+        c.slots = slots_supported(p) &&
+                  (c.precision == CIGPU_MIXED || (c.allow_compact && slots64_pay(p)));
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         if (c.slots) {
             // values-only layout: the fill counts the rows itself
-            c.val32.alloc(slots_count(p));
-            c.val32lo.alloc(slots_count(p));
-            fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
+            if (c.precision == CIGPU_MIXED) {
+                c.val32.alloc(slots_count(p));
+                c.val32lo.alloc(slots_count(p));
+                fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
+            } else {
+                c.val64.alloc(slots_count(p));
+                fill_slots64_launch(p, c.val64.p, count.p, c.upper_off.p, s);
+            }
             c.slot_desc.alloc(std::max<int64_t>(slot_desc_count(p), 1));
             c.slot_st.alloc(std::max<int64_t>(slot_st_count(p), 4));
             slot_tables_launch(p, c.slot_desc.p, c.slot_st.p, s);
@@ -339,6 +388,41 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         doci_diag_launch(p, c.diag.p, s);
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
+        // MIXED is matrix-free (its FP32 product costs about what the FP32 CRS costs,
+        // and the build drops from a CRS count + sort + fill to the pair table); the
+        // FP64 form keeps the CRS, whose FP64 product is the faster one (1.24 against
+        // 1.70 ms at L=24, 12 pairs), and its 120-odd matvecs outweigh the build
+        if (c.allow_compact && c.precision == CIGPU_MIXED) {
+            // matrix-free: the pair-hop table and, for MIXED, the FP32 diagonal; the
+            // stored-element counts follow from K: a pair (j, k) with K_jk != 0 hops in
+            // the C(L-2, n-1) strings holding j and not k
+            const int L = c.L, n = c.nup;
+            c.pairs = true;
+            c.rows_ready = false;
+            c.kpair64.alloc((size_t)L * L);
+            c.kpair32.alloc((size_t)L * L);
+            doci_pair_table_launch(L, h.d_eri.p, c.kpair64.p, c.kpair32.p, s);
+            if (c.precision == CIGPU_MIXED) {
+                c.diag32.alloc(dim);
+                dev_convert(c.diag.p, c.diag32.p, dim, s);
+            }
+            std::vector<double> K((size_t)L * L);
+            CIGPU_CUDA(cudaMemcpyAsync(K.data(), c.kpair64.p, sizeof(double) * K.size(), cudaMemcpyDeviceToHost, s));
+            const int64_t nd = count_nonzero(c.diag.p, dim, s);  // synchronises s
+            int64_t nk = 0, nku = 0;
+            for (int j = 0; j < L; ++j)
+                for (int k = 0; k < L; ++k)
+                    if (K[(size_t)j * L + k] != 0.0) {
+                        ++nk;
+                        nku += k > j;
+                    }
+            const int64_t per = (n >= 1 && L >= 2) ? d_binom(L - 2, n - 1) : 0;
+            c.nnz_full = nd + nk * per;
+            c.nnz_upper = nd + nku * per;
+            tr.mark("strings + diag + pair table");
+            c.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            return;
+        }
         doci_launch(kCount, p, s);
         tr.mark("strings + diag + count");
     }
@@ -394,12 +478,19 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         dets_mv64(c, x, y, s);
         return;
     }
+    if (c.pairs) {
+        doci_mv64(DociMv{c.L, c.nup, c.dim, c.strings.p}, c.kpair64.p, c.diag.p, x, y, s);
+        return;
+    }
     if (c.precision == CIGPU_MIXED) {
         if (!c.x32.p) c.x32.alloc(std::max<int64_t>(c.dim, 1));
         dev_convert(x, c.x32.p, c.dim, s);
     }
     if (c.slots) {
-        spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
+        if (c.precision == CIGPU_FP64)
+            spmv_slots_f64(c.fp, c.val64.p, x, y, s);
+        else
+            spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
         return;
     }
     if (c.precision == CIGPU_FP64) {
@@ -417,6 +508,10 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
 
 void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
     if (c.precision != CIGPU_MIXED || c.onthefly) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
+    if (c.pairs) {
+        doci_mv32(DociMv{c.L, c.nup, c.dim, c.strings.p}, c.kpair32.p, c.diag32.p, x, y, s);
+        return;
+    }
     if (c.slots) {
         spmv_slots_f32(c.fp, c.val32.p, x, y, s);
         return;
@@ -585,6 +680,13 @@ int cigpu_estimate_bytes(int L, int nup, int ndown, int method, int precision, s
 }
 
 int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, cigpu_crs **out) {
+    return build_handle(ham, method, precision, stream, true, out);
+}
+
+}  // extern "C"
+
+namespace cigpu {
+int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool compact, cigpu_crs **out) {
     if (!ham || !out) return CIGPU_EINVAL;
     *out = nullptr;
     if (method != CIGPU_FCI && method != CIGPU_DOCI) return CIGPU_EINVAL;
@@ -603,6 +705,7 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
     c->nup = ham->nup;
     c->ndown = ham->ndown;
     c->dim = dim;
+    c->allow_compact = compact;
     if (stream) {
         c->stream = static_cast<cudaStream_t>(stream);
     } else {
@@ -615,6 +718,9 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
     return CIGPU_OK;
     CIGPU_CATCH
 }
+}  // namespace cigpu
+
+extern "C" {
 
 int cigpu_crs_destroy(cigpu_crs *crs) {
     if (!crs) return CIGPU_OK;
@@ -640,8 +746,12 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
 
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
     if (!crs) return CIGPU_EINVAL;
-    if (layout) *layout = crs->onthefly ? CIGPU_LAYOUT_ONTHEFLY : crs->slots ? CIGPU_LAYOUT_SLOTS : CIGPU_LAYOUT_CRS;
-    if (stored) *stored = crs->onthefly ? 0 : crs->slots ? slots_count(crs->fp) : crs->nnz_full;
+    if (layout)
+        *layout = crs->onthefly ? CIGPU_LAYOUT_ONTHEFLY
+                  : crs->pairs  ? CIGPU_LAYOUT_PAIRS
+                  : crs->slots  ? CIGPU_LAYOUT_SLOTS
+                                : CIGPU_LAYOUT_CRS;
+    if (stored) *stored = (crs->onthefly || crs->pairs) ? 0 : crs->slots ? slots_count(crs->fp) : crs->nnz_full;
     return CIGPU_OK;
 }
 
@@ -653,16 +763,19 @@ int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double 
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
     const int64_t dim = crs->dim;
+    ExplicitCrs ex;
+    const bool gen = crs->slots || crs->pairs;  // no stored explicit CRS: generate it
+    if (gen) ex.make(*crs, s);
     DevBuf<uint32_t> ucnt(dim);
     DevBuf<int64_t> urow(dim + 1);
     upper_counts_launch(dim, crs->row_ptr.p, crs->upper_off.p, ucnt.p, s);
     exclusive_scan_u32(ucnt.p, urow.p, dim, s);
     DevBuf<uint32_t> ucol(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
     DevBuf<double> uval(crs->nnz_upper > 0 ? crs->nnz_upper : 1);
-    ExplicitFp32 ex;
-    if (crs->slots) ex.make(*crs, s);
-    extract_upper_launch(dim, crs->row_ptr.p, crs->upper_off.p, crs->slots ? ex.col.p : crs->col.p, crs->val64.p,
-                         crs->slots ? ex.hi.p : crs->val32.p, urow.p, ucol.p, uval.p, s);
+    const bool f64 = crs->precision == CIGPU_FP64;
+    extract_upper_launch(dim, crs->row_ptr.p, crs->upper_off.p, gen ? ex.col.p : crs->col.p,
+                         f64 ? (gen ? ex.v64.p : crs->val64.p) : nullptr,
+                         f64 ? nullptr : (gen ? ex.hi.p : crs->val32.p), urow.p, ucol.p, uval.p, s);
     std::vector<int64_t> hr(dim + 1);
     CIGPU_CUDA(cudaMemcpyAsync(hr.data(), urow.p, sizeof(int64_t) * (dim + 1), cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaMemcpyAsync(col, ucol.p, sizeof(uint32_t) * crs->nnz_upper, cudaMemcpyDeviceToHost, s));
@@ -679,17 +792,19 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
     CIGPU_TRY
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
-    ExplicitFp32 ex;
-    if (crs->slots) ex.make(*crs, s);
+    ExplicitCrs ex;
+    const bool gen = crs->slots || crs->pairs;  // no stored explicit CRS: generate it
+    if (gen) ex.make(*crs, s);
     CIGPU_CUDA(cudaMemcpyAsync(row, crs->row_ptr.p, sizeof(int64_t) * (crs->dim + 1), cudaMemcpyDeviceToHost, s));
-    CIGPU_CUDA(cudaMemcpyAsync(col, crs->slots ? ex.col.p : crs->col.p, sizeof(uint32_t) * crs->nnz_full,
+    CIGPU_CUDA(cudaMemcpyAsync(col, gen ? ex.col.p : crs->col.p, sizeof(uint32_t) * crs->nnz_full,
                                cudaMemcpyDeviceToHost, s));
     if (crs->precision == CIGPU_FP64) {
-        CIGPU_CUDA(cudaMemcpyAsync(val, crs->val64.p, sizeof(double) * crs->nnz_full, cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(val, gen ? ex.v64.p : crs->val64.p, sizeof(double) * crs->nnz_full,
+                                   cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaStreamSynchronize(s));
     } else {
         std::vector<float> tmp(crs->nnz_full);
-        CIGPU_CUDA(cudaMemcpyAsync(tmp.data(), crs->slots ? ex.hi.p : crs->val32.p, sizeof(float) * crs->nnz_full,
+        CIGPU_CUDA(cudaMemcpyAsync(tmp.data(), gen ? ex.hi.p : crs->val32.p, sizeof(float) * crs->nnz_full,
                                    cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaStreamSynchronize(s));
         for (int64_t i = 0; i < crs->nnz_full; ++i) val[i] = tmp[i];

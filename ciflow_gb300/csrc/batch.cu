@@ -815,7 +815,7 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                     cigpu_ham_destroy(it.ham);
                     it.ham = rotated;
                 }
-                if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, CIGPU_FP64, s, &it.crs);
+                if (stc == CIGPU_OK) stc = build_handle(it.ham, q.method, CIGPU_FP64, s, false, &it.crs);
                 it.status = stc;
                 if (stc != CIGPU_OK && failed[t] == CIGPU_OK) failed[t] = stc;
             }

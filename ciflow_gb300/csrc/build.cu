@@ -322,15 +322,21 @@ __global__ void __launch_bounds__(kFciThreads) k_fci_rows(FciParams p) {
 // ---------------------------------------------------------------------------
 // DOCI.
 __global__ void k_unrank(int L, int n, int64_t D, uint64_t *strings) {
+    __shared__ int64_t binom[64 * 33];  // C(p, m) for p < 64, m <= 32 (n <= 32 is enforced by the host)
+    for (int i = threadIdx.x; i < 64 * 33; i += blockDim.x) {
+        const int pp = i / 33, mm = i % 33;
+        binom[i] = (pp <= L && mm <= n) ? d_binom(pp, mm) : 0;
+    }
+    __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
         // inverse of rank = sum_m C(p_m, m): pick the largest p with C(p, m) <= remaining
         uint64_t s = 0;
         int64_t rem = i;
         int p = L - 1;
         for (int m = n; m >= 1; --m) {
-            while (p >= 0 && d_binom(p, m) > rem) --p;
+            while (p >= 0 && binom[p * 33 + m] > rem) --p;
             s |= (uint64_t)1 << p;
-            rem -= d_binom(p, m);
+            rem -= binom[p * 33 + m];
             --p;
         }
         strings[i] = s;

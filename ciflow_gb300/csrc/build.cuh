@@ -58,23 +58,30 @@ struct DociParams {
 };
 
 // C(n, k) exactly while it fits in int64, else INT64_MAX (saturated). Each step
-// r <- r (n-k+i) / i is carried out as (r/g) ((n-k+i)/(i/g)) with g = gcd(r, i),
-// which is exact (i divides r (n-k+i)) and has no intermediate larger than the
-// result, so nothing overflows for any n (Hamiltonians go up to 128 orbitals).
+// r <- r (n-k+i) / i is exact (i divides r (n-k+i)); it runs in 64 bits while
+// r (n-k+i) fits, and otherwise as (r/g) ((n-k+i)/(i/g)) with g = gcd(r, i), whose
+// factors are at most the result, so nothing overflows for any n (Hamiltonians go
+// up to 128 orbitals).
 __host__ __device__ inline int64_t d_binom(int n, int k) {
     if (k < 0 || k > n) return 0;
     if (k > n - k) k = n - k;
     uint64_t r = 1;
     for (int i = 1; i <= k; ++i) {
-        uint64_t g = r, b = (uint64_t)i;
-        while (b) {
-            const uint64_t t = g % b;
-            g = b;
-            b = t;
+        const uint64_t m = (uint64_t)(n - k + i);
+        if (r <= UINT64_MAX / m) {
+            r = r * m / (uint64_t)i;
+        } else {
+            uint64_t g = r, b = (uint64_t)i;
+            while (b) {
+                const uint64_t t = g % b;
+                g = b;
+                b = t;
+            }
+            const uint64_t a = r / g, f = m / ((uint64_t)i / g);
+            if (a > UINT64_MAX / f) return INT64_MAX;
+            r = a * f;
         }
-        const uint64_t a = r / g, m = (uint64_t)(n - k + i) / ((uint64_t)i / g);
-        if (a > (uint64_t)INT64_MAX / m) return INT64_MAX;
-        r = a * m;
+        if (r > (uint64_t)INT64_MAX) return INT64_MAX;
     }
     return (int64_t)r;
 }

@@ -1,9 +1,16 @@
 // The CRS handle shared by the ABI, RDM and server translation units.
 #pragma once
 
+#include <memory>
+
 #include "build.cuh"
+#include "doci_mv.cuh"
 #include "lanczos.cuh"
 #include "slots.cuh"
+
+namespace cigpu {
+struct FciRdmPlan;  // rdm.cu
+}
 
 struct cigpu_crs {
     cigpu_ham *ham = nullptr;
@@ -28,6 +35,15 @@ struct cigpu_crs {
     // MIXED FCI: values-only slot tiles (val32/val32lo hold slots_count(fp) values,
     // no col); row_ptr/upper_off/nnz still describe the explicit matrix for export
     bool slots = false;
+    // compact layouts allowed: FP64 slot tiles for FP64 FCI, the matrix-free pair-hop
+    // form for DOCI (the lockstep batch concatenates explicit CRS matrices)
+    bool allow_compact = true;
+    // DOCI without a stored matrix: the matvecs generate the pair hops (doci_mv.cu)
+    // from the strings and K_jk; row_ptr / upper_off are filled on demand (export)
+    bool pairs = false;
+    bool rows_ready = true;
+    cigpu::DevBuf<double> kpair64;
+    cigpu::DevBuf<float> kpair32, diag32;
     cigpu::DevBuf<uint64_t> slot_desc;  // the slot matvecs' staging tables (slot_tables_launch)
     cigpu::DevBuf<uint32_t> slot_st;
     cigpu::DevBuf<float> x32;  // MIXED: FP32 copy of x for the FP64 product from hi + lo
@@ -38,6 +54,7 @@ struct cigpu_crs {
     bool onthefly = false;          // CI_Big: no stored matrix, elements recomputed in every matvec
     cigpu::DevBuf<uint64_t> dets;   // [dim][2 * det_words]: up words, then down words
     double build_seconds = 0;
+    std::shared_ptr<cigpu::FciRdmPlan> rdm_plan;  // FCI RDM plan, made by the first RDM call
 
     ~cigpu_crs() {
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -45,6 +62,9 @@ struct cigpu_crs {
 };
 
 namespace cigpu {
+// cigpu_build with a choice of layout: fp64_tiles = false keeps an FP64 FCI matrix
+// as a CRS (the lockstep batch concatenates CRS matrices).
+int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool fp64_tiles, cigpu_crs **out);
 // Builds the CRS for `ham` on stream `s` (throws on failure).
 void build_crs(cigpu_crs &c, cudaStream_t s);
 // FP64 product y = H x on the CRS stream (device pointers).

@@ -31,6 +31,7 @@
 // Determinant lists (DensFILE) are handled in dets.cu: a pair scan with 64-bit
 // fixed-point integer atomics (order-independent sums, also bit-reproducible).
 #include <algorithm>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 
@@ -43,14 +44,22 @@ constexpr int kRdmThreads = 256;
 
 inline int pidx(int p, int q, int L) { return p * L + q - (p + 1) * (p + 2) / 2; }
 
-int64_t hbinom(int n, int k) { return d_binom(n, k); }
+// C(n, k) for n, k < 64 (strings of up to 63 orbitals), filled once.
+struct BinomTable {
+    int64_t c[64][65];
+    BinomTable() {
+        for (int n = 0; n < 64; ++n)
+            for (int k = 0; k <= 64; ++k) c[n][k] = d_binom(n, k);
+    }
+};
 
 uint32_t hrank(uint64_t s) {
+    static const BinomTable bt;
     int64_t r = 0;
     int m = 0;
     while (s) {
         ++m;
-        r += hbinom(__builtin_ctzll(s), m);
+        r += bt.c[__builtin_ctzll(s)][m];
         s &= s - 1;
     }
     return (uint32_t)r;
@@ -76,7 +85,11 @@ struct Plan {
     size_t off_ga, off_gb, off_g0, off_g1, off_g2, nslots;
     // density layout: [Da0 | Daz | Db0 | Dbz]
     size_t off_da0, off_daz, off_db0, off_dbz, ndens;
-    std::vector<std::vector<std::pair<uint32_t, int8_t>>> terms;  // per slot
+    struct Term {
+        uint32_t slot, dens;
+        int8_t coef;
+    };
+    std::vector<Term> terms;  // in generation order; grouped by slot (stably) afterwards
     // alpha-beta doubles
     std::vector<uint32_t> ap_ptr;   // [np+1] alpha pairs per (ar<ac)
     std::vector<uint64_t> ap;       // Ia | Ja << 32
@@ -87,7 +100,7 @@ struct Plan {
 };
 
 void add_term(Plan &P, size_t slot, size_t dens, int coef) {
-    P.terms[slot].push_back({(uint32_t)dens, (int8_t)coef});
+    P.terms.push_back({(uint32_t)slot, (uint32_t)dens, (int8_t)coef});
 }
 
 // Slot of a symmetric pair matrix entry (min, max) of dimension dimx at offset off.
@@ -381,38 +394,135 @@ __global__ void k_transpose(const double *__restrict__ a, int64_t rows, int64_t 
 }
 
 // ---------------------------------------------------------------------------
-// DOCI: thread (j,k) of an L*L block accumulates, over a slice of pair strings,
-//   A_jk = sum c_I^2 n_j n_k   and   B_jk = sum_{j in I, k not in I, k > j} c_I c_J.
+// DOCI: thread (j,k) of an L*L block accumulates, over the block's pair strings,
+//   A_jk = sum c_I^2 n_j n_k   and   B_jk = sum_{j in I, k not in I, k > j} c_I c_J,
+// J = I - j + k. The block stages kDociChunk strings at a time in shared memory
+// (one coalesced load of strings and c) with each string's rank prefix, so every
+// pair-hop rank costs O(1): with p_1 < ... < p_n the occupied orbitals and
+// rank(S) = sum_m C(p_m, m), moving the electron at j = p_{a+1} to the empty
+// k > j (b electrons below k, j included) shifts p_{a+2..b} down one place:
+//   rank(J) = I - C(j, a+1) + (P_b - P_{a+1}) + C(k, b),
+//   P_m = sum_{i <= m} (C(p_i, i-1) - C(p_i, i)),
+// evaluated modulo 2^32 (the result is a rank below 2^32, so the wrap cancels).
+//
+// The sums are 64-bit fixed-point integers (value * 2^60) on the integer pipe: a
+// thread's FP64 add would occupy GB300's FP64 pipe (2 lanes per clock per SM) for
+// the whole warp even when one lane of it needs the add, and most lanes of a warp
+// skip a given string. Each coefficient becomes c * 2^62 (rounded to nearest, from
+// its bit fields, |c| <= 1 for a normalised state), a product is the rounded high
+// half of the 128-bit product (scale 2^60), and integer addition is associative, so
+// the sums do not depend on order; each term is rounded by at most 2^-61 and every
+// sum lies within +-1.
+constexpr int kDociChunk = 128;
+constexpr int kDociMaxL = 32;
+constexpr int kRdmBatch = 8;  // pair hops gathered per round (loads in flight per thread)
+
+// c * 2^62 rounded to nearest (|c| <= 1), from the IEEE-754 fields on the integer pipe.
+__device__ __forceinline__ long long fx62(double c) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(c);
+    const int e = (int)((u >> 52) & 0x7FF);
+    if (e == 0) return 0;  // zero (and subnormals, below 2^-1022)
+    const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    const int sh = e - 1013;  // c * 2^62 = m * 2^(e - 1023 - 52 + 62)
+    unsigned long long r;
+    if (sh >= 0)
+        r = sh <= 10 ? (m << sh) : 0x4000000000000000ull;  // |c| <= 1 keeps sh <= 10
+    else if (sh > -64)
+        r = (m + (1ull << (-sh - 1))) >> (-sh);
+    else
+        r = 0;
+    return (u >> 63) ? -(long long)r : (long long)r;
+}
+
+// (a * b) / 2^64 rounded to nearest: a, b at scale 2^62 give a product at 2^60.
+__device__ __forceinline__ long long fxmul(long long a, long long b) {
+    const long long hi = __mul64hi(a, b);
+    const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+    return hi + (long long)(lo >> 63);
+}
+
 __global__ void k_doci_rdm(const double *__restrict__ c, const uint64_t *__restrict__ strings, int64_t D, int L,
                            int n, double *__restrict__ partial) {
-    __shared__ uint32_t binom[64 * 33];
-    for (int i = threadIdx.x; i < 64 * 33; i += blockDim.x) {
-        const int nn = i / 33, kk = i % 33;
-        binom[i] = (nn <= L && kk <= n) ? (uint32_t)d_binom(nn, kk) : 0u;
+    __shared__ uint32_t binom[(kDociMaxL + 1) * (kDociMaxL + 2)];  // C(nn, kk), nn <= L, kk <= n + 1
+    __shared__ uint64_t ss[kDociChunk];
+    __shared__ long long cs[kDociChunk], cs2[kDociChunk];  // c_I * 2^62, c_I^2 * 2^60
+    __shared__ uint32_t pre[kDociChunk][kDociMaxL + 1];
+    constexpr int BW = kDociMaxL + 2;
+    for (int i = threadIdx.x; i < (kDociMaxL + 1) * BW; i += blockDim.x) {
+        const int nn = i / BW, kk = i % BW;
+        binom[i] = (nn <= L && kk <= n + 1) ? (uint32_t)d_binom(nn, kk) : 0u;
     }
-    __syncthreads();
+    // thread t owns the pair (j, k), j <= k, of the upper triangle in row-major
+    // order (A is symmetric, B is summed for j < k only)
     const int t = threadIdx.x;
-    const int j = t / L, k = t % L;
-    double A = 0, B = 0;
-    if (t < L * L) {
-        for (int64_t I = blockIdx.x; I < D; I += gridDim.x) {
-            const uint64_t s = strings[I];
-            const double cI = c[I];
-            const bool nj = (s >> j) & 1, nk = (s >> k) & 1;
-            if (nj && nk) A += cI * cI;
-            if (nj && !nk && k > j) {
-                const uint64_t u = s ^ ((uint64_t)1 << j) ^ ((uint64_t)1 << k);
-                uint32_t r = 0;
-                int m = 0;
-                for (uint64_t x = u; x; x &= x - 1) {
-                    ++m;
-                    r += binom[(__ffsll((long long)x) - 1) * 33 + m];
-                }
-                B += cI * c[r];
+    const bool work = t < L * (L + 1) / 2;
+    int j = 0, k = 0;
+    if (work) {
+        int rem = t;
+        while (rem >= L - j) {
+            rem -= L - j;
+            ++j;
+        }
+        k = j + rem;
+    }
+    const bool hop = work && k > j;
+    const uint64_t below_j = work ? (((uint64_t)1 << j) - 1) : 0, below_k = work ? (((uint64_t)1 << k) - 1) : 0;
+    long long A = 0, B = 0;
+    for (int64_t base = (int64_t)blockIdx.x * kDociChunk; base < D; base += (int64_t)gridDim.x * kDociChunk) {
+        __syncthreads();  // the previous chunk is consumed (and the table is ready)
+        const int cnt = (D - base) < kDociChunk ? (int)(D - base) : kDociChunk;
+        for (int q = t; q < cnt; q += blockDim.x) {  // blocks of fewer than kDociChunk threads loop
+            const uint64_t st = strings[base + q];
+            const long long cf = fx62(c[base + q]);
+            ss[q] = st;
+            cs[q] = cf;
+            cs2[q] = fxmul(cf, cf);
+            uint32_t P = 0;
+            pre[q][0] = 0;
+            int m = 0;
+            for (uint64_t x = st; x; x &= x - 1) {
+                ++m;
+                const int pm = __ffsll((long long)x) - 1;
+                P += binom[pm * BW + m - 1] - binom[pm * BW + m];
+                pre[q][m] = P;
             }
         }
-        partial[((int64_t)blockIdx.x * 2) * L * L + t] = A;
-        partial[((int64_t)blockIdx.x * 2 + 1) * L * L + t] = B;
+        __syncthreads();
+        if (work) {
+            // kRdmBatch strings per round: ranks first, then their gathers of c
+            // together, so several L2 loads are in flight per thread
+            for (int i0 = 0; i0 < cnt; i0 += kRdmBatch) {
+                uint32_t rr[kRdmBatch];
+#pragma unroll
+                for (int u = 0; u < kRdmBatch; ++u) {
+                    const int i = i0 + u;
+                    rr[u] = 0xFFFFFFFFu;
+                    if (i < cnt) {
+                        const uint64_t st = ss[i];
+                        const bool nj = (st >> j) & 1, nk = (st >> k) & 1;
+                        if (nj && nk) A += cs2[i];
+                        if (hop && nj && !nk) {
+                            const int a = __popcll(st & below_j), b = __popcll(st & below_k);
+                            rr[u] = (uint32_t)(base + i) - binom[j * BW + a + 1] + pre[i][b] - pre[i][a + 1] +
+                                    binom[k * BW + b];
+                        }
+                    }
+                }
+                double cv[kRdmBatch];
+#pragma unroll
+                for (int u = 0; u < kRdmBatch; ++u) cv[u] = rr[u] < (uint64_t)D ? __ldg(c + rr[u]) : 0.0;
+#pragma unroll
+                for (int u = 0; u < kRdmBatch; ++u)
+                    if (rr[u] < (uint64_t)D) B += fxmul(cs[i0 + u], fx62(cv[u]));
+            }
+        }
+    }
+    // fixed-point sums at (j, k), j <= k, of the block's [2][L][L] partials (the
+    // lower triangle is not written and not read), read back by the finishing kernels
+    if (work) {
+        long long *pl = reinterpret_cast<long long *>(partial);
+        pl[((int64_t)blockIdx.x * 2) * L * L + j * L + k] = A;
+        pl[((int64_t)blockIdx.x * 2 + 1) * L * L + j * L + k] = B;
     }
 }
 
@@ -421,12 +531,15 @@ __global__ void k_doci_rdm_finish(const double *__restrict__ partial, int G, int
     const int L2 = L * L;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= L2) return;
-    double A = 0, B = 0;
-    for (int b = 0; b < G; ++b) {
-        A += partial[((int64_t)b * 2) * L2 + t];
-        B += partial[((int64_t)b * 2 + 1) * L2 + t];
-    }
     const int j = t / L, k = t % L;
+    const int tu = j <= k ? t : k * L + j;  // the partials hold j <= k
+    const long long *pl = reinterpret_cast<const long long *>(partial);  // fixed point, 2^60
+    long long Af = 0, Bf = 0;
+    for (int b = 0; b < G; ++b) {
+        Af += pl[((int64_t)b * 2) * L2 + tu];
+        Bf += pl[((int64_t)b * 2 + 1) * L2 + tu];
+    }
+    const double A = (double)Af * 0x1p-60, B = (double)Bf * 0x1p-60;
     // 1-RDM (both spins): gamma_jj = A_jj
     if (j == k) {
         rdm1[j * L + j] = A;
@@ -452,12 +565,14 @@ __global__ void k_doci_pairs_finish(const double *__restrict__ partial, int G, i
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= L2) return;
     const int j = t / L, k = t % L;
-    const int tb = j < k ? t : k * L + j;  // B is accumulated for j < k only
-    double A = 0, B = 0;
+    const int tu = j <= k ? t : k * L + j;  // the partials hold j <= k (B: j < k)
+    const long long *pl = reinterpret_cast<const long long *>(partial);  // fixed point, 2^60
+    long long Af = 0, Bf = 0;
     for (int b = 0; b < G; ++b) {
-        A += partial[((int64_t)b * 2) * L2 + t];
-        B += partial[((int64_t)b * 2 + 1) * L2 + tb];
+        Af += pl[((int64_t)b * 2) * L2 + tu];
+        Bf += pl[((int64_t)b * 2 + 1) * L2 + tu];
     }
+    const double A = (double)Af * 0x1p-60, B = (double)Bf * 0x1p-60;
     Pm[t] = j == k ? A : B;
     Dm[t] = j == k ? 0.0 : A;
 }
@@ -471,6 +586,113 @@ DevBuf<T> upload(const std::vector<T> &v, cudaStream_t s) {
 
 }  // namespace
 
+// The device copy of an FCI CRS's RDM plan: the string-pair lists, the per-element
+// term lists and the alpha-beta excitation lists. It depends on the string tables
+// only, so it is made on the first RDM call of a CRS and kept with it.
+struct FciRdmPlan {
+    int64_t npa = 0, nza = 0, npb = 0, nzb = 0;
+    size_t ndens = 0, nslots = 0;
+    size_t off_da0 = 0, off_daz = 0, off_db0 = 0, off_dbz = 0;
+    size_t off_ga = 0, off_gb = 0, off_g0 = 0, off_g1 = 0, off_g2 = 0;
+    int nsplit = 4;
+    DevBuf<uint64_t> sa, sb;                  // alpha / beta strings
+    DevBuf<uint32_t> aI, aJ, bI, bJ;          // string pairs per spin
+    DevBuf<uint32_t> dptr, didx;              // terms of every RDM element (CSR)
+    DevBuf<int8_t> dcf;
+    DevBuf<uint32_t> app, bxp;                // alpha-beta doubles: alpha pairs per (ar<ac), beta per (br,bc)
+    DevBuf<uint64_t> apd, bxd;
+    DevBuf<int8_t> aps, bxs;
+};
+
+std::shared_ptr<FciRdmPlan> make_fci_rdm_plan(cigpu_crs &c, cudaStream_t s) {
+    const int L = c.L, np = L * (L - 1) / 2;
+    const int64_t L2 = (int64_t)L * L;
+    const int64_t n2 = (int64_t)np * np, n3 = L2 * L2;
+    const SpinTables &ta = c.ta;
+    const SpinTables &tb = (c.ndown == c.nup) ? c.ta : c.tb;
+    Plan P;
+    P.L = L;
+    P.np = np;
+    P.Da = ta.D;
+    P.Db = tb.D;
+    P.off_ga = 0;
+    P.off_gb = L2;
+    P.off_g0 = 2 * L2;
+    P.off_g2 = P.off_g0 + n2;
+    P.off_g1 = P.off_g2 + n2;
+    P.nslots = P.off_g1 + n3;
+    // pair counts first (densities layout needs them)
+    auto count_pairs = [&](const SpinTables &t, size_t &npair, size_t &nz) {
+        size_t ns = 0, nd = 0;
+        for (int64_t I = 0; I < t.D; ++I) {
+            for (int q = 0; q < t.ns; ++q)
+                if (t.s_target[(size_t)I * t.ns + q] > (uint32_t)I) ++ns;
+            for (int q = 0; q < t.nd; ++q)
+                if (t.d_target[(size_t)I * t.nd + q] > (uint32_t)I) ++nd;
+        }
+        nz = (size_t)t.D + ns;
+        npair = nz + nd;
+    };
+    size_t npa, nza, npb, nzb;
+    count_pairs(ta, npa, nza);
+    count_pairs(tb, npb, nzb);
+    P.off_da0 = 0;
+    P.off_daz = npa;
+    P.off_db0 = P.off_daz + nza * L;
+    P.off_dbz = P.off_db0 + npb;
+    P.ndens = P.off_dbz + nzb * L;
+    plan_spin(P, ta, true);
+    plan_spin(P, tb, false);
+    plan_ab(P, ta, tb);
+    if (P.a.I.size() != npa || P.b.I.size() != npb) throw std::runtime_error("rdm plan: pair count mismatch");
+    // CSR of the slot terms: a stable counting sort keeps each slot's generation order
+    std::vector<uint32_t> ptr(P.nslots + 1, 0), idx(P.terms.size());
+    std::vector<int8_t> cf(P.terms.size());
+    for (const auto &t : P.terms) ++ptr[t.slot + 1];
+    for (size_t q = 0; q < P.nslots; ++q) ptr[q + 1] += ptr[q];
+    {
+        std::vector<uint32_t> fill(ptr.begin(), ptr.end() - 1);
+        for (const auto &t : P.terms) {
+            const uint32_t at = fill[t.slot]++;
+            idx[at] = t.dens;
+            cf[at] = t.coef;
+        }
+    }
+    auto R = std::make_shared<FciRdmPlan>();
+    R->npa = (int64_t)npa;
+    R->nza = (int64_t)nza;
+    R->npb = (int64_t)npb;
+    R->nzb = (int64_t)nzb;
+    R->ndens = P.ndens;
+    R->nslots = P.nslots;
+    R->off_da0 = P.off_da0;
+    R->off_daz = P.off_daz;
+    R->off_db0 = P.off_db0;
+    R->off_dbz = P.off_dbz;
+    R->off_ga = P.off_ga;
+    R->off_gb = P.off_gb;
+    R->off_g0 = P.off_g0;
+    R->off_g1 = P.off_g1;
+    R->off_g2 = P.off_g2;
+    R->sa = upload(ta.strings, s);
+    R->sb = upload(tb.strings, s);
+    R->aI = upload(P.a.I, s);
+    R->aJ = upload(P.a.J, s);
+    R->bI = upload(P.b.I, s);
+    R->bJ = upload(P.b.J, s);
+    R->dptr = upload(ptr, s);
+    R->didx = upload(idx, s);
+    R->dcf = upload(cf, s);
+    R->app = upload(P.ap_ptr, s);
+    R->bxp = upload(P.bx_ptr, s);
+    R->apd = upload(P.ap, s);
+    R->bxd = upload(P.bx, s);
+    R->aps = upload(P.ap_sign, s);
+    R->bxs = upload(P.bx_sign, s);
+    CIGPU_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+    return R;
+}
+
 void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double *ab, double *bb, cudaStream_t s) {
     if (c.method == CIGPU_DETS) {
         dets_rdm(c, c_dev, rdm1, aa, ab, bb, s);
@@ -481,67 +703,28 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
     const int64_t n1 = 2 * L2, n2 = (int64_t)np * np, n3 = L2 * L2;
     DevBuf<double> out(n1 + 2 * n2 + n3);
     double *o1 = out.p, *oaa = out.p + n1, *obb = out.p + n1 + n2, *oab = out.p + n1 + 2 * n2;
+    Trace tr("rdm", s);
     if (c.method == CIGPU_DOCI) {
         if (L * L > 1024) throw std::invalid_argument("DOCI RDM needs L <= 32");
         CIGPU_CUDA(cudaMemsetAsync(out.p, 0, sizeof(double) * out.n, s));
         const int G = sm_count() * 4;
         DevBuf<double> partial((size_t)G * 2 * L2);
-        const int th = ((L * L + 31) / 32) * 32;
+        const int th = ((L * (L + 1) / 2 + 31) / 32) * 32;  // one thread per pair j <= k
         k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial.p);
         k_doci_rdm_finish<<<(int)((L2 + 255) / 256), 256, 0, s>>>(partial.p, G, L, np, o1, oaa, oab, obb);
         CIGPU_CUDA(cudaGetLastError());
         count_launch(2);
         CIGPU_CUDA(cudaStreamSynchronize(s));
+        tr.mark("doci kernels");
     } else {
         if (L > 32) throw std::invalid_argument("FCI RDM needs L <= 32");
+        if (!c.rdm_plan) {
+            c.rdm_plan = make_fci_rdm_plan(c, s);
+            tr.mark("host plan");
+        }
+        const FciRdmPlan &R = *c.rdm_plan;
         const SpinTables &ta = c.ta;
         const SpinTables &tb = (c.ndown == c.nup) ? c.ta : c.tb;
-        Plan P;
-        P.L = L;
-        P.np = np;
-        P.Da = ta.D;
-        P.Db = tb.D;
-        P.off_ga = 0;
-        P.off_gb = L2;
-        P.off_g0 = 2 * L2;
-        P.off_g2 = P.off_g0 + n2;
-        P.off_g1 = P.off_g2 + n2;
-        P.nslots = P.off_g1 + n3;
-        // pair counts first (densities layout needs them)
-        auto count_pairs = [&](const SpinTables &t, size_t &npair, size_t &nz) {
-            size_t ns = 0, nd = 0;
-            for (int64_t I = 0; I < t.D; ++I) {
-                for (int q = 0; q < t.ns; ++q)
-                    if (t.s_target[(size_t)I * t.ns + q] > (uint32_t)I) ++ns;
-                for (int q = 0; q < t.nd; ++q)
-                    if (t.d_target[(size_t)I * t.nd + q] > (uint32_t)I) ++nd;
-            }
-            nz = (size_t)t.D + ns;
-            npair = nz + nd;
-        };
-        size_t npa, nza, npb, nzb;
-        count_pairs(ta, npa, nza);
-        count_pairs(tb, npb, nzb);
-        P.off_da0 = 0;
-        P.off_daz = npa;
-        P.off_db0 = P.off_daz + nza * L;
-        P.off_dbz = P.off_db0 + npb;
-        P.ndens = P.off_dbz + nzb * L;
-        P.terms.assign(P.nslots, {});
-        plan_spin(P, ta, true);
-        plan_spin(P, tb, false);
-        plan_ab(P, ta, tb);
-        if (P.a.I.size() != npa || P.b.I.size() != npb) throw std::runtime_error("rdm plan: pair count mismatch");
-        // CSR of the slot terms
-        std::vector<uint32_t> ptr(P.nslots + 1, 0), idx;
-        std::vector<int8_t> cf;
-        for (size_t q = 0; q < P.nslots; ++q) {
-            ptr[q + 1] = ptr[q] + (uint32_t)P.terms[q].size();
-            for (auto &e : P.terms[q]) {
-                idx.push_back(e.first);
-                cf.push_back(e.second);
-            }
-        }
         // C^T for the beta densities
         DevBuf<double> Ct((size_t)c.dim);
         {
@@ -549,25 +732,20 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
             k_transpose<<<grid, dim3(32, 8), 0, s>>>(c_dev, ta.D, tb.D, Ct.p);
             count_launch();
         }
-        DevBuf<uint64_t> sa = upload(ta.strings, s), sb = upload(tb.strings, s);
-        DevBuf<uint32_t> aI = upload(P.a.I, s), aJ = upload(P.a.J, s), bI = upload(P.b.I, s), bJ = upload(P.b.J, s);
-        DevBuf<double> dens(P.ndens);
+        DevBuf<double> dens(R.ndens);
         const int G = sm_count() * 8;
-        k_pair_dens<<<G, kRdmThreads, 0, s>>>(c_dev, tb.D, aI.p, aJ.p, (int64_t)npa, (int64_t)nza, sb.p, L,
-                                              dens.p + P.off_da0, dens.p + P.off_daz);
-        k_pair_dens<<<G, kRdmThreads, 0, s>>>(Ct.p, ta.D, bI.p, bJ.p, (int64_t)npb, (int64_t)nzb, sa.p, L,
-                                              dens.p + P.off_db0, dens.p + P.off_dbz);
+        k_pair_dens<<<G, kRdmThreads, 0, s>>>(c_dev, tb.D, R.aI.p, R.aJ.p, R.npa, R.nza, R.sb.p, L,
+                                              dens.p + R.off_da0, dens.p + R.off_daz);
+        k_pair_dens<<<G, kRdmThreads, 0, s>>>(Ct.p, ta.D, R.bI.p, R.bJ.p, R.npb, R.nzb, R.sa.p, L,
+                                              dens.p + R.off_db0, dens.p + R.off_dbz);
         count_launch(2);
-        DevBuf<uint32_t> dptr = upload(ptr, s), didx = upload(idx, s);
-        DevBuf<int8_t> dcf = upload(cf, s);
-        DevBuf<double> acc(P.nslots);
-        k_slot_gather<<<G, kRdmThreads, 0, s>>>(dptr.p, didx.p, dcf.p, dens.p, (int64_t)P.nslots, acc.p);
+        tr.mark("pair densities");
+        DevBuf<double> acc(R.nslots);
+        k_slot_gather<<<G, kRdmThreads, 0, s>>>(R.dptr.p, R.didx.p, R.dcf.p, dens.p, (int64_t)R.nslots, acc.p);
         count_launch();
+        tr.mark("slot sums");
         // alpha-beta doubles
-        const int nsplit = 4;
-        DevBuf<uint32_t> app = upload(P.ap_ptr, s), bxp = upload(P.bx_ptr, s);
-        DevBuf<uint64_t> apd = upload(P.ap, s), bxd = upload(P.bx, s);
-        DevBuf<int8_t> aps = upload(P.ap_sign, s), bxs = upload(P.bx_sign, s);
+        const int nsplit = R.nsplit;
         DevBuf<double> slices((size_t)std::max(np, 1) * nsplit * L2);
         if (np > 0) {
             const size_t sm = sizeof(double) * 2 * (size_t)tb.D;
@@ -577,12 +755,13 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
                 cudaFuncSetAttribute(k_ab_doubles, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             CIGPU_CUDA(attr);
             const int th = std::min(1024, (int)((L2 + 31) / 32 * 32));
-            k_ab_doubles<<<np * nsplit, th, sm, s>>>(c_dev, tb.D, app.p, apd.p, aps.p, bxp.p, bxd.p,
-                                                                      bxs.p, L, nsplit, slices.p);
+            k_ab_doubles<<<np * nsplit, th, sm, s>>>(c_dev, tb.D, R.app.p, R.apd.p, R.aps.p, R.bxp.p, R.bxd.p,
+                                                     R.bxs.p, L, nsplit, slices.p);
             count_launch();
         }
-        k_rdm_assemble<<<G, kRdmThreads, 0, s>>>(acc.p, slices.p, nsplit, L, np, P.off_ga, P.off_gb, P.off_g0, P.off_g1,
-                                                 P.off_g2, o1, oaa, oab, obb);
+        tr.mark("alpha-beta doubles");
+        k_rdm_assemble<<<G, kRdmThreads, 0, s>>>(acc.p, slices.p, nsplit, L, np, R.off_ga, R.off_gb, R.off_g0, R.off_g1,
+                                                 R.off_g2, o1, oaa, oab, obb);
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
         CIGPU_CUDA(cudaStreamSynchronize(s));
@@ -592,6 +771,7 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
     if (bb) CIGPU_CUDA(cudaMemcpyAsync(bb, obb, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
     if (ab) CIGPU_CUDA(cudaMemcpyAsync(ab, oab, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
     CIGPU_CUDA(cudaStreamSynchronize(s));
+    tr.mark("assemble + copy out");
 }
 
 int doci_pair_partials() { return sm_count() * 4; }
@@ -599,7 +779,7 @@ int doci_pair_partials() { return sm_count() * 4; }
 void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, double *Pm, double *Dm, cudaStream_t s) {
     if (c.method != CIGPU_DOCI || c.L > 32) throw std::invalid_argument("DOCI pair matrices need a DOCI CRS, L <= 32");
     const int L = c.L, G = doci_pair_partials();
-    const int th = ((L * L + 31) / 32) * 32;
+    const int th = ((L * (L + 1) / 2 + 31) / 32) * 32;  // one thread per pair j <= k
     k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial);
     k_doci_pairs_finish<<<(L * L + 255) / 256, 256, 0, s>>>(partial, G, L, Pm, Dm);
     CIGPU_CUDA(cudaGetLastError());

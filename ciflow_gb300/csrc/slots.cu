@@ -239,9 +239,35 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
 
 // ---------------------------------------------------------------------------
 // Fill: the same element values as the CRS generator, as FP32 hi + lo splits (zero
-// where |v| <= 1e-14), with each row's nonzero count and lower-triangle count.
+// where |v| <= 1e-14; F64 = false) or as FP64 values (zero where |v| <= 1e-14;
+// F64 = true, the plain method's tiles), with each row's nonzero count and
+// lower-triangle count.
+template <bool F64>
+struct FillVals;
+template <>
+struct FillVals<false> {  // FP32 hi + lo
+    float h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+    __device__ __forceinline__ void from_split(int j, const float *hi, const float *lo, size_t at) {
+        h[j] = __ldg(hi + at);
+        l[j] = __ldg(lo + at);
+    }
+    __device__ __forceinline__ bool nonzero(int j) const { return (__float_as_uint(h[j]) & 0x7FFFFFFFu) != 0u; }
+    __device__ __forceinline__ void clear(int j) { h[j] = l[j] = 0.0f; }
+};
+template <>
+struct FillVals<true> {  // FP64, |v| <= 1e-14 stored as zero
+    double v[4] = {0, 0, 0, 0};
+    __device__ __forceinline__ void set(int j, double x) {
+        v[j] = (x > kZero || x < -kZero) ? x : 0.0;
+    }
+    __device__ __forceinline__ bool nonzero(int j) const { return v[j] != 0.0; }
+    __device__ __forceinline__ void clear(int j) { v[j] = 0.0; }
+};
+
+template <bool F64>
 __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, float *__restrict__ hi,
-                                                             float *__restrict__ lo, uint32_t *__restrict__ count,
+                                                             float *__restrict__ lo, double *__restrict__ v64,
+                                                             uint32_t *__restrict__ count,
                                                              uint32_t *__restrict__ lower) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t cnt[kSplits][kTileRows], low[kSplits][kTileRows];
@@ -250,8 +276,10 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     const int L2 = p.L * p.L, nsa = p.a.ns;
     uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
     uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
+    // alpha-single integral slices: FP32 hi then lo (F64 = false) or FP64 (true), nsa * L2 each
     float *slhi = reinterpret_cast<float *>(st + p.b.ns * kTileRows);
     float *sllo = slhi + (size_t)nsa * L2;
+    double *sl64 = reinterpret_cast<double *>(slhi);
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
     const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
     stage_tile(p, m, ia, t, desc, st);
@@ -261,8 +289,12 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
             const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
             const int ar = (info >> 12) & 63, ac = (info >> 18) & 63;
             const size_t at = ((size_t)ar * p.L + ac) * L2 + tt;
-            slhi[i] = __ldg(p.eri_hi + at);
-            sllo[i] = __ldg(p.eri_lo + at);
+            if constexpr (F64) {
+                sl64[i] = __ldg(p.eri + at);
+            } else {
+                slhi[i] = __ldg(p.eri_hi + at);
+                sllo[i] = __ldg(p.eri_lo + at);
+            }
         }
     }
     __syncthreads();
@@ -279,19 +311,23 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     // one quad at a time; a quad lies in one segment, so the branch is uniform
     for (int c = c0; c < c1; ++c) {
         const int k0 = 4 * c;
-        float h4[4] = {0, 0, 0, 0}, l4[4] = {0, 0, 0, 0};
+        FillVals<F64> q;
         bool lw[4] = {false, false, false, false};  // column below the diagonal
         if (k0 < m.s1) {  // S0: the diagonal
-            h4[0] = p.diag_hi[r];
-            l4[0] = p.diag_lo[r];
+            if constexpr (F64) {
+                q.set(0, p.diag[r]);
+            } else {
+                q.h[0] = p.diag_hi[r];
+                q.l[0] = p.diag_lo[r];
+            }
         } else if (k0 < m.s2) {  // S1: beta singles (one_diff_orbital), precomputed per row
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int xb = k0 - m.s1 + j;
                 if (xb < nsb) {
                     const size_t at = (size_t)r * nsr + nsa + xb;
-                    h4[j] = __ldg(p.sgl_hi + at);
-                    l4[j] = __ldg(p.sgl_lo + at);
+                    if constexpr (F64) q.set(j, __ldg(p.sgl64 + at));
+                    else q.from_split(j, p.sgl_hi, p.sgl_lo, at);
                     lw[j] = st[xb * kTileRows + rr] < (uint32_t)ib;
                 }
             }
@@ -301,8 +337,8 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                 const int xb = k0 - m.s2 + j;
                 if (xb < ndb) {
                     const size_t at = ib * ndb + xb;
-                    h4[j] = __ldg(p.b.d_hi + at);
-                    l4[j] = __ldg(p.b.d_lo + at);
+                    if constexpr (F64) q.set(j, __ldg(p.b.d_val + at));
+                    else q.from_split(j, p.b.d_hi, p.b.d_lo, at);
                     lw[j] = __ldg(p.b.d_target + at) < (uint32_t)ib;
                 }
             }
@@ -312,12 +348,12 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                 const int i = k0 - m.s3 + j;
                 if (i < nsa) {
                     const size_t at = (size_t)r * nsr + i;
-                    h4[j] = __ldg(p.sgl_hi + at);
-                    l4[j] = __ldg(p.sgl_lo + at);
+                    if constexpr (F64) q.set(j, __ldg(p.sgl64 + at));
+                    else q.from_split(j, p.sgl_hi, p.sgl_lo, at);
                 } else if (i < nsa + nda) {
                     const size_t at = ia * nda + (i - nsa);
-                    h4[j] = __ldg(p.a.d_hi + at);
-                    l4[j] = __ldg(p.a.d_lo + at);
+                    if constexpr (F64) q.set(j, __ldg(p.a.d_val + at));
+                    else q.from_split(j, p.a.d_hi, p.a.d_lo, at);
                 }
                 lw[j] = (uint32_t)desc[k0 + j] < (uint32_t)ia;
             }
@@ -331,18 +367,29 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                     const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + xb);
                     const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
                     const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
-                    float h, l;
-                    if (p.staged) {
-                        h = slhi[xa * L2 + tt];
-                        l = sllo[xa * L2 + tt];
+                    if constexpr (F64) {
+                        double e;
+                        if (p.staged) {
+                            e = sl64[xa * L2 + tt];
+                        } else {
+                            const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
+                            e = __ldg(p.eri + ((size_t)ar * L + ac) * L2 + tt);
+                        }
+                        q.set(j, __longlong_as_double(__double_as_longlong(e) ^ ((long long)odd << 63)));
                     } else {
-                        const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
-                        const size_t at = ((size_t)ar * L + ac) * L2 + tt;
-                        h = __ldg(p.eri_hi + at);
-                        l = __ldg(p.eri_lo + at);
+                        float h, l;
+                        if (p.staged) {
+                            h = slhi[xa * L2 + tt];
+                            l = sllo[xa * L2 + tt];
+                        } else {
+                            const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
+                            const size_t at = ((size_t)ar * L + ac) * L2 + tt;
+                            h = __ldg(p.eri_hi + at);
+                            l = __ldg(p.eri_lo + at);
+                        }
+                        q.h[j] = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
+                        q.l[j] = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
                     }
-                    h4[j] = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
-                    l4[j] = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
                     lw[j] = (uint32_t)desc[k0 + j] < (uint32_t)ia;
                     if (++xb == nsb && j < 3) {
                         xb = 0;
@@ -354,14 +401,20 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            if (!active) h4[j] = l4[j] = 0.0f;
-            const bool keep = (__float_as_uint(h4[j]) & 0x7FFFFFFFu) != 0u;  // |v| > 1e-14
+            if (!active) q.clear(j);
+            const bool keep = q.nonzero(j);  // |v| > 1e-14
             n_keep += keep;
             n_low += keep && lw[j];
         }
         const int64_t at = ((qbase + c) * kTileRows + rr) * 4;
-        *reinterpret_cast<float4 *>(hi + at) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-        *reinterpret_cast<float4 *>(lo + at) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+        if constexpr (F64) {
+            double2 *d = reinterpret_cast<double2 *>(v64 + at);
+            d[0] = make_double2(q.v[0], q.v[1]);
+            d[1] = make_double2(q.v[2], q.v[3]);
+        } else {
+            *reinterpret_cast<float4 *>(hi + at) = make_float4(q.h[0], q.h[1], q.h[2], q.h[3]);
+            *reinterpret_cast<float4 *>(lo + at) = make_float4(q.l[0], q.l[1], q.l[2], q.l[3]);
+        }
     }
     cnt[ks][rr] = n_keep;
     low[ks][rr] = n_low;
@@ -410,12 +463,29 @@ void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *coun
     const size_t base = tile_smem(p), sl = slice_smem(p);
     p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
     static const bool attr_set = [] {  // thread-safe one-time init
-        cudaFuncSetAttribute(k_fill_slots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
+        cudaFuncSetAttribute(k_fill_slots<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
         return true;
     }();
     (void)attr_set;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    k_fill_slots<<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, hi, lo, count, lower);
+    k_fill_slots<false><<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, hi, lo, nullptr,
+                                                                                                count, lower);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void fill_slots64_launch(const FciParams &p0, double *v64, uint32_t *count, uint32_t *lower, cudaStream_t s) {
+    FciParams p = p0;
+    const size_t base = tile_smem(p), sl = slice_smem(p);  // an FP64 slice takes the bytes of hi + lo
+    p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
+    static const bool attr_set = [] {  // thread-safe one-time init
+        cudaFuncSetAttribute(k_fill_slots<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
+        return true;
+    }();
+    (void)attr_set;
+    const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
+    k_fill_slots<true><<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, nullptr, nullptr,
+                                                                                               v64, count, lower);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -438,6 +508,10 @@ void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float 
 void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, const float *x32,
                      double *y, cudaStream_t s) {
     launch_slots(p, HiLo{hi, lo, x, x32}, y, s);
+}
+
+void spmv_slots_f64(const FciParams &p, const double *val, const double *x, double *y, cudaStream_t s) {
+    launch_slots(p, Plain<double>{val, x}, y, s);
 }
 
 }  // namespace cigpu

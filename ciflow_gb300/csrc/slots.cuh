@@ -1,4 +1,5 @@
-// Values-only FCI layout of the mixed method ("slot tiles", slots.cu).
+// Values-only FCI layout ("slot tiles", slots.cu): FP32 hi + lo for the mixed
+// method, FP64 for the plain one.
 #pragma once
 
 #include "build.cuh"
@@ -15,6 +16,13 @@ int64_t slots_count(const FciParams &p);
 // Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p) and
 // each row's stored-nonzero count and lower-triangle count (count, lower: [dim]).
 void fill_slots_launch(const FciParams &p, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s);
+// Fills FP64 slot values (|v| <= 1e-14 stored as zero; needs the FP64 row singles
+// in p) and the same row counts: the plain method's tiles.
+void fill_slots64_launch(const FciParams &p, double *v64, uint32_t *count, uint32_t *lower, cudaStream_t s);
+// Whether FP64 tiles pay off: the tiles' padding rows add at most a quarter.
+inline bool slots64_pay(const FciParams &p) {
+    return ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * 4 <= 5 * p.Db;
+}
 // Sizes (elements) of the matvecs' staging tables: slot descriptors per alpha
 // string (uint64) and beta single targets per tile (uint32).
 int64_t slot_desc_count(const FciParams &p);
@@ -24,6 +32,8 @@ int64_t slot_st_count(const FciParams &p);
 void slot_tables_launch(const FciParams &p, uint64_t *desc, uint32_t *st, cudaStream_t s);
 // y = H x from FP32 slot values, FP32 x/y and accumulation.
 void spmv_slots_f32(const FciParams &p, const float *val, const float *x, float *y, cudaStream_t s);
+// FP64 y = H x from FP64 slot values (one DFMA per slot).
+void spmv_slots_f64(const FciParams &p, const double *val, const double *x, double *y, cudaStream_t s);
 // FP64 y = H x from the split slot values hi + lo; x32 is an FP32 copy of x.
 void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const double *x, const float *x32,
                      double *y, cudaStream_t s);

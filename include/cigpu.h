@@ -114,11 +114,14 @@ int cigpu_crs_destroy(cigpu_crs *crs);
 int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full);
 /* Device storage of the matrix (no reference counterpart; reported with matvec
  * measurements). CIGPU_LAYOUT_CRS: full symmetric CRS, stored = nnz_full values
- * with a 4-byte column each. CIGPU_LAYOUT_SLOTS (MIXED FCI): values only, every
- * structural slot of every row (zeros included, rows padded to tiles of 64 beta
- * strings), stored = that slot count; columns are regenerated from the string
- * tables. */
-enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1, CIGPU_LAYOUT_ONTHEFLY = 2 };
+ * with a 4-byte column each. CIGPU_LAYOUT_SLOTS (FCI): values only (FP32 hi + lo
+ * for MIXED, FP64 for FP64), every structural slot of every row (zeros included,
+ * rows padded to tiles of 64 beta strings), stored = that slot count; columns are
+ * regenerated from the string tables. CIGPU_LAYOUT_PAIRS (DOCI): no stored matrix,
+ * stored = 0; every matvec generates the pair hops from the pair strings and the
+ * L x L table K_jk = (jk|jk). CIGPU_LAYOUT_ONTHEFLY: determinant lists without a
+ * stored matrix. The explicit CRS of every layout is generated for the exports. */
+enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1, CIGPU_LAYOUT_ONTHEFLY = 2, CIGPU_LAYOUT_PAIRS = 3 };
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored);
 /* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
  * SparseMatrix_CRS.h:107-111): row[dim+1], col[nnz_upper], val[nnz_upper]. Host buffers. */

@@ -5,6 +5,8 @@ oracle) to FP64 round-off; E0 must match the reference ARPACK energy to 1e-8 Eh
 (plain FP64) and to 1e-6 Eh (mixed), including the DOCI known answer
 -15.225362047972723 (reference tests/src/TestDOCI.cpp:31).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -33,6 +35,47 @@ def test_mvprod_matches_reference_matvec(name, precision):
     scale = np.abs(y_ref).max()
     # FP64 product (from the split FP32 values hi + lo for the mixed CRS): summation order only
     assert np.abs(y - y_ref).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("L,n", [(8, 4), (10, 3), (12, 6), (14, 1), (9, 9), (16, 8), (33, 2)])
+@pytest.mark.parametrize("precision", [A.FP64, A.MIXED])
+def test_doci_matvec_matches_reference_matvec(L, n, precision):
+    """The DOCI matvec (MIXED: matrix-free, pair hops generated per row, here its
+    FP64 product; FP64: the CRS) equals the reference's Sym::mvprod over the DOCI
+    CRS (oracle restatement) to FP64 round-off, and its element counts equal the
+    CRS's."""
+    ints = make_integrals(L, n, n, nchol=8, seed=5 * L + n)
+    ref = O.build_upper(O.DOCI, ints)
+    m = build(DOCI, ints, precision).get_mat()
+    lay, stored = ctypes.c_int(), ctypes.c_int64()
+    A.check(A.lib().cigpu_crs_layout(m.handle, ctypes.byref(lay), ctypes.byref(stored)))
+    if precision == A.MIXED:
+        assert lay.value == A.LAYOUT_PAIRS and stored.value == 0
+    else:
+        assert lay.value == A.LAYOUT_CRS
+    dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    A.check(A.lib().cigpu_crs_dims(m.handle, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf)))
+    assert nu.value == ref.nnz and nf.value == 2 * ref.nnz - int(np.count_nonzero(ref.full_csr().diagonal()))
+    x = np.random.default_rng(11).standard_normal(m.n)
+    y_ref = O.sym_mvprod(ref, x)
+    y = m.mvprod(x)
+    assert np.abs(y - y_ref).max() <= 1e-12 * max(np.abs(y_ref).max(), 1.0)
+
+
+def test_doci_pair_matvec_fp32():
+    torch = pytest.importorskip("torch")
+    ints = make_integrals(12, 6, 6, nchol=8, seed=9)
+    ref = O.build_upper(O.DOCI, ints)
+    m = build(DOCI, ints, A.MIXED).get_mat()
+    x = np.random.default_rng(3).standard_normal(m.n)
+    y_ref = O.sym_mvprod(ref, x)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    m.mvprod_device(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy().astype(np.float64)
+    # FP32 K, x and accumulation over 37 terms per row
+    assert np.abs(y - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
 
 
 def test_fp32_device_matvec():
