@@ -120,3 +120,56 @@ def test_rotation_fixture_is_the_four_index_transform():
         eri = np.einsum("ap,bq,cr,ds,pqrs->abcd", U, U, U, U, ints.eri, optimize=True)
         assert np.abs(g[f"{tag}_h"] - h).max() <= 1e-12 * np.abs(h).max()
         assert np.abs(g[f"{tag}_eri"] - eri).max() <= 1e-12 * np.abs(eri).max()
+
+
+def test_c1_state_rdm_fixture():
+    """The RDMs of the c1 FP64 ground state (ARPACK on the reference CRS, the oracle's
+    DensFCI) satisfy CIDens::test_invariants: traces and E_dens = E0."""
+    from .helpers import load_golden
+    from ciflow_gb300.synthetic import config_integrals
+    meta, g = load_golden("c1")
+    ints = config_integrals("c1")
+    r1, aa, ab, bb = g["rdm1"], g["aa"], g["ab"], g["bb"]
+    N = ints.nup + ints.ndown
+    assert abs(np.trace(r1[0]) + np.trace(r1[1]) - N) < 1e-10
+    assert abs(np.trace(aa) + np.trace(ab) + np.trace(bb) - N * (N - 1) / 2) < 1e-8
+    assert abs(O.dens_energy(ints, r1, aa, ab, bb) - meta["state_rdm"]["e0"]) < 1e-9
+    assert abs(meta["state_rdm"]["e0"] - meta["e0"]) < 1e-10
+
+
+def test_calibration_fixture():
+    """The CPU-baseline calibration (tests/golden/calibration.json): ARPACK's matvec
+    count at the reference's settings and the reference/port time ratios for every
+    configuration, with ARPACK's E0 equal to the reference golden."""
+    with open(os.path.join(GOLDEN, "calibration.json")) as f:
+        cal = json.load(f)
+    assert cal["threads"] >= 1
+    for name in ("c0", "c4", "c2", "c1"):
+        rec = cal[name]
+        with open(os.path.join(GOLDEN, f"{name}.json")) as f:
+            meta = json.load(f)
+        assert rec["dim"] == meta["dim"]
+        assert rec["arpack_matvecs"] > 0
+        assert abs(rec["e0"] - meta["e0"]) < 1e-8 * max(1.0, abs(meta["e0"]))
+        assert rec["build_ratio_ref_over_port"] > 0 and rec["mvprod_ratio_ref_over_port"] > 0
+
+
+def test_port_is_not_slower_than_reference_c0():
+    """Timed here where the reference library exists: the reference's c0 build takes
+    at least as long as the port's (so a port-based CPU baseline, calibrated by the
+    committed ratios, does not understate the reference's time)."""
+    import time
+    if O.ref() is None:
+        pytest.skip("reference tree not available")
+    from ciflow_gb300.synthetic import config_integrals
+    ints = config_integrals("c0")
+    tr, tp = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = O.RefCI(O.FCI, ints=ints)
+        tr.append(time.perf_counter() - t0)
+        r.close()
+        t0 = time.perf_counter()
+        O.build_rows(O.FCI, ints, 0, 4900)
+        tp.append(time.perf_counter() - t0)
+    assert min(tr) >= 0.8 * min(tp)
