@@ -44,12 +44,12 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--cpu-full-solve", type=int, default=1,
                     help="1: also time one whole CPU solve of L=10 5a5b end to end (about 20 s)")
-    ap.add_argument("--served-requests", type=int, default=200,
-                    help="served-stream requests per form (0 skips the served stream)")
-    ap.add_argument("--served-rate", type=float, default=1000.0, help="Poisson arrival rate of the served stream (1/s)")
+    ap.add_argument("--served-requests", type=int, default=2000,
+                    help="served-stream requests per form and rate (0 skips the served stream)")
+    ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--served-inflight", type=int, default=8, help="server worker slots")
-    ap.add_argument("--served-low-rates", type=float, nargs="*", default=[30.0, 100.0],
-                    help="further arrival rates (1/s) for latencies below saturation")
+    ap.add_argument("--served-low-rates", type=float, nargs="*", default=[1000.0, 200.0, 50.0],
+                    help="further arrival rates (1/s), down to below saturation")
     ap.add_argument("--dets-orbitals", type=int, default=32,
                     help="orbitals of the CISD determinant-list section (0: skip); electrons per spin = L/4")
     ap.add_argument("--doci", type=int, default=1, help="1: the DOCI L=24 12-pair section (0 skips it)")
@@ -589,8 +589,13 @@ def run_cigpu(args, rank: int, world: int, dist):
     if args.served_requests > 0:
         from benchmarks.serve_bench import served as run_served
         barrier()
+        oracle_srv = None
+        if rank == 0:  # a sample of the rotated requests against the oracle, after the timed streams
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle as oracle_srv
         served = run_served(args.served_requests, args.served_rate, args.served_inflight, tol_mixed=args.tol,
-                            tol_fp64=args.tol, seed=4 + rank, extra_rates=tuple(args.served_low_rates))
+                            tol_fp64=args.tol, seed=4 + rank, extra_rates=tuple(args.served_low_rates),
+                            oracle=oracle_srv)
         if dist is not None:
             tm, tp = reduce_over_ranks([served["mixed"]["solves_per_s"], served["plain_fp64"]["solves_per_s"]],
                                        dist, "sum")
@@ -602,7 +607,11 @@ def run_cigpu(args, rank: int, world: int, dist):
     if args.batched_problems > 0:
         from benchmarks.batch_bench import run as run_batched
         barrier()
-        batched = run_batched(args.batched_problems, seed=rank)
+        oracle_mod = None
+        if rank == 0:  # the sample check against the oracle runs after the timed calls
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle as oracle_mod
+        batched = run_batched(args.batched_problems, seed=rank, oracle=oracle_mod)
 
     # orbital optimisation: the optimisers' set_ham -> solve loop on the device
     orbopt = None

@@ -8,8 +8,9 @@ integrals on the device (cigpu_ham_rotate) inside the measured path. Mixed
 with uneven problems of the batched-solve shape (L uniform in 6..12, FCI with
 1..L/2 electrons per spin or DOCI with 2..L/2 pairs) and a few L=12 6a6b
 requests. The same request list runs through the mixed FP32/FP64 form and the
-plain FP64 form; every mixed result carries |dE0| against the plain FP64 result
-of the same request, solved to a tighter tolerance.
+plain FP64 form; every result carries |dE0| against the plain FP64 result of the
+same request solved to a tighter tolerance, and a seeded sample of the rotated
+requests is checked against the oracle.
 
     python -m benchmarks.serve_bench --rate 1000 --requests 300
 """
@@ -119,12 +120,35 @@ def summarise(stream, results, wall):
     }
 
 
+def oracle_check(stream, res_m, res_p, oracle, sample: int, seed: int) -> dict:
+    """A seeded sample of the rotated L=10 requests against the oracle: the integrals
+    rotated on the host (synthetic.rotate_integrals, the transform the reference's
+    OrbitalTransform::fillHamCI performs, pinned by tests/golden/rotate.*), the
+    oracle's CRS and ARPACK (eigsh, tol 1e-12) on it."""
+    from ciflow_gb300.synthetic import rotate_integrals
+    O = oracle
+    idx = [i for i, s in enumerate(stream) if s[0] == "c4"]
+    pick = sorted(np.random.default_rng(seed + 99).choice(idx, size=min(sample, len(idx)), replace=False).tolist())
+    errs_m, errs_p = [], []
+    t0 = time.perf_counter()
+    for i in pick:
+        ints = rotate_integrals(stream[i][1], 0.05, seed=10**6 + i)
+        e_ref, _ = O.lowest_eigenpair(O.build_upper(O.FCI, ints), tol=1e-12)
+        e_ref += ints.econst
+        errs_m.append(abs(res_m[i]["e0"] - e_ref))
+        errs_p.append(abs(res_p[i]["e0"] - e_ref))
+    return {"requests": pick, "max_abs_dE0_vs_oracle": {"mixed": float(max(errs_m)), "plain_fp64": float(max(errs_p))},
+            "oracle_s": time.perf_counter() - t0}
+
+
 def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed: float = 1e-5,
            tol_fp64: float = 1e-5, tol_ref: float = 1e-8, every_big: int = 100, seed: int = 4,
-           ref_results=None, extra_rates=()):
+           ref_results=None, extra_rates=(), oracle=None, oracle_sample: int = 3):
     """Both forms over the same stream; the tighter FP64 pass gives each request's E0.
     `extra_rates`: further arrival rates at which both forms run the same stream
-    again, for latencies below saturation (summaries under "by_rate")."""
+    again, for latencies at and below saturation (summaries under "by_rate").
+    `oracle`: the oracle module (given by the caller) for a sample check of the
+    rotated requests, run after all timed streams."""
     stream = make_stream(n, seed=seed, every_big=every_big)
     res_m, wall_m = run_stream(stream, A.MIXED, rate, tol_mixed, max_inflight, seed=seed)
     res_p, wall_p = run_stream(stream, A.FP64, rate, tol_fp64, max_inflight, seed=seed)
@@ -159,6 +183,8 @@ def served(n: int = 300, rate: float = 1000.0, max_inflight: int = 8, tol_mixed:
         by_rate[str(r)] = row
     if by_rate:
         out["by_rate"] = by_rate
+    if oracle is not None and oracle_sample > 0:
+        out["oracle_sample"] = oracle_check(stream, res_m, res_p, oracle, oracle_sample, seed)
     return out
 
 

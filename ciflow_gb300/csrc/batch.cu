@@ -25,6 +25,7 @@
 // Problems above max_batched_dim go through cigpu_solve with their requested
 // precision, on worker streams that overlap with each other.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -50,6 +51,8 @@ constexpr int kChunkRows = 2048;     // rows per chunk of the segmented kernels
 constexpr int kRowThreads = 256;
 constexpr int kDotVecs = 8;          // basis vectors per dot-product block
 constexpr int64_t kDefaultMaxBatchedDim = 65536;
+// Worker threads (one stream each) for the problems above the batching limit.
+constexpr int kBigWorkers = 3;
 constexpr int64_t kMaxBatchRows = int64_t(1) << 22;  // rows per batch (basis: 40 x 4M doubles)
 
 // action codes written by the analysis kernel
@@ -743,10 +746,13 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
         }
         int hw = (int)std::thread::hardware_concurrency();
         const int nthreads = std::max(1, std::min({8, hw > 0 ? hw : 4, (int)small_idx.size()}));
+        // problems above the limit: the largest first, on kBigWorkers streams
+        std::stable_sort(big_idx.begin(), big_idx.end(), [&](int a, int b) { return items[a].dim > items[b].dim; });
+        const int nbig = std::max(1, std::min(kBigWorkers, (int)big_idx.size()));
         int device = 0;
         CIGPU_CUDA(cudaGetDevice(&device));
         // streams live until the call returns: the built matrices keep them
-        std::vector<cudaStream_t> wstreams(nthreads + 1, nullptr);
+        std::vector<cudaStream_t> wstreams(nthreads + nbig, nullptr);
         struct StreamsGuard {
             std::vector<cudaStream_t> &v;
             ~StreamsGuard() {
@@ -758,15 +764,19 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
             }
         } wguard{wstreams};
         for (auto &w : wstreams) CIGPU_CUDA(cudaStreamCreateWithFlags(&w, cudaStreamNonBlocking));
-        std::vector<int> failed(nthreads + 1, CIGPU_OK);
-        // Problems above the limit: one at a time, in their requested precision, on
-        // their own stream and thread. They are bandwidth-bound, so running several
-        // at once gains nothing; the batched problems (latency-bound) overlap them.
-        auto big_worker = [&]() {
+        std::vector<int> failed(nthreads + nbig, CIGPU_OK);
+        // Problems above the limit, in their requested precision: each worker thread
+        // takes the largest one left and solves it on its own stream, so the
+        // host-side parts (tables, the projected eigenproblems, the per-iteration
+        // reads) of one overlap the matvecs of another, and the batched problems
+        // (latency-bound) overlap them all.
+        std::atomic<size_t> next_big{0};
+        auto big_worker = [&](int wk) {
             cudaSetDevice(device);
-            cudaStream_t s = wstreams[nthreads];
+            cudaStream_t s = wstreams[nthreads + wk];
             StreamScope scope(s);
-            for (int i : big_idx) {
+            for (size_t nb = next_big.fetch_add(1); nb < big_idx.size(); nb = next_big.fetch_add(1)) {
+                const int i = big_idx[nb];
                 Item &it = items[i];
                 const cigpu_request &q = req[i];
                 int stc = cigpu_ham_create(q.L, q.nup, q.ndown, q.econst, q.h, q.eri, &it.ham);
@@ -788,17 +798,20 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 if (it.ham) cigpu_ham_destroy(it.ham);
                 it.ham = nullptr;
                 it.status = stc;
-                if (stc != CIGPU_OK && stc != CIGPU_ENOCONV && failed[nthreads] == CIGPU_OK) failed[nthreads] = stc;
+                if (stc != CIGPU_OK && stc != CIGPU_ENOCONV && failed[nthreads + wk] == CIGPU_OK)
+                    failed[nthreads + wk] = stc;
             }
             cudaStreamSynchronize(s);
         };
-        std::thread big_thread(big_worker);
+        std::vector<std::thread> big_threads;
         struct Joiner {
-            std::thread &t;
+            std::vector<std::thread> &t;
             ~Joiner() {
-                if (t.joinable()) t.join();
+                for (auto &th : t)
+                    if (th.joinable()) th.join();
             }
-        } big_join{big_thread};
+        } big_join{big_threads};
+        for (int wk = 0; wk < nbig && !big_idx.empty(); ++wk) big_threads.emplace_back(big_worker, wk);
         // build the batched problems on worker streams
         auto worker = [&](int t) {
             cudaSetDevice(device);
@@ -852,7 +865,7 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                 }
             }
         }
-        big_thread.join();
+        for (auto &th : big_threads) th.join();
         for (int f : failed)
             if (f != CIGPU_OK && first_err == CIGPU_OK) first_err = f;
         for (auto &it : items) {

@@ -51,9 +51,15 @@ def test_batch_matches_single_solves_and_splits_by_size():
     e0, infos, status, stats = solve_batch(probs, tol=1e-7, max_batched_dim=5000)
     assert stats["batched"] + stats["individual"] == len(probs)
     assert stats["batched"] > 0 and stats["individual"] > 0
-    for (ints, m, _), e, st in zip(probs, e0, status):
+    for (ints, m, _), e, st, inf in zip(probs, e0, status, infos):
         assert st == A.OK
         assert abs(e - single_e0(ints, m)) <= 1e-6  # mixed single solves: |dE0| <= 1e-6
+        n = O.dim(O.DOCI if m == A.DOCI else O.FCI, ints.L, ints.nup, ints.ndown)
+        # the lockstep solves FP64; the problems above the limit keep MIXED
+        assert inf["precision"] == (A.FP64 if n <= 5000 else A.MIXED)
+        if n <= 20000:  # against the oracle's ARPACK eigenpair of the reference CRS
+            e_ref, _ = O.lowest_eigenpair(O.build_upper(O.DOCI if m == A.DOCI else O.FCI, ints), tol=1e-12)
+            assert abs(e - (e_ref + ints.econst)) <= 1e-6
 
 
 def test_batch_twice_same_result_and_rejects_bad_requests():
