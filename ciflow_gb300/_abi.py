@@ -11,6 +11,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libcigpu.so")
+CHECKED_LIB_PATH = os.path.join(HERE, "_lib", "libcigpu_checked.so")
 
 OK, EINVAL, ENOMEM, EAGAIN, ECANCELED, ETIMEDOUT, ENOTSUP, ENOCONV, ECUDA, ENOTFOUND = (
     0, 22, 12, 11, 125, 110, 95, 200, 201, 202)
@@ -87,6 +88,8 @@ SIGNATURES = {
     "cigpu_strerror": (ctypes.c_char_p, [_I]),
     "cigpu_device_count": (_I, [_P]),
     "cigpu_kernel_launches": (_I64, []),
+    "cigpu_checked_build": (_I, []),
+    "cigpu_check_word": (_I, [_P, _I]),
     "cigpu_ham_create": (_I, [_I, _I, _I, _D, _P, _P, _P]),
     "cigpu_ham_destroy": (_I, [_P]),
     "cigpu_ham_rotate": (_I, [_P, _P, _P, _P]),
@@ -131,6 +134,7 @@ SIGNATURES = {
 }
 
 _lib = None
+_lib_checked = None
 
 
 class CigpuError(RuntimeError):
@@ -140,20 +144,33 @@ class CigpuError(RuntimeError):
         super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
 
 
+def _load(path: str):
+    if not os.path.exists(path):
+        raise ImportError(f"{os.path.basename(path)} is missing ({path}); build it with "
+                          "`python -m ciflow_gb300.build` (nvcc, sm_103a)")
+    l = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(l, name)
+        f.restype = res
+        f.argtypes = args
+    return l
+
+
 def lib():
     """The loaded library; raises if the CUDA extension has not been built."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise ImportError(f"libcigpu.so is missing ({LIB_PATH}); build it with "
-                              "`python -m ciflow_gb300.build` (nvcc, sm_103a)")
-        l = ctypes.CDLL(LIB_PATH)
-        for name, (res, args) in SIGNATURES.items():
-            f = getattr(l, name)
-            f.restype = res
-            f.argtypes = args
-        _lib = l
+        _lib = _load(LIB_PATH)
     return _lib
+
+
+def checked_lib():
+    """The checked build (bounds checks recorded in a device error word), loaded
+    beside the regular library."""
+    global _lib_checked
+    if _lib_checked is None:
+        _lib_checked = _load(CHECKED_LIB_PATH)
+    return _lib_checked
 
 
 def check(status: int, what: str = "") -> None:

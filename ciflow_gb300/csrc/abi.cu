@@ -11,6 +11,9 @@
 #include <stdexcept>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
+#include "checked.cuh"
 #include "crs.cuh"
 #include "spmv.cuh"
 
@@ -176,18 +179,47 @@ static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Every Trace is also an NVTX range ("cigpu <scope>") with a marker at each phase
+// end, so a profiler timeline shows the phases without CIGPU_TRACE.
 Trace::Trace(const char *sc, cudaStream_t st) : scope(sc), s(st) {
     const char *e = std::getenv("CIGPU_TRACE");
     on = e && e[0] == '1';
     t0 = now_s();
+    char name[64];
+    std::snprintf(name, sizeof(name), "cigpu %s", sc);
+    nvtxRangePushA(name);
 }
 
+Trace::~Trace() { nvtxRangePop(); }
+
 void Trace::mark(const char *what) {
+    nvtxMarkA(what);
     if (!on) return;
     cudaStreamSynchronize(s);
     const double t = now_s();
     std::fprintf(stderr, "[cigpu %s] %-24s %9.3f ms\n", scope, what, (t - t0) * 1e3);
     t0 = t;
+}
+
+// The checked build's error word, one per device, allocated and cleared on first use.
+unsigned long long *check_word_device() {
+#if CIGPU_CHECKED_BUILD
+    constexpr int kMaxDev = 64;
+    static std::mutex mu;
+    static unsigned long long *words[kMaxDev] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!words[dev]) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+        words[dev] = static_cast<unsigned long long *>(p);
+    }
+    return words[dev];
+#else
+    return nullptr;
+#endif
 }
 
 int status_from_exception() {
@@ -582,6 +614,22 @@ using namespace cigpu;
 extern "C" {
 
 int cigpu_get_version(void) { return CIGPU_ABI_VERSION; }
+
+int cigpu_checked_build(void) { return CIGPU_CHECKED_BUILD; }
+
+int cigpu_check_word(uint64_t *word, int reset) {
+    if (!word) return CIGPU_EINVAL;
+    *word = 0;
+    if (!CIGPU_CHECKED_BUILD) return CIGPU_ENOTSUP;
+    unsigned long long *w = check_word_device();
+    if (!w) return CIGPU_ECUDA;
+    unsigned long long h = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess) return CIGPU_ECUDA;
+    if (cudaMemcpy(&h, w, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return CIGPU_ECUDA;
+    if (reset && cudaMemset(w, 0, sizeof(*w)) != cudaSuccess) return CIGPU_ECUDA;
+    *word = h;
+    return CIGPU_OK;
+}
 
 const char *cigpu_strerror(int st) {
     switch (st) {

@@ -86,6 +86,9 @@ struct Trace {
     bool on;
     double t0;
     Trace(const char *sc, cudaStream_t st);
+    ~Trace();
+    Trace(const Trace &) = delete;
+    Trace &operator=(const Trace &) = delete;
     void mark(const char *what);
 };
 

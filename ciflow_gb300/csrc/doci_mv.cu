@@ -164,7 +164,13 @@ __global__ void __launch_bounds__(kMvThreads) k_doci_mv(const DociMv p, const T 
             T xv[kHopBatch];
 #pragma unroll
             for (int u = 0; u < kHopBatch; ++u)
-                if (u < nu) xv[u] = J[u] < (uint64_t)p.D ? __ldg(x + J[u]) : (T)0;
+                if (u < nu) {
+                    // 0xFFFFFFFF marks a lane without a hop this round; any other rank
+                    // outside the space is a violation (skipped in every build)
+                    bool ok = index_ok(J[u], (uint64_t)p.D);
+                    if (J[u] != 0xFFFFFFFFu) ok = CIGPU_CHECK(p.err, ok, kCheckHopRank, J[u]) && ok;
+                    xv[u] = ok ? __ldg(x + J[u]) : (T)0;
+                }
 #pragma unroll
             for (int u = 0; u < kHopBatch; ++u)
                 if (u < nu) acc += kv[u] * xv[u];
@@ -200,7 +206,9 @@ __global__ void k_count_nonzero(const double *__restrict__ v, int64_t n, unsigne
 }
 
 template <typename T, int G>
-void launch_mv_g(const DociMv &p, const T *K, const T *diag, const T *x, T *y, cudaStream_t s) {
+void launch_mv_g(const DociMv &p0, const T *K, const T *diag, const T *x, T *y, cudaStream_t s) {
+    DociMv p = p0;
+    p.err = check_word_device();
     const size_t sm = sizeof(T) * (size_t)p.L * p.L;
     static const bool attr_set = [] {  // thread-safe one-time init (L = 63: 31 KB of FP64 K)
         cudaFuncSetAttribute(k_doci_mv<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "build.cuh"
+#include "checked.cuh"
 
 namespace cigpu {
 
@@ -9,6 +10,7 @@ struct DociMv {
     int L, n;                  // orbitals, electron pairs (n <= 32)
     int64_t D;                 // pair strings (rows)
     const uint64_t *strings;   // [D], colex order
+    unsigned long long *err = nullptr;  // checked build: the error word
 };
 
 // K_jk = (jk|jk) for j != k, zero where |v| <= 1e-14 (and on the diagonal): the

@@ -35,6 +35,7 @@
 #include <mutex>
 #include <stdexcept>
 
+#include "checked.cuh"
 #include "crs.cuh"
 
 namespace cigpu {
@@ -272,13 +273,20 @@ void plan_ab(Plan &P, const SpinTables &ta, const SpinTables &tb) {
 __global__ void k_pair_dens(const double *__restrict__ C, int64_t D2, const uint32_t *__restrict__ pI,
                             const uint32_t *__restrict__ pJ, int64_t npairs, int64_t nz,
                             const uint64_t *__restrict__ other, int L, double *__restrict__ d0,
-                            double *__restrict__ dz) {
+                            double *__restrict__ dz, int64_t D1, unsigned long long *err) {
     const int lane = threadIdx.x & 31;
     const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t p = wid; p < npairs; p += nw) {
-        const double *ri = C + (int64_t)pI[p] * D2;
-        const double *rj = C + (int64_t)pJ[p] * D2;
+        const uint32_t I = pI[p], J = pJ[p];
+        if (!CIGPU_CHECK(err, index_ok(I, (uint64_t)D1) && index_ok(J, (uint64_t)D1), kCheckRdmPair, p)) {
+            if (lane == 0) d0[p] = 0;  // the same for the whole warp
+            if (p < nz)
+                for (int z = lane; z < L; z += 32) dz[p * L + z] = 0;
+            continue;
+        }
+        const double *ri = C + (int64_t)I * D2;
+        const double *rj = C + (int64_t)J * D2;
         double acc = 0;
         for (int64_t b = lane; b < D2; b += 32) acc += ri[b] * rj[b];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -298,10 +306,13 @@ __global__ void k_pair_dens(const double *__restrict__ C, int64_t D2, const uint
 // Step 2: per-slot ordered sums of +/- densities.
 __global__ void k_slot_gather(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ idx,
                               const int8_t *__restrict__ coef, const double *__restrict__ dens, int64_t nslots,
-                              double *__restrict__ acc) {
+                              double *__restrict__ acc, int64_t ndens, unsigned long long *err) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nslots; s += (int64_t)gridDim.x * blockDim.x) {
         double v = 0;
-        for (uint32_t e = ptr[s]; e < ptr[s + 1]; ++e) v += (double)coef[e] * dens[idx[e]];
+        for (uint32_t e = ptr[s]; e < ptr[s + 1]; ++e) {
+            const uint32_t k = idx[e];
+            if (CIGPU_CHECK(err, index_ok(k, (uint64_t)ndens), kCheckRdmTerm, e)) v += (double)coef[e] * dens[k];
+        }
         acc[s] = v;
     }
 }
@@ -311,7 +322,8 @@ __global__ void k_slot_gather(const uint32_t *__restrict__ ptr, const uint32_t *
 __global__ void k_ab_doubles(const double *__restrict__ C, int64_t Db, const uint32_t *__restrict__ ap_ptr,
                              const uint64_t *__restrict__ ap, const int8_t *__restrict__ ap_sign,
                              const uint32_t *__restrict__ bx_ptr, const uint64_t *__restrict__ bx,
-                             const int8_t *__restrict__ bx_sign, int L, int nsplit, double *__restrict__ slices) {
+                             const int8_t *__restrict__ bx_sign, int L, int nsplit, double *__restrict__ slices,
+                             int64_t Da, unsigned long long *err) {
     extern __shared__ double rows[];  // [2][Db]
     const int q = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
     const uint32_t a0 = ap_ptr[q], a1 = ap_ptr[q + 1];
@@ -323,6 +335,10 @@ __global__ void k_ab_doubles(const double *__restrict__ C, int64_t Db, const uin
     for (int i = 0; i < kMaxTypesPerThread; ++i) acc[i] = 0;
     for (uint32_t e = s0; e < s1; ++e) {
         const uint64_t pr = ap[e];
+        // the same pair for the whole block, so a skip keeps the barriers aligned
+        if (!CIGPU_CHECK(err, index_ok((uint32_t)pr, (uint64_t)Da) && index_ok((uint32_t)(pr >> 32), (uint64_t)Da),
+                         kCheckRdmPair, e))
+            continue;
         const double *ri = C + (int64_t)(uint32_t)pr * Db;
         const double *rj = C + (int64_t)(uint32_t)(pr >> 32) * Db;
         __syncthreads();
@@ -338,6 +354,9 @@ __global__ void k_ab_doubles(const double *__restrict__ C, int64_t Db, const uin
             double part = 0;
             for (uint32_t x = bx_ptr[ty]; x < bx_ptr[ty + 1]; ++x) {
                 const uint64_t bb = bx[x];
+                if (!CIGPU_CHECK(err, index_ok((uint32_t)bb, (uint64_t)Db) && index_ok((uint32_t)(bb >> 32), (uint64_t)Db),
+                                 kCheckRdmExcit, x))
+                    continue;
                 part += (double)bx_sign[x] * rows[(uint32_t)bb] * rows[Db + (uint32_t)(bb >> 32)];
             }
             acc[i] += sa * part;
@@ -442,7 +461,7 @@ __device__ __forceinline__ long long fxmul(long long a, long long b) {
 }
 
 __global__ void k_doci_rdm(const double *__restrict__ c, const uint64_t *__restrict__ strings, int64_t D, int L,
-                           int n, double *__restrict__ partial) {
+                           int n, double *__restrict__ partial, unsigned long long *err) {
     __shared__ uint32_t binom[(kDociMaxL + 1) * (kDociMaxL + 2)];  // C(nn, kk), nn <= L, kk <= n + 1
     __shared__ uint64_t ss[kDociChunk];
     __shared__ long long cs[kDociChunk], cs2[kDociChunk];  // c_I * 2^62, c_I^2 * 2^60
@@ -505,6 +524,7 @@ __global__ void k_doci_rdm(const double *__restrict__ c, const uint64_t *__restr
                             const int a = __popcll(st & below_j), b = __popcll(st & below_k);
                             rr[u] = (uint32_t)(base + i) - binom[j * BW + a + 1] + pre[i][b] - pre[i][a + 1] +
                                     binom[k * BW + b];
+                            if (!CIGPU_CHECK(err, index_ok(rr[u], (uint64_t)D), kCheckHopRank, rr[u])) rr[u] = 0xFFFFFFFFu;
                         }
                     }
                 }
@@ -710,7 +730,7 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
         const int G = sm_count() * 4;
         DevBuf<double> partial((size_t)G * 2 * L2);
         const int th = ((L * (L + 1) / 2 + 31) / 32) * 32;  // one thread per pair j <= k
-        k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial.p);
+        k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial.p, check_word_device());
         k_doci_rdm_finish<<<(int)((L2 + 255) / 256), 256, 0, s>>>(partial.p, G, L, np, o1, oaa, oab, obb);
         CIGPU_CUDA(cudaGetLastError());
         count_launch(2);
@@ -734,14 +754,16 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
         }
         DevBuf<double> dens(R.ndens);
         const int G = sm_count() * 8;
+        unsigned long long *ew = check_word_device();
         k_pair_dens<<<G, kRdmThreads, 0, s>>>(c_dev, tb.D, R.aI.p, R.aJ.p, R.npa, R.nza, R.sb.p, L,
-                                              dens.p + R.off_da0, dens.p + R.off_daz);
+                                              dens.p + R.off_da0, dens.p + R.off_daz, ta.D, ew);
         k_pair_dens<<<G, kRdmThreads, 0, s>>>(Ct.p, ta.D, R.bI.p, R.bJ.p, R.npb, R.nzb, R.sa.p, L,
-                                              dens.p + R.off_db0, dens.p + R.off_dbz);
+                                              dens.p + R.off_db0, dens.p + R.off_dbz, tb.D, ew);
         count_launch(2);
         tr.mark("pair densities");
         DevBuf<double> acc(R.nslots);
-        k_slot_gather<<<G, kRdmThreads, 0, s>>>(R.dptr.p, R.didx.p, R.dcf.p, dens.p, (int64_t)R.nslots, acc.p);
+        k_slot_gather<<<G, kRdmThreads, 0, s>>>(R.dptr.p, R.didx.p, R.dcf.p, dens.p, (int64_t)R.nslots, acc.p,
+                                                (int64_t)R.ndens, ew);
         count_launch();
         tr.mark("slot sums");
         // alpha-beta doubles
@@ -756,7 +778,7 @@ void crs_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, double
             CIGPU_CUDA(attr);
             const int th = std::min(1024, (int)((L2 + 31) / 32 * 32));
             k_ab_doubles<<<np * nsplit, th, sm, s>>>(c_dev, tb.D, R.app.p, R.apd.p, R.aps.p, R.bxp.p, R.bxd.p,
-                                                     R.bxs.p, L, nsplit, slices.p);
+                                                     R.bxs.p, L, nsplit, slices.p, ta.D, ew);
             count_launch();
         }
         tr.mark("alpha-beta doubles");
@@ -780,7 +802,7 @@ void doci_pair_matrices(cigpu_crs &c, const double *c_dev, double *partial, doub
     if (c.method != CIGPU_DOCI || c.L > 32) throw std::invalid_argument("DOCI pair matrices need a DOCI CRS, L <= 32");
     const int L = c.L, G = doci_pair_partials();
     const int th = ((L * (L + 1) / 2 + 31) / 32) * 32;  // one thread per pair j <= k
-    k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial);
+    k_doci_rdm<<<G, th, 0, s>>>(c_dev, c.strings.p, c.dim, L, c.nup, partial, check_word_device());
     k_doci_pairs_finish<<<(L * L + 255) / 256, 256, 0, s>>>(partial, G, L, Pm, Dm);
     CIGPU_CUDA(cudaGetLastError());
     count_launch(2);
@@ -867,7 +889,7 @@ extern "C" int cigpu_rdm_doci_noalloc(cigpu_crs *crs, const double *c, double *r
         cudaMemsetAsync(rdm2_ab, 0, sizeof(double) * L2 * L2, s) != cudaSuccess)
         return CIGPU_ECUDA;
     const int th = (int)((L2 + 31) / 32 * 32);
-    k_doci_rdm<<<G, th, 0, s>>>(c, crs->strings.p, crs->dim, L, crs->nup, scratch);
+    k_doci_rdm<<<G, th, 0, s>>>(c, crs->strings.p, crs->dim, L, crs->nup, scratch, nullptr);  // no error word: allocates nothing
     k_doci_rdm_finish<<<(int)((L2 + 255) / 256), 256, 0, s>>>(scratch, G, L, np, rdm1, rdm2_aa, rdm2_ab, rdm2_bb);
     if (cudaGetLastError() != cudaSuccess) return CIGPU_ECUDA;
     count_launch(2);

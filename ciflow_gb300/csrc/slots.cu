@@ -435,7 +435,10 @@ size_t tile_smem(const FciParams &p) { return (size_t)slot_map(p).wp * 8 + (size
 size_t slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
 
 template <typename F>
-void launch_slots(const FciParams &p, const F &f, typename F::X *y, cudaStream_t s) {
+void launch_slots(const FciParams &p, const F &f0, typename F::X *y, cudaStream_t s) {
+    F f = f0;
+    f.nx = (uint64_t)(p.a.D * p.Db);
+    f.err = check_word_device();
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_spmv_slots<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
         return true;

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_rows(int64_t n, const int
             sn = __ldg(row_ptr + rn);
             en = __ldg(row_ptr + rn + 1);
         }
-        if (!m.skip(r)) {  // the same for the G lanes of the row
+        if (!m.skip(r) && CIGPU_CHECK(f.err, row_ok(s, e, n), kCheckRowBounds, r)) {  // the same for the row's lanes
             typename F::Acc acc{};
             const int64_t s4 = (s + 3) & ~(int64_t)3;
             const int64_t head_end = s4 < e ? s4 : e;
@@ -135,8 +135,11 @@ int sm_count_spmv() {
 // the rows once (at most a full persistent grid), so a small matrix leaves SMs
 // free for the kernels of concurrent solves on other streams.
 template <typename F>
-static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const F &f,
+static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const uint32_t *col, const F &f0,
                         typename F::X *y, cudaStream_t s) {
+    F f = f0;
+    f.nx = (uint64_t)n;
+    f.err = check_word_device();
     const double chunks = n > 0 ? (double)nnz / n / 4.0 : 0;
     const int G = chunks >= 48 ? 32 : 8;  // DOCI L=24 (36 chunks): 8 lanes 19% over 16
     const int64_t need = (n * G + kSpmvThreads - 1) / kSpmvThreads;
@@ -153,7 +156,9 @@ static void launch_rows(int64_t n, int64_t nnz, const int64_t *row_ptr, const ui
 
 void spmv_f64_shape(int64_t n, const int64_t *row_ptr, const uint32_t *col, const double *val, const double *x,
                     double *y, int lanes, int grid, cudaStream_t s, const int *row_prob, const int *status) {
-    const Plain<double> f{val, x};
+    Plain<double> f{val, x};
+    f.nx = (uint64_t)n;
+    f.err = check_word_device();
     using P = Plain<double>;
     if (row_prob) {
         const ActiveRows m{row_prob, status};

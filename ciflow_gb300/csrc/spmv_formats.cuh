@@ -2,6 +2,7 @@
 // matvec (slots.cu).
 #pragma once
 
+#include "checked.cuh"
 #include "cigpu_internal.h"
 
 namespace cigpu {
@@ -26,6 +27,8 @@ struct Plain {
     using X = VT;
     const VT *__restrict__ val;
     const VT *__restrict__ x;
+    uint64_t nx = ~(uint64_t)0;           // length of x (checked build: columns are tested against it)
+    unsigned long long *err = nullptr;    // checked build: the error word
     struct Acc {  // value-initialise (Acc a{}) to zero
         VT s;
     };
@@ -41,9 +44,11 @@ struct Plain {
     }
     __device__ __forceinline__ void zero(Chunk &c) const { c.v[0] = c.v[1] = c.v[2] = c.v[3] = 0; }
     __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
+        if (!CIGPU_CHECK(err, index_ok((uint64_t)col, nx), kCheckColumn, col)) return;
         a.s += c.v[j] * __ldg(x + col);
     }
     __device__ __forceinline__ void term1(int64_t at, int64_t col, Acc &a) const {
+        if (!CIGPU_CHECK(err, index_ok((uint64_t)col, nx), kCheckColumn, col)) return;
         a.s += __ldcs(val + at) * __ldg(x + col);
     }
     __device__ __forceinline__ void reduce(Acc &a, unsigned mask, int o) const { a.s += __shfl_xor_sync(mask, a.s, o); }
@@ -91,6 +96,8 @@ struct HiLo {
     const float *__restrict__ lo;
     const double *__restrict__ x;
     const float *__restrict__ x32;  // FP32 copy of x
+    uint64_t nx = ~(uint64_t)0;           // length of x (checked build: columns are tested against it)
+    unsigned long long *err = nullptr;    // checked build: the error word
     struct Acc {  // value-initialise (Acc a{}) to zero
         double d;
         float f;
@@ -112,12 +119,14 @@ struct HiLo {
     }
     __device__ __forceinline__ void zero(Chunk &c) const { c.h = c.l = make_float4(0, 0, 0, 0); }
     __device__ __forceinline__ void term(const Chunk &c, int j, int64_t col, Acc &a) const {
+        if (!CIGPU_CHECK(err, index_ok((uint64_t)col, nx), kCheckColumn, col)) return;
         const float h = j == 0 ? c.h.x : j == 1 ? c.h.y : j == 2 ? c.h.z : c.h.w;
         const float l = j == 0 ? c.l.x : j == 1 ? c.l.y : j == 2 ? c.l.z : c.l.w;
         a.d = ::fma(f2d_bits(h), __ldg(x + col), a.d);
         a.f = fmaf(l, __ldg(x32 + col), a.f);
     }
     __device__ __forceinline__ void term1(int64_t at, int64_t col, Acc &a) const {
+        if (!CIGPU_CHECK(err, index_ok((uint64_t)col, nx), kCheckColumn, col)) return;
         a.d = ::fma(f2d_bits(__ldcs(hi + at)), __ldg(x + col), a.d);
         a.f = fmaf(__ldcs(lo + at), __ldg(x32 + col), a.f);
     }

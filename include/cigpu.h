@@ -80,6 +80,18 @@ const char *cigpu_strerror(int status);
 int cigpu_device_count(int *count);
 /* Kernels this library launched since load (for launch accounting). */
 int64_t cigpu_kernel_launches(void);
+/* The checked build (libcigpu_checked.so, compiled with -DCIGPU_CHECKED) tests every
+ * index its kernels derive from stored data before using it (matvec columns, CRS row
+ * bounds, DOCI hop ranks, RDM pair / term / excitation indices), skips a failing
+ * access and records the first violation in a per-device error word: code << 56 |
+ * index (codes: 1 column, 2 row bounds, 3 hop rank, 4 RDM pair, 5 RDM term, 6 RDM
+ * excitation). The reference asserts the same bounds in its accessors
+ * (matrix.cpp:676-677, SparseMatrix_CRS.cpp:691-693) and exits on a failure.
+ * cigpu_checked_build returns 1 in the checked build, 0 otherwise. cigpu_check_word
+ * waits for the device and reads (reset != 0: then clears) the current device's
+ * word (0: no violation); CIGPU_ENOTSUP in the regular build. */
+int cigpu_checked_build(void);
+int cigpu_check_word(uint64_t *word, int reset);
 
 /* ---- Hamiltonian: replaces Hamiltonian(L, nGroup=0, nup, ndown, Econst) plus
  * setTmat/setVmat (Hamiltonian.cpp:77-113, 255-320) and the getTmat/getVmat

@@ -95,3 +95,18 @@ def test_unitary_exp_matches_scipy(lib):
     assert lib.cigpu_unitary_exp(3, A.ptr(bad), A.ptr(np.empty((3, 3)))) == A.EINVAL
     assert lib.cigpu_ham_rotate(None, None, None, None) == A.EINVAL
     assert lib.cigpu_ham_export(None, None, None) == A.EINVAL
+
+
+def test_checked_build_exports_and_flags(lib):
+    """The bounds-checked build loads beside the regular one, exports the same
+    symbols, and says which it is; the regular build has no error word."""
+    if not os.path.exists(A.CHECKED_LIB_PATH):
+        from ciflow_gb300 import build
+        build.build()
+    chk = A.checked_lib()
+    for s in declared_symbols():
+        assert hasattr(chk, s), s
+    assert lib.cigpu_checked_build() == 0 and chk.cigpu_checked_build() == 1
+    w = ctypes.c_uint64(7)
+    assert lib.cigpu_check_word(ctypes.byref(w), 0) == A.ENOTSUP and w.value == 0
+    assert chk.cigpu_check_word(None, 0) == A.EINVAL
