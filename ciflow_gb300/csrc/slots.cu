@@ -256,12 +256,16 @@ struct FillVals<false> {  // FP32 hi + lo
 };
 template <>
 struct FillVals<true> {  // FP64, |v| <= 1e-14 stored as zero
-    double v[4] = {0, 0, 0, 0};
+    // the threshold test and the zero test on the bit patterns (integer pipe): FP64
+    // compares, two per element, left the fill bound by GB300's FP64 pipe
+    uint64_t b[4] = {0, 0, 0, 0};
     __device__ __forceinline__ void set(int j, double x) {
-        v[j] = (x > kZero || x < -kZero) ? x : 0.0;
+        const uint64_t u = (uint64_t)__double_as_longlong(x);
+        b[j] = (u & 0x7FFFFFFFFFFFFFFFull) > 0x3D06849B86A12B9Bull ? u : 0ull;  // bits of 1e-14
     }
-    __device__ __forceinline__ bool nonzero(int j) const { return v[j] != 0.0; }
-    __device__ __forceinline__ void clear(int j) { v[j] = 0.0; }
+    __device__ __forceinline__ bool nonzero(int j) const { return b[j] != 0ull; }
+    __device__ __forceinline__ void clear(int j) { b[j] = 0ull; }
+    __device__ __forceinline__ double v(int j) const { return __longlong_as_double((long long)b[j]); }
 };
 
 template <bool F64>
@@ -276,13 +280,33 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     const int L2 = p.L * p.L, nsa = p.a.ns;
     uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
     uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
-    // alpha-single integral slices: FP32 hi then lo (F64 = false) or FP64 (true), nsa * L2 each
-    float *slhi = reinterpret_cast<float *>(st + p.b.ns * kTileRows);
-    float *sllo = slhi + (size_t)nsa * L2;
-    double *sl64 = reinterpret_cast<double *>(slhi);
+    // per (beta single, row): orbital pair tt = br * L + bc | parity << 31; per alpha
+    // single: parity << 31 | (Ja < Ia) << 30 -- what an S4 element needs besides
+    // its integral, read from shared memory instead of one dependent global load each
+    uint32_t *sbi = st + p.b.ns * kTileRows;
+    uint32_t *sai = sbi + p.b.ns * kTileRows;
+    // alpha-single integral slices, nsa * L2 entries: FP32 (hi, lo) pairs (F64 = false,
+    // one 8-byte shared load per element) or FP64 (true)
+    float2 *slhl = reinterpret_cast<float2 *>(sai + pad4(nsa));  // 16-byte aligned: every region is a multiple of 16 bytes
+    double *sl64 = reinterpret_cast<double *>(slhl);
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
     const int64_t ia = blockIdx.x / T, t = blockIdx.x - ia * T;
     stage_tile(p, m, ia, t, desc, st);
+    for (int i = threadIdx.x; i < p.b.ns * kTileRows; i += blockDim.x) {
+        const int xb = i / kTileRows, r = i - xb * kTileRows;
+        const int64_t ibr = t * kTileRows + r;
+        uint32_t w = 0;
+        if (ibr < p.Db) {
+            const uint32_t info = __ldg(p.b.s_info + ibr * p.b.ns + xb);
+            w = (((info >> 12) & 63) * p.L + ((info >> 18) & 63)) | (((info >> 24) & 1u) << 31);
+        }
+        sbi[i] = w;
+    }
+    for (int xa = threadIdx.x; xa < nsa; xa += blockDim.x) {
+        const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
+        const uint32_t Ja = __ldg(p.a.s_target + ia * nsa + xa);
+        sai[xa] = (((info >> 24) & 1u) << 31) | ((uint32_t)(Ja < (uint32_t)ia) << 30);
+    }
     if (p.staged) {
         for (int i = threadIdx.x; i < nsa * L2; i += blockDim.x) {
             const int xa = i / L2, tt = i - xa * L2;
@@ -292,8 +316,7 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
             if constexpr (F64) {
                 sl64[i] = __ldg(p.eri + at);
             } else {
-                slhi[i] = __ldg(p.eri_hi + at);
-                sllo[i] = __ldg(p.eri_lo + at);
+                slhl[i] = make_float2(__ldg(p.eri_hi + at), __ldg(p.eri_lo + at));
             }
         }
     }
@@ -360,18 +383,19 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
         } else {  // S4: alpha-beta doubles (ar ac|br bc), sign from both phases (CIMethod.cpp:444-457)
             const int i0 = k0 - m.s4;
             int xa = nsb > 0 ? i0 / nsb : 0, xb = i0 - xa * nsb;
-            uint32_t infoA = xa < nsa ? __ldg(p.a.s_info + ia * nsa + xa) : 0u;
+            uint32_t a = xa < nsa ? sai[xa] : 0u;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (i0 + j < nsa * nsb) {
-                    const uint32_t infoB = __ldg(p.b.s_info + ib * nsb + xb);
-                    const int tt = ((infoB >> 12) & 63) * L + ((infoB >> 18) & 63);
-                    const uint32_t odd = ((infoA ^ infoB) >> 24) & 1;
+                    const uint32_t w = sbi[xb * kTileRows + rr];
+                    const int tt = (int)(w & 0xFFFu);
+                    const uint32_t odd = (a ^ w) >> 31;
                     if constexpr (F64) {
                         double e;
                         if (p.staged) {
                             e = sl64[xa * L2 + tt];
                         } else {
+                            const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
                             const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
                             e = __ldg(p.eri + ((size_t)ar * L + ac) * L2 + tt);
                         }
@@ -379,9 +403,11 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                     } else {
                         float h, l;
                         if (p.staged) {
-                            h = slhi[xa * L2 + tt];
-                            l = sllo[xa * L2 + tt];
+                            const float2 hl = slhl[xa * L2 + tt];
+                            h = hl.x;
+                            l = hl.y;
                         } else {
+                            const uint32_t infoA = __ldg(p.a.s_info + ia * nsa + xa);
                             const int ar = (infoA >> 12) & 63, ac = (infoA >> 18) & 63;
                             const size_t at = ((size_t)ar * L + ac) * L2 + tt;
                             h = __ldg(p.eri_hi + at);
@@ -390,11 +416,11 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
                         q.h[j] = __uint_as_float(__float_as_uint(h) ^ (odd << 31));
                         q.l[j] = __uint_as_float(__float_as_uint(l) ^ (odd << 31));
                     }
-                    lw[j] = (uint32_t)desc[k0 + j] < (uint32_t)ia;
+                    lw[j] = (a >> 30) & 1u;  // Ja < Ia: the column lies below the diagonal
                     if (++xb == nsb && j < 3) {
                         xb = 0;
                         ++xa;
-                        infoA = xa < nsa ? __ldg(p.a.s_info + ia * nsa + xa) : 0u;
+                        a = xa < nsa ? sai[xa] : 0u;
                     }
                 }
             }
@@ -409,8 +435,8 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
         const int64_t at = ((qbase + c) * kTileRows + rr) * 4;
         if constexpr (F64) {
             double2 *d = reinterpret_cast<double2 *>(v64 + at);
-            d[0] = make_double2(q.v[0], q.v[1]);
-            d[1] = make_double2(q.v[2], q.v[3]);
+            d[0] = make_double2(q.v(0), q.v(1));
+            d[1] = make_double2(q.v(2), q.v(3));
         } else {
             *reinterpret_cast<float4 *>(hi + at) = make_float4(q.h[0], q.h[1], q.h[2], q.h[3]);
             *reinterpret_cast<float4 *>(lo + at) = make_float4(q.l[0], q.l[1], q.l[2], q.l[3]);
@@ -432,6 +458,10 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
 }
 
 size_t tile_smem(const FciParams &p) { return (size_t)slot_map(p).wp * 8 + (size_t)p.b.ns * kTileRows * 4; }
+// the fill's staging: the tile tables, the beta singles' pairs / parities, the alpha flags
+size_t fill_smem(const FciParams &p) {
+    return tile_smem(p) + (size_t)p.b.ns * kTileRows * 4 + (size_t)pad4(p.a.ns) * 4;
+}
 size_t slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
 
 template <typename F>
@@ -453,7 +483,7 @@ void launch_slots(const FciParams &p, const F &f0, typename F::X *y, cudaStream_
 }  // namespace
 
 bool slots_supported(const FciParams &p) {
-    return tile_smem(p) <= kSlotsMaxSmem && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
+    return fill_smem(p) <= kSlotsMaxSmem && (int64_t)p.L * p.L <= 4096 && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
            (int64_t)p.a.ns * p.b.ns < (int64_t)INT32_MAX / 8;
 }
 
@@ -463,7 +493,7 @@ int64_t slots_count(const FciParams &p) {
 
 void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s) {
     FciParams p = p0;
-    const size_t base = tile_smem(p), sl = slice_smem(p);
+    const size_t base = fill_smem(p), sl = slice_smem(p);
     p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fill_slots<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
@@ -479,7 +509,7 @@ void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *coun
 
 void fill_slots64_launch(const FciParams &p0, double *v64, uint32_t *count, uint32_t *lower, cudaStream_t s) {
     FciParams p = p0;
-    const size_t base = tile_smem(p), sl = slice_smem(p);  // an FP64 slice takes the bytes of hi + lo
+    const size_t base = fill_smem(p), sl = slice_smem(p);  // an FP64 slice takes the bytes of hi + lo
     p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fill_slots<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
