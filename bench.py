@@ -541,6 +541,17 @@ def run_cigpu(args, rank: int, world: int, dist):
                      "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{cfg['method'].lower()}_L{cfg['L']}_{cfg['nup']}a{cfg['ndown']}b"),
                      "algorithmic_bytes": bytes_alg, "layout": layout, "ms_per_launch": t * 1000,
                      "nnz_full": nf.value, "peak_source": peaks["source"]}
+        if tag == "fp64":
+            # the plain FP64 matvec issues one DFMA per stored slot (padding included);
+            # GB300 retires 2 FP64 FMAs per clock per SM, so this is its bound
+            lay, stored = ctypes.c_int(), ctypes.c_int64()
+            lib.cigpu_crs_layout(crs, ctypes.byref(lay), ctypes.byref(stored))
+            fmas = stored.value if stored.value > 0 else nf.value
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            peak_fma = 2.0 * sms * 2070e6  # at the maximum SM clock (2070 MHz on GB300)
+            roof[tag]["fp64_pipe"] = {"dfma_per_launch": fmas, "achieved_dfma_per_s": fmas / t,
+                                      "peak_dfma_per_s": peak_fma, "frac": fmas / t / peak_fma,
+                                      "note": "2 FP64 FMA per clock per SM x SMs x 2070 MHz"}
         lib.cigpu_crs_destroy(crs)
 
     # e2e through the C ABI with host buffers, H2D of the integrals and D2H of c inside the region

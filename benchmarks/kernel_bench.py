@@ -3,9 +3,11 @@ named configuration (used for profiler captures and roofline timing).
 
     python -m benchmarks.kernel_bench --config c4 --kernel spmv_f32 --reps 3
 
-Kernels: spmv_f32, spmv_f64 (CRS matvec), build_f64, build_f32 (CRS build:
-count + fill passes), matvec_hilo (FP64 product from the FP32 hi + lo values of a mixed CRS),
-solve_mixed / solve_fp64 (one eigensolve on a prebuilt CRS).
+Kernels: spmv_f32 (the mixed form's FP32 matvec), spmv_f64 (the plain form's FP64
+matvec), build_f64, build_f32 (the matrix build of either form), matvec_hilo (the
+mixed form's FP64 product), solve_mixed / solve_fp64 (one eigensolve on a prebuilt
+matrix), rdm (cigpu_rdm of a random normalised vector: 1- and 2-RDM, DOCI spaces
+beyond 32 orbitals the 1-RDM).
 Prints one JSON line with the CUDA-event time per launch and the algorithmic
 bytes of the matvec.
 """
@@ -23,7 +25,7 @@ def main() -> None:
     ap.add_argument("--config", default="c4")
     ap.add_argument("--kernel", default="spmv_f32",
                     choices=["spmv_f32", "spmv_f64", "build_f64", "build_f32", "matvec_hilo", "solve_mixed",
-                             "solve_fp64"])
+                             "solve_fp64", "rdm"])
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=1)
@@ -44,7 +46,7 @@ def main() -> None:
     A.check(lib.cigpu_ham_create(ints.L, ints.nup, ints.ndown, ints.econst, A.ptr(h), A.ptr(eri), ctypes.byref(ham)))
     stream = torch.cuda.Stream()
     sh = ctypes.c_void_p(stream.cuda_stream)
-    prec = A.MIXED if args.kernel in ("spmv_f32", "build_f32", "matvec_hilo", "solve_mixed") else A.FP64
+    prec = A.MIXED if args.kernel in ("spmv_f32", "build_f32", "matvec_hilo", "solve_mixed", "rdm") else A.FP64
 
     def build():
         crs = ctypes.c_void_p()
@@ -66,6 +68,28 @@ def main() -> None:
         torch.cuda.synchronize()
         out["ms_per_solve"] = e0.elapsed_time(e1) / args.reps
         out["info"] = info.as_dict()
+        lib.cigpu_crs_destroy(crs)
+    elif args.kernel == "rdm":
+        crs = build()
+        dim = ctypes.c_int64()
+        lib.cigpu_crs_dims(crs, ctypes.byref(dim), None, None)
+        c = np.random.default_rng(0).standard_normal(dim.value)
+        c /= np.linalg.norm(c)
+        L = ints.L
+        np_ = L * (L - 1) // 2
+        r1, aa = np.empty((2, L, L)), np.empty((np_, np_))
+        ab, bb = np.empty((L * L, L * L)), np.empty((np_, np_))
+        outs = (A.ptr(r1), A.ptr(aa), A.ptr(ab), A.ptr(bb)) if L <= 32 else (A.ptr(r1), None, None, None)
+        for _ in range(args.warmup):
+            A.check(lib.cigpu_rdm(crs, A.ptr(c), *outs))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.reps):
+            A.check(lib.cigpu_rdm(crs, A.ptr(c), *outs))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["ms_per_rdm"] = e0.elapsed_time(e1) / args.reps
+        out["trace"] = float(r1[0].trace() + r1[1].trace())
         lib.cigpu_crs_destroy(crs)
     elif args.kernel.startswith("build"):
         for _ in range(args.warmup):
