@@ -239,6 +239,18 @@ int status_from_exception() {
 
 static int64_t binom64(int n, int k) { return d_binom(n, k); }
 
+// The mixed FCI method's FP32 product, read at every build from CIGPU_FP32_PRODUCT:
+// "slots" takes the stored FP32 slot values, "sigma" the factorised sigma operator
+// on any space it supports, anything else the sigma operator where its tile grid
+// fills the GPU. Both are complete products; the choice exists to compare them.
+enum SigmaMode { kSigmaOff = 0, kSigmaAuto = 1, kSigmaForced = 2 };
+int sigma_mode() {
+    const char *e = std::getenv("CIGPU_FP32_PRODUCT");
+    if (e && std::strcmp(e, "slots") == 0) return kSigmaOff;
+    if (e && std::strcmp(e, "sigma") == 0) return kSigmaForced;
+    return kSigmaAuto;
+}
+
 size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     int64_t dim, W;
     dim = std::max<int64_t>(space_dim(method, L, nup, ndown), 0);
@@ -251,8 +263,12 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     const size_t vbytes = precision == CIGPU_MIXED ? 4 : 8;
     // col + values (FP64, or FP32 hi + lo); the mixed FCI layout stores values only
     size_t b = (size_t)dim * W * 12;
-    if (method == CIGPU_FCI && precision == CIGPU_MIXED)  // slot tiles of kTileRows beta strings, hi + lo
+    if (method == CIGPU_FCI && precision == CIGPU_MIXED) {  // slot tiles of kTileRows beta strings, hi + lo
         b = (size_t)binom64(L, nup) * ((binom64(L, ndown) + kTileRows - 1) / kTileRows * kTileRows) * (W + 16) * 8;
+        if (sigma_applies(L))  // the FP32 sigma operator at its largest rank
+            b += sigma_bytes(L, binom64(L, nup), binom64(L, ndown),
+                             std::min(kSigmaMaxRank, (L * (L + 1) / 2 + kSigmaChunk - 1) / kSigmaChunk * kSigmaChunk));
+    }
     if (method == CIGPU_DOCI)  // matrix-free: strings and the FP32 diagonal
         b = (size_t)dim * (8 + 4);
     b += (size_t)dim * (8 + 8 + 4 + 4);          // row_ptr, diag, counts, upper offsets
@@ -400,6 +416,14 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
             p.desc_tab = c.slot_desc.p;
             p.st_tab = c.slot_st.p;
             tr.mark("slot fill");
+            const int smode = sigma_mode();
+            if (c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
+                c.sig.reset(new SigmaOp);
+                if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
+                                   smode == kSigmaForced, s))
+                    c.sig.reset();
+                tr.mark("sigma factors");
+            }
         } else {
             fci_launch(kCount, p, s);
             tr.mark("count pass");
@@ -542,6 +566,10 @@ void crs_mv32(cigpu_crs &c, const float *x, float *y, cudaStream_t s) {
     if (c.precision != CIGPU_MIXED || c.onthefly) throw std::invalid_argument("FP32 matvec needs a MIXED CRS");
     if (c.pairs) {
         doci_mv32(DociMv{c.L, c.nup, c.dim, c.strings.p}, c.kpair32.p, c.diag32.p, x, y, s);
+        return;
+    }
+    if (c.sig) {
+        sigma_mv32(*c.sig, c.fp, x, y, s);
         return;
     }
     if (c.slots) {

@@ -6,6 +6,7 @@
 #include "build.cuh"
 #include "doci_mv.cuh"
 #include "lanczos.cuh"
+#include "sigma.cuh"
 #include "slots.cuh"
 
 namespace cigpu {
@@ -47,6 +48,9 @@ struct cigpu_crs {
     cigpu::DevBuf<uint64_t> slot_desc;  // the slot matvecs' staging tables (slot_tables_launch)
     cigpu::DevBuf<uint32_t> slot_st;
     cigpu::DevBuf<float> x32;  // MIXED: FP32 copy of x for the FP64 product from hi + lo
+    // MIXED FCI: the FP32 product as a factorised direct-CI sigma vector (sigma.cu);
+    // null when the space or the rank does not qualify (the FP32 slot values serve)
+    std::unique_ptr<cigpu::SigmaOp> sig;
     cigpu::FciParams fp{};
     cigpu::DociParams dp{};
     // determinant lists (FCI_File / CI_Big)

@@ -101,12 +101,25 @@ __device__ __forceinline__ void stage_tile(const FciParams &p, const SlotMap &m,
 
 // The matvec's staging from the precomputed tables (the tile's slot descriptors
 // and beta single targets) with 16-byte loads: a few independent loads per thread
-// where computing them took ~10 dependent table reads.
+// where computing them took ~10 dependent table reads. The descriptors are staged
+// in the matvec's own form: the low word is the x panel's start Ja * Db (the
+// matrix dimension fits 32 bits), the high word the beta kind plus, shifted by 2,
+// the offset of the beta target: xb * kTileRows into the staged single targets, or
+// xb into the row's double targets. A column is then one 32-bit add.
+__device__ __forceinline__ uint2 mv_desc(uint32_t lo, uint32_t hi, uint32_t Db) {
+    const uint32_t kind = hi & 3u, xb = hi >> 2;
+    return make_uint2(lo * Db, kind | ((kind == kSingle ? xb * kTileRows : xb) << 2));
+}
 __device__ __forceinline__ void stage_tile_tab(const FciParams &p, const SlotMap &m, int64_t ia, int64_t t,
                                                uint64_t *desc, uint32_t *st) {
     const uint4 *ds = reinterpret_cast<const uint4 *>(p.desc_tab + ia * m.wp);
     uint4 *dd = reinterpret_cast<uint4 *>(desc);
-    for (int i = threadIdx.x; i < m.wp / 2; i += blockDim.x) dd[i] = __ldg(ds + i);
+    const uint32_t Db = (uint32_t)p.Db;
+    for (int i = threadIdx.x; i < m.wp / 2; i += blockDim.x) {
+        const uint4 d = __ldg(ds + i);
+        const uint2 a = mv_desc(d.x, d.y, Db), b = mv_desc(d.z, d.w, Db);
+        dd[i] = make_uint4(a.x, a.y, b.x, b.y);
+    }
     const int n4 = p.b.ns * kTileRows / 4;
     const uint4 *ss = reinterpret_cast<const uint4 *>(p.st_tab + t * p.b.ns * kTileRows);
     uint4 *sd = reinterpret_cast<uint4 *>(st);
@@ -192,7 +205,9 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
     const int64_t ib_raw = t * kTileRows + rr;
     const bool active = ib_raw < p.Db;
     const int64_t ib = active ? ib_raw : p.Db - 1;
+    const uint32_t ib32 = (uint32_t)ib;
     const uint32_t *dt = p.b.d_target + ib * p.b.nd;
+    const uint32_t *stl = st + rr;  // this row's beta single targets, kTileRows apart
     constexpr int kQuadsInFlight = SlotInFlight<F>::kQuads;
     typename F::Acc acc{};
     typename F::Chunk v[kQuadsInFlight];
@@ -208,22 +223,31 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
 #pragma unroll
         for (int u = 0; u < kQuadsInFlight; ++u) {
             if (c + u < c1) {
-                const uint64_t *d = desc + 4 * (c + u);
-                const uint32_t kind = (uint32_t)(d[0] >> 32) & 3u;
-                int64_t col[4];
+                // the quad's four staged descriptors: (panel start, kind | target offset << 2)
+                const uint4 *dq = reinterpret_cast<const uint4 *>(desc + 4 * (c + u));
+                const uint32_t kind = reinterpret_cast<const uint32_t *>(dq)[1] & 3u;  // one kind per quad
+                uint32_t col[4];
                 if (kind == kSelf) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) col[j] = (int64_t)(uint32_t)d[j] * p.Db + ib;
+                    const uint4 q0 = dq[0], q1 = dq[1];
+                    col[0] = q0.x + ib32;
+                    col[1] = q0.z + ib32;
+                    col[2] = q1.x + ib32;
+                    col[3] = q1.z + ib32;
                 } else if (kind == kSingle) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        col[j] = (int64_t)(uint32_t)d[j] * p.Db + st[(uint32_t)(d[j] >> 34) * kTileRows + rr];
+                    const uint4 q0 = dq[0], q1 = dq[1];
+                    col[0] = q0.x + stl[q0.y >> 2];
+                    col[1] = q0.z + stl[q0.w >> 2];
+                    col[2] = q1.x + stl[q1.y >> 2];
+                    col[3] = q1.z + stl[q1.w >> 2];
                 } else {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) col[j] = (int64_t)(uint32_t)d[j] * p.Db + __ldg(dt + (uint32_t)(d[j] >> 34));
+                    const uint4 q0 = dq[0], q1 = dq[1];
+                    col[0] = q0.x + __ldg(dt + (q0.y >> 2));
+                    col[1] = q0.z + __ldg(dt + (q0.w >> 2));
+                    col[2] = q1.x + __ldg(dt + (q1.y >> 2));
+                    col[3] = q1.z + __ldg(dt + (q1.w >> 2));
                 }
 #pragma unroll
-                for (int j = 0; j < 4; ++j) f.term(v[u], j, col[j], acc);
+                for (int j = 0; j < 4; ++j) f.term(v[u], j, (int64_t)col[j], acc);
             }
         }
     }
@@ -483,7 +507,7 @@ void launch_slots(const FciParams &p, const F &f0, typename F::X *y, cudaStream_
 }  // namespace
 
 bool slots_supported(const FciParams &p) {
-    return fill_smem(p) <= kSlotsMaxSmem && (int64_t)p.L * p.L <= 4096 && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
+    return p.a.D * p.Db < (int64_t)UINT32_MAX && fill_smem(p) <= kSlotsMaxSmem && (int64_t)p.L * p.L <= 4096 && p.a.D * ((p.Db + kTileRows - 1) / kTileRows) < (int64_t)INT32_MAX &&
            (int64_t)p.a.ns * p.b.ns < (int64_t)INT32_MAX / 8;
 }
 

@@ -78,9 +78,16 @@ def test_doci_pair_matvec_fp32():
     assert np.abs(y - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
 
 
-def test_fp32_device_matvec():
+@pytest.mark.parametrize("case", ["c0", "c4", "9x3x5", "11x5x4"])
+def test_fp32_device_matvec(case):
+    """The FP32 slot matvec against the reference mvprod: equal and unequal spin
+    counts, last tiles with padding rows."""
     torch = pytest.importorskip("torch")
-    ints = integrals("c0")
+    if "x" in case:
+        L, na, nb = (int(v) for v in case.split("x"))
+        ints = make_integrals(L, na, nb, nchol=8, seed=L + 7 * na + 11 * nb)
+    else:
+        ints = integrals(case)
     ref = O.build_upper(O.FCI, ints)
     m = build(FCI, ints, A.MIXED).get_mat()
     x = np.random.default_rng(3).standard_normal(m.n)
@@ -92,6 +99,59 @@ def test_fp32_device_matvec():
     y = yd.cpu().numpy().astype(np.float64)
     # FP32 values and FP32 accumulation over ~361 terms per row
     assert np.abs(y - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
+
+
+def _ints_case(case):
+    """'LxNaxNb[xK]' with K factors (8 by default); a trailing '-indefinite' subtracts
+    a rank-one pair term, so the two-electron part is no longer positive semidefinite."""
+    indefinite = case.endswith("-indefinite")
+    parts = [int(v) for v in case.replace("-indefinite", "").split("x")]
+    L, na, nb = parts[:3]
+    k = parts[3] if len(parts) > 3 else 8
+    ints = make_integrals(L, na, nb, nchol=k, seed=L + 7 * na + 11 * nb + k)
+    if indefinite:
+        m = np.random.default_rng(L).normal(0.0, 0.2, (L, L))
+        v = (m + m.T).reshape(-1)
+        ints.eri = (ints.eri.reshape(L * L, L * L) - np.multiply.outer(v, v)).reshape(L, L, L, L)
+    return ints
+
+
+@pytest.mark.parametrize("case", ["8x4x4", "9x3x5", "10x5x3x24", "7x3x3-indefinite", "11x5x4", "6x1x5"])
+def test_sigma_fp32_matvec(case, monkeypatch):
+    """The mixed method's factorised FP32 product (a direct-CI sigma vector, two
+    one-body passes over every determinant's single excitations), forced onto small
+    spaces: equal and unequal spin counts, ragged 32 x 32 string tiles, a rank above
+    one 16-factor chunk, and integrals whose pair matrix is indefinite (eigenpair
+    factors with signs) against the reference mvprod."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("CIGPU_FP32_PRODUCT", "sigma")
+    ints = _ints_case(case)
+    ref = O.build_upper(O.FCI, ints)
+    m = build(FCI, ints, A.MIXED).get_mat()
+    x = np.random.default_rng(5).standard_normal(m.n)
+    y_ref = O.sym_mvprod(ref, x)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    torch.cuda.synchronize()
+    n0 = A.lib().cigpu_kernel_launches()
+    m.mvprod_device(xd, yd)
+    torch.cuda.synchronize()
+    assert A.lib().cigpu_kernel_launches() - n0 == 3  # transpose + the two passes: the sigma operator ran
+    y = yd.cpu().numpy().astype(np.float64)
+    assert np.abs(y - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
+
+
+@pytest.mark.parametrize("case", ["9x3x5", "7x3x3-indefinite"])
+def test_sigma_mixed_solve(case, monkeypatch):
+    """A mixed solve whose FP32 corrections come from the factorised operator
+    reaches the FP64 ground state of the stored matrix (the anchors' residual is
+    exact)."""
+    monkeypatch.setenv("CIGPU_FP32_PRODUCT", "sigma")
+    ints = _ints_case(case)
+    e_ref = np.linalg.eigvalsh(O.build_upper(O.FCI, ints).full_csr().toarray())[0] + ints.econst
+    f = build(FCI, ints, A.MIXED)
+    f.solve(tol=1e-8)
+    assert abs(f.get_ci_energy() - e_ref) < 1e-9
 
 
 def test_doci_known_answer():
