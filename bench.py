@@ -512,18 +512,30 @@ def run_cigpu(args, rank: int, world: int, dist):
     mixed = summary(ms_mixed, tot_mixed, inf_mixed)
     plain = summary(ms_plain, tot_plain, inf_plain)
 
-    # dominant kernel: the CRS matvec, timed alone with CUDA events on its stream
+    # dominant kernels, timed alone with CUDA events on their stream: the mixed
+    # method's FP32 product (the factorised sigma vector where it applies), the same
+    # product from the stored FP32 slot values, and the plain FP64 matvec
     roof = {}
     peaks = measured_peaks()
-    for prec, tag in ((A.MIXED, "fp32"), (A.FP64, "fp64")):
+    for prec, tag in ((A.MIXED, "fp32"), (A.MIXED, "fp32_slots"), (A.FP64, "fp64")):
+        if tag == "fp32_slots":
+            os.environ["CIGPU_FP32_PRODUCT"] = "slots"  # read by the build
         crs = ctypes.c_void_p()
-        A.check(lib.cigpu_build(ham, method, prec, sh, ctypes.byref(crs)))
+        try:
+            A.check(lib.cigpu_build(ham, method, prec, sh, ctypes.byref(crs)))
+        finally:
+            os.environ.pop("CIGPU_FP32_PRODUCT", None)
+        kind = A.fp32_product(crs) if prec == A.MIXED else (A.FP32_STORED, 0, 0)
+        if tag == "fp32_slots" and roof.get("fp32", {}).get("bound") == "hbm":
+            lib.cigpu_crs_destroy(crs)  # the default product is the stored one already
+            continue
         dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         lib.cigpu_crs_dims(crs, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf))
-        dt = torch.float32 if tag == "fp32" else torch.float64
+        f32 = tag.startswith("fp32")
+        dt = torch.float32 if f32 else torch.float64
         x = torch.randn(dim.value, device="cuda", dtype=dt)
         y = torch.empty_like(x)
-        dtype_code = 1 if tag == "fp32" else 0
+        dtype_code = 1 if f32 else 0
         for _ in range(3):
             lib.cigpu_mvprod_device(crs, A.ptr(x), A.ptr(y), dtype_code, sh)
         reps = 20
@@ -535,12 +547,31 @@ def run_cigpu(args, rank: int, world: int, dist):
         e1.record(stream)
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / 1000.0 / reps
-        bytes_alg, layout = A.matvec_bytes(crs, tag == "fp32")
-        ach = bytes_alg / t / 1e9
-        roof[tag] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / peaks["hbm_gbs"], "traffic": ncu_traffic(f"spmv_{tag}_{cfg['method'].lower()}_L{cfg['L']}_{cfg['nup']}a{cfg['ndown']}b"),
-                     "algorithmic_bytes": bytes_alg, "layout": layout, "ms_per_launch": t * 1000,
-                     "nnz_full": nf.value, "peak_source": peaks["source"]}
+        shape = f"{cfg['method'].lower()}_L{cfg['L']}_{cfg['nup']}a{cfg['ndown']}b"
+        if kind[0] == A.FP32_SIGMA:
+            # the factorised sigma vector reads the matrix from no DRAM stream: its work
+            # is FP32 FMAs over every determinant's single excitations times the rank,
+            # on vectors that stay in L2; its roofline is the FP32 FMA rate
+            w = A.sigma_work(cfg["L"], cfg["nup"], cfg["ndown"], kind[1], kind[2])
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            peak_tf = sms * 128 * 2 * 2070e6 / 1e12
+            ach = w["flops"] / t / 1e12
+            roof[tag] = {"bound": "fp32", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s", "frac": ach / peak_tf,
+                         "traffic": ncu_traffic(f"sigma_fp32_{shape}"), "algorithmic_flops": w["flops"],
+                         "l2_bytes_per_launch": w["l2_bytes"], "l2_gbs": w["l2_bytes"] / t / 1e9,
+                         "layout": f"sigma-fp32 (rank {kind[1]}, padded {kind[2]})",
+                         "kernels": "k_transpose32 + k_sigma_a + k_sigma_b", "ms_per_launch": t * 1000,
+                         "nnz_full": nf.value,
+                         "peak_source": "nominal FP32 FMA rate: SMs x 128 lanes x 2 flops x 2070 MHz "
+                                        "(no measured FP32 figure)"}
+        else:
+            bytes_alg, layout = A.matvec_bytes(crs, f32)
+            ach = bytes_alg / t / 1e9
+            roof[tag] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / peaks["hbm_gbs"],
+                         "traffic": ncu_traffic(f"spmv_{'fp32' if f32 else 'fp64'}_{shape}"),
+                         "algorithmic_bytes": bytes_alg, "layout": layout, "ms_per_launch": t * 1000,
+                         "nnz_full": nf.value, "peak_source": peaks["source"]}
         if tag == "fp64":
             # the plain FP64 matvec issues one DFMA per stored slot (padding included);
             # GB300 retires 2 FP64 FMAs per clock per SM, so this is its bound
@@ -673,7 +704,7 @@ def run_cigpu(args, rank: int, world: int, dist):
         "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"],
         "mixed": mixed, "plain_fp64": plain,
         "mixed_over_plain": mixed["solves_per_s"] / plain["solves_per_s"],
-        "roofline": roof["fp32"], "roofline_fp64": roof["fp64"],
+        "roofline": roof["fp32"], "roofline_fp32_slots": roof.get("fp32_slots"), "roofline_fp64": roof["fp64"],
         "e2e": e2e, "gpu_launches": launches_mixed,
         "gpu_launches_plain": launches_plain,
         "clocks": clk.summary(),

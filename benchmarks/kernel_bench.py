@@ -3,7 +3,8 @@ named configuration (used for profiler captures and roofline timing).
 
     python -m benchmarks.kernel_bench --config c4 --kernel spmv_f32 --reps 3
 
-Kernels: spmv_f32 (the mixed form's FP32 matvec), spmv_f64 (the plain form's FP64
+Kernels: spmv_f32 (the mixed form's FP32 matvec: the factorised sigma vector for
+FCI where it applies, CIGPU_FP32_PRODUCT=slots for the stored FP32 values), spmv_f64 (the plain form's FP64
 matvec), build_f64, build_f32 (the matrix build of either form), matvec_hilo (the
 mixed form's FP64 product), solve_mixed / solve_fp64 (one eigensolve on a prebuilt
 matrix), rdm (cigpu_rdm of a random normalised vector: 1- and 2-RDM, DOCI spaces
@@ -120,9 +121,16 @@ def main() -> None:
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / args.reps
         n = dim.value
-        alg, layout = A.matvec_bytes(crs, f32)
-        out.update({"dim": n, "nnz_full": nf.value, "layout": layout, "ms_per_launch": t, "algorithmic_bytes": alg,
-                    "achieved_gbs": alg / (t / 1000) / 1e9})
+        kind, rank, padded = A.fp32_product(crs) if prec == A.MIXED else (A.FP32_STORED, 0, 0)
+        if f32 and kind == A.FP32_SIGMA:  # the factorised sigma vector: FMAs, not a matrix stream
+            w = A.sigma_work(ints.L, ints.nup, ints.ndown, rank, padded)
+            out.update({"dim": n, "nnz_full": nf.value, "layout": f"sigma-fp32 (rank {rank}, padded {padded})",
+                        "ms_per_launch": t, "algorithmic_flops": w["flops"],
+                        "achieved_tflops": w["flops"] / (t / 1000) / 1e12, "l2_bytes": w["l2_bytes"]})
+        else:
+            alg, layout = A.matvec_bytes(crs, f32)
+            out.update({"dim": n, "nnz_full": nf.value, "layout": layout, "ms_per_launch": t, "algorithmic_bytes": alg,
+                        "achieved_gbs": alg / (t / 1000) / 1e9})
         lib.cigpu_crs_destroy(crs)
     lib.cigpu_ham_destroy(ham)
     print(json.dumps(out))

@@ -19,6 +19,7 @@ FCI, DOCI, DETS = 0, 1, 2
 DETS_CRS, DETS_ONTHEFLY = 0, 1
 FP64, MIXED = 0, 1
 LAYOUT_CRS, LAYOUT_SLOTS, LAYOUT_ONTHEFLY, LAYOUT_PAIRS = 0, 1, 2, 3
+FP32_STORED, FP32_SIGMA = 0, 1
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -99,6 +100,7 @@ SIGNATURES = {
     "cigpu_crs_destroy": (_I, [_P]),
     "cigpu_crs_dims": (_I, [_P, _P, _P, _P]),
     "cigpu_crs_layout": (_I, [_P, _P, _P]),
+    "cigpu_crs_fp32_product": (_I, [_P, _P, _P, _P]),
     "cigpu_crs_export_upper": (_I, [_P, _P, _P, _P]),
     "cigpu_crs_export_full": (_I, [_P, _P, _P, _P]),
     "cigpu_mvprod": (_I, [_P, _P, _P, _P]),
@@ -198,6 +200,29 @@ def estimate_bytes(L: int, nup: int, ndown: int, method: int, precision: int) ->
     b = ctypes.c_size_t()
     check(lib().cigpu_estimate_bytes(L, nup, ndown, method, precision, ctypes.byref(b)), "cigpu_estimate_bytes")
     return b.value
+
+
+def fp32_product(handle) -> tuple[int, int, int]:
+    """(kind, rank, padded rank) of a MIXED matrix's FP32 product (FP32_STORED or
+    FP32_SIGMA, the factorised direct-CI sigma vector)."""
+    kind, rank, padded = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(lib().cigpu_crs_fp32_product(handle, ctypes.byref(kind), ctypes.byref(rank), ctypes.byref(padded)))
+    return kind.value, rank.value, padded.value
+
+
+def sigma_work(L: int, nup: int, ndown: int, rank: int, padded: int) -> dict:
+    """Algorithmic work of one FP32 sigma product on the FCI space (nup, ndown) of L
+    orbitals with `rank` factors: FP32 FMAs per determinant (pass 1: (R + 1) per
+    single excitation and on the diagonal, the one-body matrix included; pass 2: R
+    per excitation and on the diagonal) and the bytes the passes move through L2
+    (x read per excitation, the padded factor vectors written twice and read per
+    excitation, y written)."""
+    from math import comb
+    ns = nup * (L - nup) + ndown * (L - ndown)
+    dim = comb(L, nup) * comb(L, ndown)
+    fma = dim * (ns * (rank + 1) + rank + 1 + rank + ns * rank)
+    l2 = dim * 4 * ((1 + ns) + 2 * padded + (1 + ns) * padded + 2)
+    return {"fma": fma, "flops": 2 * fma, "l2_bytes": l2, "dim": dim, "excitations_per_det": ns}
 
 
 def matvec_bytes(handle, fp32: bool) -> tuple[int, str]:

@@ -401,8 +401,19 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         if (c.slots) {
-            // values-only layout: the fill counts the rows itself
-            if (c.precision == CIGPU_MIXED) {
+            // MIXED: the FP32 products as the factorised sigma vector where it applies
+            const int smode = sigma_mode();
+            if (c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
+                c.sig.reset(new SigmaOp);
+                if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
+                                   smode == kSigmaForced, s))
+                    c.sig.reset();
+                tr.mark("sigma factors");
+            }
+            // values-only layout: the fill counts the rows itself; MIXED stores FP32
+            // hi + lo for its FP32 and FP64 products, or, with the sigma vector doing
+            // the FP32 ones, the FP64 values (its anchors take the plain FP64 product)
+            if (c.precision == CIGPU_MIXED && !c.sig) {
                 c.val32.alloc(slots_count(p));
                 c.val32lo.alloc(slots_count(p));
                 fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
@@ -416,14 +427,6 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
             p.desc_tab = c.slot_desc.p;
             p.st_tab = c.slot_st.p;
             tr.mark("slot fill");
-            const int smode = sigma_mode();
-            if (c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
-                c.sig.reset(new SigmaOp);
-                if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
-                                   smode == kSigmaForced, s))
-                    c.sig.reset();
-                tr.mark("sigma factors");
-            }
         } else {
             fci_launch(kCount, p, s);
             tr.mark("count pass");
@@ -538,15 +541,16 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         doci_mv64(DociMv{c.L, c.nup, c.dim, c.strings.p}, c.kpair64.p, c.diag.p, x, y, s);
         return;
     }
+    if (c.slots && c.val64.p) {  // FP64 slot values: the plain method, or MIXED with the sigma vector
+        spmv_slots_f64(c.fp, c.val64.p, x, y, s);
+        return;
+    }
     if (c.precision == CIGPU_MIXED) {
         if (!c.x32.p) c.x32.alloc(std::max<int64_t>(c.dim, 1));
         dev_convert(x, c.x32.p, c.dim, s);
     }
     if (c.slots) {
-        if (c.precision == CIGPU_FP64)
-            spmv_slots_f64(c.fp, c.val64.p, x, y, s);
-        else
-            spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
+        spmv_slots_hilo(c.fp, c.val32.p, c.val32lo.p, x, c.x32.p, y, s);
         return;
     }
     if (c.precision == CIGPU_FP64) {
@@ -828,6 +832,15 @@ int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
                   : crs->slots  ? CIGPU_LAYOUT_SLOTS
                                 : CIGPU_LAYOUT_CRS;
     if (stored) *stored = (crs->onthefly || crs->pairs) ? 0 : crs->slots ? slots_count(crs->fp) : crs->nnz_full;
+    return CIGPU_OK;
+}
+
+int cigpu_crs_fp32_product(const cigpu_crs *crs, int *kind, int *rank, int *padded) {
+    if (!crs) return CIGPU_EINVAL;
+    const bool sig = crs->sig != nullptr;
+    if (kind) *kind = sig ? CIGPU_FP32_SIGMA : CIGPU_FP32_STORED;
+    if (rank) *rank = sig ? crs->sig->rank : 0;
+    if (padded) *padded = sig ? crs->sig->R : 0;
     return CIGPU_OK;
 }
 

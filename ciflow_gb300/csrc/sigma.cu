@@ -23,15 +23,21 @@
 // products and residuals keep using the stored matrix, whose elements are the
 // reference's bit for bit; the residual the solver reports is that exact one.
 //
-// Both passes run on tiles of 32 alpha x 32 beta strings, 8 warps. In the alpha
+// Both passes run on tiles of 32 alpha x 32 beta strings (8 warps in the first
+// pass, 16 in the second). In the alpha
 // phase warp w takes alpha rows of the tile with its lanes on consecutive beta
 // strings: every lane of the warp walks the same alpha excitations (uniform
 // coefficients, broadcast from shared memory) and reads x at consecutive beta
 // strings (coalesced). In the beta phase the warp takes beta columns with its
 // lanes on consecutive alpha strings and reads the transposed vectors. The two
 // phases meet in a shared-memory tile; the A_k x vectors are written in both
-// orders ([Da][R][Db] and [Db][R][Da]) so that the second pass reads both phases
-// coalesced.
+// string orders, in blocks of 32 strings with the factor index outside the 32
+// ([Da][Db/32][R][32] and [Db][Da/32][R][32]): in the second pass each load
+// instruction of a warp reads 128 contiguous bytes (one factor of 32 consecutive
+// strings) and one excitation's R factors are one contiguous block. (Factors
+// innermost per determinant, read with 16-byte lane loads, spread every such load
+// over 16 cache lines: 156 against 126 us at L=11.) The tile's excitation lists
+// (target, orbital pair, sign) are staged in shared memory.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -44,25 +50,40 @@ namespace cigpu {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;   // pass 1: 8 warps, 4 rows (columns) of the tile each
 constexpr int kWarps = kThreads / 32;
+constexpr int kThreadsB = 512;  // pass 2: 16 warps, 2 rows (columns) each
+constexpr int kWarpsB = kThreadsB / 32;
 constexpr int kYtRow = kSigmaChunk * (kTile + 1) + 1;  // staging tile row (odd: the column phase is conflict-free)
 
 struct SigmaArgs {
     int L, R, nsa, nsb;
     int64_t Da, Db;
+    int64_t nTa, nTb;  // 32-string tiles of each spin (the factor blocks of Ya, Yb)
     const uint32_t *sa_t, *sa_i, *sb_t, *sb_i;  // single excitations: targets and packed info per string
 };
 
-// The e-th single excitation of string S: target J, orbital pair index lo * L + hi,
-// and the sign of <S|E_pq|J> (odd number of electrons between the two orbitals).
-__device__ __forceinline__ void excitation(const uint32_t *tgt, const uint32_t *info, int64_t at, int L, uint32_t &J,
-                                           int &pq, float &sg) {
-    J = __ldg(tgt + at);
-    const uint32_t inf = __ldg(info + at);
-    pq = (int)(inf & 63u) * L + (int)((inf >> 6) & 63u);
-    sg = (inf >> 24) & 1u ? -1.f : 1.f;
+// The single excitations of the tile's 32 strings s0.. in shared memory, as
+// {target J, (lo * L + hi) << 1 | negative}: the orbital pair of E_pq and the sign
+// of <S|E_pq|J> (odd number of electrons between the two orbitals). Strings past
+// the space get {0, 0}.
+__device__ __forceinline__ void stage_excitations(const uint32_t *__restrict__ tgt, const uint32_t *__restrict__ info,
+                                                  int64_t s0, int64_t D, int ns, int L, uint2 *dst) {
+    for (int i = threadIdx.x; i < kTile * ns; i += blockDim.x) {
+        const int r = i / ns;
+        const int64_t S = s0 + r;
+        uint2 v = make_uint2(0u, 0u);
+        if (S < D) {
+            const int64_t at = S * ns + (i - r * ns);
+            const uint32_t inf = __ldg(info + at);
+            v.x = __ldg(tgt + at);
+            v.y = (((inf & 63u) * (uint32_t)L + ((inf >> 6) & 63u)) << 1) | ((inf >> 24) & 1u);
+        }
+        dst[i] = v;
+    }
 }
+__device__ __forceinline__ float exc_sign(uint32_t packed) { return (packed & 1u) ? -1.f : 1.f; }
+__device__ __forceinline__ float dot4(const float4 a, const float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
 
 __global__ void k_transpose32(const float *__restrict__ a, int64_t rows, int64_t cols, float *__restrict__ t) {
     __shared__ float tile[kTile][kTile + 1];
@@ -78,42 +99,48 @@ __global__ void k_transpose32(const float *__restrict__ a, int64_t rows, int64_t
     }
 }
 
-// Pass 1: Ya[Ia][k][Ib] = Yb[Ib][k][Ia] = (A_k x)(Ia, Ib), kx = K x.
-__global__ void __launch_bounds__(kThreads, 2)
+// Pass 1: (A_k x)(Ia, Ib) into Ya at ((Ia * nTb + Ib / 32) * R + k) * 32 + Ib % 32
+// and into Yb at ((Ib * nTa + Ia / 32) * R + k) * 32 + Ia % 32, and kx = K x.
+// Per-string diagonal sums fa, fb are factor-major ([R][D]).
+__global__ void __launch_bounds__(kThreads, 2)  // shared memory holds it to two blocks per SM
     k_sigma_a(const SigmaArgs a, const float *__restrict__ F, const float *__restrict__ K1,
               const float *__restrict__ fa, const float *__restrict__ fb, const float *__restrict__ ka,
               const float *__restrict__ kb, const float *__restrict__ x, const float *__restrict__ xT,
               float *__restrict__ Ya, float *__restrict__ Yb, float *__restrict__ kx) {
     extern __shared__ __align__(16) float sm[];
     const int L2 = a.L * a.L, R = a.R;
-    float *Fs = sm;                               // [L2][R]
-    float *Ks = Fs + (size_t)L2 * R;              // [L2] (padded to 4)
-    float *yt = Ks + ((L2 + 3) & ~3);             // [kTile][kYtRow]
-    float *kt = yt + kTile * kYtRow;              // [kTile][kTile + 1]
+    float *Fs = sm;                                                 // [L2][R]
+    float *Ks = Fs + (size_t)L2 * R;                                // [L2] (padded to 4)
+    uint2 *ea = reinterpret_cast<uint2 *>(Ks + ((L2 + 3) & ~3));    // [kTile][nsa]
+    uint2 *eb = ea + kTile * a.nsa;                                 // [kTile][nsb]
+    float *yt = reinterpret_cast<float *>(eb + kTile * a.nsb);      // [kTile][kYtRow]
+    float *kt = yt + kTile * kYtRow;                                // [kTile][kTile + 1]
     for (int i = threadIdx.x; i < L2 * R; i += kThreads) Fs[i] = F[i];
     for (int i = threadIdx.x; i < L2; i += kThreads) Ks[i] = K1[i];
     const int64_t ta = (int64_t)blockIdx.y * kTile, tb = (int64_t)blockIdx.x * kTile;
+    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea);
+    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int c = 0; c < R; c += kSigmaChunk) {
         __syncthreads();  // tables staged / the previous chunk's tile written out
         // alpha phase: warp rows r, lanes on beta strings
         for (int r = warp; r < kTile; r += kWarps) {
             const int64_t Ia = ta + r, Ib = tb + lane;
-            const bool rowok = Ia < a.Da, ok = rowok && Ib < a.Db;
+            const bool ok = Ia < a.Da && Ib < a.Db;
             float acc[kSigmaChunk], kacc = 0.f;
-            const float xi = ok ? x[Ia * a.Db + Ib] : 0.f;
 #pragma unroll
-            for (int k = 0; k < kSigmaChunk; ++k)
-                acc[k] = ok ? xi * (fa[(int64_t)(c + k) * a.Da + Ia] + fb[(int64_t)(c + k) * a.Db + Ib]) : 0.f;
-            if (c == 0 && ok) kacc = xi * (ka[Ia] + kb[Ib]);
-            if (rowok) {
+            for (int k = 0; k < kSigmaChunk; ++k) acc[k] = 0.f;
+            if (ok) {
+                const float xi = x[Ia * a.Db + Ib];
+#pragma unroll
+                for (int k = 0; k < kSigmaChunk; ++k)
+                    acc[k] = xi * (fa[(int64_t)(c + k) * a.Da + Ia] + fb[(int64_t)(c + k) * a.Db + Ib]);
+                if (c == 0) kacc = xi * (ka[Ia] + kb[Ib]);
+                const uint2 *ex = ea + r * a.nsa;
                 for (int e = 0; e < a.nsa; ++e) {
-                    uint32_t J;
-                    int pq;
-                    float sg;
-                    excitation(a.sa_t, a.sa_i, Ia * a.nsa + e, a.L, J, pq, sg);
-                    const float xv = ok ? sg * x[(int64_t)J * a.Db + Ib] : 0.f;
-                    const float4 *f4 = reinterpret_cast<const float4 *>(Fs + (size_t)pq * R + c);
+                    const uint2 v = ex[e];
+                    const float xv = exc_sign(v.y) * x[(int64_t)v.x * a.Db + Ib];
+                    const float4 *f4 = reinterpret_cast<const float4 *>(Fs + (size_t)(v.y >> 1) * R + c);
 #pragma unroll
                     for (int q = 0; q < kSigmaChunk / 4; ++q) {
                         const float4 f = f4[q];
@@ -122,7 +149,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                         acc[4 * q + 2] += f.z * xv;
                         acc[4 * q + 3] += f.w * xv;
                     }
-                    if (c == 0) kacc += Ks[pq] * xv;
+                    if (c == 0) kacc += Ks[v.y >> 1] * xv;
                 }
             }
 #pragma unroll
@@ -133,18 +160,16 @@ __global__ void __launch_bounds__(kThreads, 2)
         // beta phase: warp columns cl, lanes on alpha strings
         for (int cl = warp; cl < kTile; cl += kWarps) {
             const int64_t Ib = tb + cl, Ia = ta + lane;
-            const bool colok = Ib < a.Db, ok = colok && Ia < a.Da;
+            const bool ok = Ib < a.Db && Ia < a.Da;
             float acc[kSigmaChunk], kacc = 0.f;
 #pragma unroll
             for (int k = 0; k < kSigmaChunk; ++k) acc[k] = 0.f;
-            if (colok) {
+            if (ok) {
+                const uint2 *ex = eb + cl * a.nsb;
                 for (int e = 0; e < a.nsb; ++e) {
-                    uint32_t J;
-                    int pq;
-                    float sg;
-                    excitation(a.sb_t, a.sb_i, Ib * a.nsb + e, a.L, J, pq, sg);
-                    const float xv = ok ? sg * xT[(int64_t)J * a.Da + Ia] : 0.f;
-                    const float4 *f4 = reinterpret_cast<const float4 *>(Fs + (size_t)pq * R + c);
+                    const uint2 v = ex[e];
+                    const float xv = exc_sign(v.y) * xT[(int64_t)v.x * a.Da + Ia];
+                    const float4 *f4 = reinterpret_cast<const float4 *>(Fs + (size_t)(v.y >> 1) * R + c);
 #pragma unroll
                     for (int q = 0; q < kSigmaChunk / 4; ++q) {
                         const float4 f = f4[q];
@@ -153,7 +178,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                         acc[4 * q + 2] += f.z * xv;
                         acc[4 * q + 3] += f.w * xv;
                     }
-                    if (c == 0) kacc += Ks[pq] * xv;
+                    if (c == 0) kacc += Ks[v.y >> 1] * xv;
                 }
             }
 #pragma unroll
@@ -161,16 +186,18 @@ __global__ void __launch_bounds__(kThreads, 2)
             if (c == 0) kt[lane * (kTile + 1) + cl] += kacc;
         }
         __syncthreads();
-        // write out both orders, 32 consecutive strings per warp row
+        // write out both orders: per string of the tile, this chunk's 16 factor rows of 32
         for (int row = warp; row < kTile * kSigmaChunk; row += kWarps) {
             const int r = row / kSigmaChunk, k = row - r * kSigmaChunk;
             {
                 const int64_t Ia = ta + r, Ib = tb + lane;
-                if (Ia < a.Da && Ib < a.Db) Ya[(Ia * R + c + k) * a.Db + Ib] = yt[r * kYtRow + k * (kTile + 1) + lane];
+                if (Ia < a.Da && Ib < a.Db)
+                    Ya[((Ia * a.nTb + blockIdx.x) * R + c + k) * kTile + lane] = yt[r * kYtRow + k * (kTile + 1) + lane];
             }
             {
                 const int64_t Ib = tb + r, Ia = ta + lane;  // r is a beta column here
-                if (Ia < a.Da && Ib < a.Db) Yb[(Ib * R + c + k) * a.Da + Ia] = yt[lane * kYtRow + k * (kTile + 1) + r];
+                if (Ia < a.Da && Ib < a.Db)
+                    Yb[((Ib * a.nTa + blockIdx.y) * R + c + k) * kTile + lane] = yt[lane * kYtRow + k * (kTile + 1) + r];
             }
         }
         if (c == 0)
@@ -181,98 +208,109 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// Pass 2: y = K x + sum_k A_k (1/2 s_k y_k), the scaled factors G = 1/2 s_k F^k.
-__global__ void __launch_bounds__(kThreads, 2)
+// sum_k G^k_pq y_k(J): g the factor row pq (shared memory), yj this lane's entry of
+// string J's factor block (factor k at yj[32 k]: a warp reads 128 contiguous bytes).
+__device__ __forceinline__ float excitation_term(const float4 *__restrict__ g, const float *__restrict__ yj, int R4) {
+    float t = 0.f;
+#pragma unroll 4
+    for (int q = 0; q < R4; ++q) {
+        const float4 gq = g[q];
+        t += gq.x * yj[(4 * q) * kTile] + gq.y * yj[(4 * q + 1) * kTile] + gq.z * yj[(4 * q + 2) * kTile] +
+             gq.w * yj[(4 * q + 3) * kTile];
+    }
+    return t;
+}
+
+// Pass 2: y = K x + sum_k A_k (1/2 s_k y_k), the scaled factors G = 1/2 s_k F^k;
+// ga, gb factor-major ([R][D]).
+__global__ void __launch_bounds__(kThreadsB, 2)
     k_sigma_b(const SigmaArgs a, const float *__restrict__ G, const float *__restrict__ ga,
               const float *__restrict__ gb, const float *__restrict__ Ya, const float *__restrict__ Yb,
               const float *__restrict__ kx, float *__restrict__ y) {
     extern __shared__ __align__(16) float sm[];
-    const int L2 = a.L * a.L, R = a.R;
-    float *Gs = sm;                     // [L2][R]
-    float *st = Gs + (size_t)L2 * R;    // [kTile][kTile + 1]
-    for (int i = threadIdx.x; i < L2 * R; i += kThreads) Gs[i] = G[i];
-    __syncthreads();
+    const int L2 = a.L * a.L, R = a.R, R4 = R / 4;
+    float *Gs = sm;                                              // [L2][R]
+    uint2 *ea = reinterpret_cast<uint2 *>(Gs + (size_t)L2 * R);  // [kTile][nsa]
+    uint2 *eb = ea + kTile * a.nsa;                              // [kTile][nsb]
+    float *st = reinterpret_cast<float *>(eb + kTile * a.nsb);   // [kTile][kTile + 1]
+    for (int i = threadIdx.x; i < L2 * R; i += kThreadsB) Gs[i] = G[i];
     const int64_t ta = (int64_t)blockIdx.y * kTile, tb = (int64_t)blockIdx.x * kTile;
+    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea);
+    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb);
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float4 *G4 = reinterpret_cast<const float4 *>(Gs);
     // alpha phase with the diagonal and K x
-    for (int r = warp; r < kTile; r += kWarps) {
+    for (int r = warp; r < kTile; r += kWarpsB) {
         const int64_t Ia = ta + r, Ib = tb + lane;
-        const bool rowok = Ia < a.Da, ok = rowok && Ib < a.Db;
         float acc = 0.f;
-        if (ok) {
+        if (Ia < a.Da && Ib < a.Db) {
             acc = kx[Ia * a.Db + Ib];
-            const float *yi = Ya + Ia * R * a.Db + Ib;
+            const float *yi = Ya + (Ia * a.nTb + blockIdx.x) * R * kTile + lane;
             for (int k = 0; k < R; ++k)
-                acc += yi[(int64_t)k * a.Db] * (ga[(int64_t)k * a.Da + Ia] + gb[(int64_t)k * a.Db + Ib]);
-        }
-        if (rowok) {
-            for (int e = 0; e < a.nsa; ++e) {
-                uint32_t J;
-                int pq;
-                float sg;
-                excitation(a.sa_t, a.sa_i, Ia * a.nsa + e, a.L, J, pq, sg);
-                if (!ok) continue;
-                const float *yj = Ya + (int64_t)J * R * a.Db + Ib;
-                const float4 *g4 = reinterpret_cast<const float4 *>(Gs + (size_t)pq * R);
-                float t = 0.f;
-                for (int q = 0; q < R / 4; ++q) {
-                    const float4 g = g4[q];
-                    t += g.x * yj[(int64_t)(4 * q) * a.Db];
-                    t += g.y * yj[(int64_t)(4 * q + 1) * a.Db];
-                    t += g.z * yj[(int64_t)(4 * q + 2) * a.Db];
-                    t += g.w * yj[(int64_t)(4 * q + 3) * a.Db];
-                }
-                acc += sg * t;
+                acc += yi[k * kTile] * (ga[(int64_t)k * a.Da + Ia] + gb[(int64_t)k * a.Db + Ib]);
+            const uint2 *ex = ea + r * a.nsa;
+            const float *yb = Ya + (int64_t)blockIdx.x * R * kTile + lane;  // string J's block: yb + J * nTb * R * 32
+            const int64_t js = a.nTb * R * kTile;
+            int e = 0;
+            for (; e + 1 < a.nsa; e += 2) {  // two excitations' loads in flight together
+                const uint2 v0 = ex[e], v1 = ex[e + 1];
+                const float t0 = excitation_term(G4 + (size_t)(v0.y >> 1) * R4, yb + v0.x * js, R4);
+                const float t1 = excitation_term(G4 + (size_t)(v1.y >> 1) * R4, yb + v1.x * js, R4);
+                acc += exc_sign(v0.y) * t0 + exc_sign(v1.y) * t1;
+            }
+            if (e < a.nsa) {
+                const uint2 v0 = ex[e];
+                acc += exc_sign(v0.y) * excitation_term(G4 + (size_t)(v0.y >> 1) * R4, yb + v0.x * js, R4);
             }
         }
         st[r * (kTile + 1) + lane] = acc;
     }
     __syncthreads();
-    for (int cl = warp; cl < kTile; cl += kWarps) {
+    for (int cl = warp; cl < kTile; cl += kWarpsB) {
         const int64_t Ib = tb + cl, Ia = ta + lane;
-        const bool colok = Ib < a.Db, ok = colok && Ia < a.Da;
         float acc = 0.f;
-        if (colok) {
-            for (int e = 0; e < a.nsb; ++e) {
-                uint32_t J;
-                int pq;
-                float sg;
-                excitation(a.sb_t, a.sb_i, Ib * a.nsb + e, a.L, J, pq, sg);
-                if (!ok) continue;
-                const float *yj = Yb + (int64_t)J * R * a.Da + Ia;
-                const float4 *g4 = reinterpret_cast<const float4 *>(Gs + (size_t)pq * R);
-                float t = 0.f;
-                for (int q = 0; q < R / 4; ++q) {
-                    const float4 g = g4[q];
-                    t += g.x * yj[(int64_t)(4 * q) * a.Da];
-                    t += g.y * yj[(int64_t)(4 * q + 1) * a.Da];
-                    t += g.z * yj[(int64_t)(4 * q + 2) * a.Da];
-                    t += g.w * yj[(int64_t)(4 * q + 3) * a.Da];
-                }
-                acc += sg * t;
+        if (Ib < a.Db && Ia < a.Da) {
+            const uint2 *ex = eb + cl * a.nsb;
+            const float *yb = Yb + (int64_t)blockIdx.y * R * kTile + lane;  // string J's block: yb + J * nTa * R * 32
+            const int64_t js = a.nTa * R * kTile;
+            int e = 0;
+            for (; e + 1 < a.nsb; e += 2) {
+                const uint2 v0 = ex[e], v1 = ex[e + 1];
+                const float t0 = excitation_term(G4 + (size_t)(v0.y >> 1) * R4, yb + v0.x * js, R4);
+                const float t1 = excitation_term(G4 + (size_t)(v1.y >> 1) * R4, yb + v1.x * js, R4);
+                acc += exc_sign(v0.y) * t0 + exc_sign(v1.y) * t1;
+            }
+            if (e < a.nsb) {
+                const uint2 v0 = ex[e];
+                acc += exc_sign(v0.y) * excitation_term(G4 + (size_t)(v0.y >> 1) * R4, yb + v0.x * js, R4);
             }
         }
         st[lane * (kTile + 1) + cl] += acc;
     }
     __syncthreads();
-    for (int r = warp; r < kTile; r += kWarps) {
+    for (int r = warp; r < kTile; r += kWarpsB) {
         const int64_t Ia = ta + r, Ib = tb + lane;
         if (Ia < a.Da && Ib < a.Db) y[Ia * a.Db + Ib] = st[r * (kTile + 1) + lane];
     }
 }
 
-size_t smem_a_bytes(int L, int R) {
+size_t smem_a_bytes(int L, int R, int nsa, int nsb) {
     const int L2 = L * L;
-    return sizeof(float) * ((size_t)L2 * R + ((L2 + 3) & ~3) + (size_t)kTile * kYtRow + (size_t)kTile * (kTile + 1));
+    return sizeof(float) * ((size_t)L2 * R + ((L2 + 3) & ~3)) + sizeof(uint2) * (size_t)kTile * (nsa + nsb) +
+           sizeof(float) * ((size_t)kTile * kYtRow + (size_t)kTile * (kTile + 1));
 }
-size_t smem_b_bytes(int L, int R) { return sizeof(float) * ((size_t)L * L * R + (size_t)kTile * (kTile + 1)); }
+size_t smem_b_bytes(int L, int R, int nsa, int nsb) {
+    return sizeof(float) * (size_t)L * L * R + sizeof(uint2) * (size_t)kTile * (nsa + nsb) +
+           sizeof(float) * (size_t)kTile * (kTile + 1);
+}
 constexpr size_t kSigmaMaxSmem = 200 * 1024;
 
 }  // namespace
 
 size_t sigma_bytes(int L, int64_t Da, int64_t Db, int R) {
-    const int64_t dim = Da * Db;
-    return sizeof(float) * ((size_t)dim * (2 * (size_t)R + 2) + (size_t)(Da + Db) * (2 * R + 1) +
+    const int64_t dim = Da * Db, padded = Da * ((Db + kTile - 1) / kTile) * kTile + Db * ((Da + kTile - 1) / kTile) * kTile;
+    return sizeof(float) * ((size_t)padded * R + 2 * (size_t)dim + (size_t)(Da + Db) * (2 * R + 1) +
                             (size_t)L * L * (2 * R + 1));
 }
 
@@ -353,7 +391,9 @@ bool sigma_prepare(SigmaOp &op, int L, const double *h, const double *eri, const
     }
     const int rank = (int)vecs.size();
     const int R = std::max(kSigmaChunk, (rank + kSigmaChunk - 1) / kSigmaChunk * kSigmaChunk);
-    if (R > kSigmaMaxRank || smem_a_bytes(L, R) > kSigmaMaxSmem || smem_b_bytes(L, R) > kSigmaMaxSmem) return false;
+    if (R > kSigmaMaxRank || smem_a_bytes(L, R, ta.ns, tb.ns) > kSigmaMaxSmem ||
+        smem_b_bytes(L, R, ta.ns, tb.ns) > kSigmaMaxSmem)
+        return false;
     std::vector<float> F(N * R, 0.f), G(N * R, 0.f), K1(N);
     for (int j = 0; j < rank; ++j)
         for (int i = 0; i < P; ++i) {
@@ -410,15 +450,16 @@ bool sigma_prepare(SigmaOp &op, int L, const double *h, const double *eri, const
     up(op.kb, kbv);
     const int64_t dim = ta.D * tb.D;
     op.xT.alloc((size_t)dim);
-    op.Ya.alloc((size_t)dim * R);
-    op.Yb.alloc((size_t)dim * R);
+    const int64_t nTa = (ta.D + kTile - 1) / kTile, nTb = (tb.D + kTile - 1) / kTile;
+    op.Ya.alloc((size_t)ta.D * nTb * kTile * R);  // factor blocks of 32 strings, the last one padded
+    op.Yb.alloc((size_t)tb.D * nTa * kTile * R);
     op.kx.alloc((size_t)dim);
     op.L = L;
     op.rank = rank;
     op.Da = ta.D;
     op.Db = tb.D;
-    op.smem_a = smem_a_bytes(L, R);
-    op.smem_b = smem_b_bytes(L, R);
+    op.smem_a = smem_a_bytes(L, R, ta.ns, tb.ns);
+    op.smem_b = smem_b_bytes(L, R, ta.ns, tb.ns);
     op.R = R;
     return true;
 }
@@ -430,12 +471,23 @@ void sigma_mv32(SigmaOp &op, const FciParams &p, const float *x, float *y, cudaS
         return true;
     }();
     (void)attr_set;
-    const SigmaArgs a{op.L, op.R, p.a.ns, p.b.ns, op.Da, op.Db, p.a.s_target, p.a.s_info, p.b.s_target, p.b.s_info};
+    const SigmaArgs a{op.L,
+                      op.R,
+                      p.a.ns,
+                      p.b.ns,
+                      op.Da,
+                      op.Db,
+                      (op.Da + kTile - 1) / kTile,
+                      (op.Db + kTile - 1) / kTile,
+                      p.a.s_target,
+                      p.a.s_info,
+                      p.b.s_target,
+                      p.b.s_info};
     const dim3 tgrid((unsigned)((op.Db + kTile - 1) / kTile), (unsigned)((op.Da + kTile - 1) / kTile));
     k_transpose32<<<tgrid, dim3(kTile, 8), 0, s>>>(x, op.Da, op.Db, op.xT.p);
     k_sigma_a<<<tgrid, kThreads, op.smem_a, s>>>(a, op.F.p, op.K1.p, op.fa.p, op.fb.p, op.ka.p, op.kb.p, x, op.xT.p,
                                                   op.Ya.p, op.Yb.p, op.kx.p);
-    k_sigma_b<<<tgrid, kThreads, op.smem_b, s>>>(a, op.G.p, op.ga.p, op.gb.p, op.Ya.p, op.Yb.p, op.kx.p, y);
+    k_sigma_b<<<tgrid, kThreadsB, op.smem_b, s>>>(a, op.G.p, op.ga.p, op.gb.p, op.Ya.p, op.Yb.p, op.kx.p, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch(3);
 }

@@ -127,7 +127,7 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
 /* Device storage of the matrix (no reference counterpart; reported with matvec
  * measurements). CIGPU_LAYOUT_CRS: full symmetric CRS, stored = nnz_full values
  * with a 4-byte column each. CIGPU_LAYOUT_SLOTS (FCI): values only (FP32 hi + lo
- * for MIXED, FP64 for FP64), every structural slot of every row (zeros included,
+ * for MIXED, FP64 for FP64 and for MIXED with the sigma FP32 product), every structural slot of every row (zeros included,
  * rows padded to tiles of 64 beta strings), stored = that slot count; columns are
  * regenerated from the string tables. CIGPU_LAYOUT_PAIRS (DOCI): no stored matrix,
  * stored = 0; every matvec generates the pair hops from the pair strings and the
@@ -135,6 +135,17 @@ int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64
  * stored matrix. The explicit CRS of every layout is generated for the exports. */
 enum { CIGPU_LAYOUT_CRS = 0, CIGPU_LAYOUT_SLOTS = 1, CIGPU_LAYOUT_ONTHEFLY = 2, CIGPU_LAYOUT_PAIRS = 3 };
 int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored);
+/* The FP32 product of a MIXED matrix (no reference counterpart; reported with
+ * matvec measurements). CIGPU_FP32_STORED: the stored FP32 values (slot tiles,
+ * CRS) or the DOCI pair hops. CIGPU_FP32_SIGMA (FCI): a direct-CI sigma vector
+ * from a factorisation (pq|rs) = sum_k s_k F^k_pq F^k_rs, rank = the factors kept,
+ * padded = the rank the kernels run (a multiple of 16); the FP64 products use the
+ * stored matrix. rank and padded are 0 for the stored product. FP64 matrices
+ * report CIGPU_FP32_STORED. The environment variable CIGPU_FP32_PRODUCT, read at
+ * each build, selects "slots" or "sigma"; by default the sigma product is taken
+ * where its 32 x 32 string tiles outnumber the SMs. */
+enum { CIGPU_FP32_STORED = 0, CIGPU_FP32_SIGMA = 1 };
+int cigpu_crs_fp32_product(const cigpu_crs *crs, int *kind, int *rank, int *padded);
 /* Upper triangle in the reference layout (SparseMatrix_CRS::row/col/data,
  * SparseMatrix_CRS.h:107-111): row[dim+1], col[nnz_upper], val[nnz_upper]. Host buffers. */
 int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val);
