@@ -31,12 +31,13 @@
 // strings (coalesced). In the beta phase the warp takes beta columns with its
 // lanes on consecutive alpha strings and reads the transposed vectors. The two
 // phases meet in a shared-memory tile; the A_k x vectors are written in both
-// string orders, in blocks of 32 strings with the factor index outside the 32
-// ([Da][Db/32][R][32] and [Db][Da/32][R][32]): in the second pass each load
-// instruction of a warp reads 128 contiguous bytes (one factor of 32 consecutive
-// strings) and one excitation's R factors are one contiguous block. (Factors
-// innermost per determinant, read with 16-byte lane loads, spread every such load
-// over 16 cache lines: 156 against 126 us at L=11.) The tile's excitation lists
+// string orders, in blocks of 32 strings with the factors in groups of four
+// outside the 32 ([Da][Db/32][R/4][32][4] and [Db][Da/32][R/4][32][4]): in the
+// second pass a lane reads four factors of its determinant with one 16-byte load
+// and the warp's load covers 512 contiguous bytes, so one excitation is R/4 loads
+// and its factors one contiguous block. (Measured at L=11: factors innermost per
+// determinant, each 16-byte load of a warp spread over 16 cache lines, 156 us;
+// one factor of 32 strings per 4-byte load, 66 us.) The tile's excitation lists
 // (target, orbital pair, sign) are staged in shared memory.
 #include <algorithm>
 #include <cmath>
@@ -99,8 +100,8 @@ __global__ void k_transpose32(const float *__restrict__ a, int64_t rows, int64_t
     }
 }
 
-// Pass 1: (A_k x)(Ia, Ib) into Ya at ((Ia * nTb + Ib / 32) * R + k) * 32 + Ib % 32
-// and into Yb at ((Ib * nTa + Ia / 32) * R + k) * 32 + Ia % 32, and kx = K x.
+// Pass 1: (A_k x)(Ia, Ib) into Ya at (((Ia * nTb + Ib / 32) * R / 4 + k / 4) * 32 + Ib % 32) * 4 + k % 4
+// and into Yb with the spins exchanged, and kx = K x.
 // Per-string diagonal sums fa, fb are factor-major ([R][D]).
 __global__ void __launch_bounds__(kThreads, 2)  // shared memory holds it to two blocks per SM
     k_sigma_a(const SigmaArgs a, const float *__restrict__ F, const float *__restrict__ K1,
@@ -186,18 +187,26 @@ __global__ void __launch_bounds__(kThreads, 2)  // shared memory holds it to two
             if (c == 0) kt[lane * (kTile + 1) + cl] += kacc;
         }
         __syncthreads();
-        // write out both orders: per string of the tile, this chunk's 16 factor rows of 32
-        for (int row = warp; row < kTile * kSigmaChunk; row += kWarps) {
-            const int r = row / kSigmaChunk, k = row - r * kSigmaChunk;
+        // write out both orders: per string of the tile, this chunk's four groups of
+        // four factors for 32 strings (512 contiguous bytes per warp store)
+        for (int row = warp; row < kTile * (kSigmaChunk / 4); row += kWarps) {
+            const int r = row / (kSigmaChunk / 4), q = row - r * (kSigmaChunk / 4);
+            const int g = c / 4 + q;  // factor group
             {
                 const int64_t Ia = ta + r, Ib = tb + lane;
-                if (Ia < a.Da && Ib < a.Db)
-                    Ya[((Ia * a.nTb + blockIdx.x) * R + c + k) * kTile + lane] = yt[r * kYtRow + k * (kTile + 1) + lane];
+                if (Ia < a.Da && Ib < a.Db) {
+                    const float *src = yt + r * kYtRow + 4 * q * (kTile + 1) + lane;
+                    reinterpret_cast<float4 *>(Ya)[((Ia * a.nTb + blockIdx.x) * (R / 4) + g) * kTile + lane] =
+                        make_float4(src[0], src[kTile + 1], src[2 * (kTile + 1)], src[3 * (kTile + 1)]);
+                }
             }
             {
                 const int64_t Ib = tb + r, Ia = ta + lane;  // r is a beta column here
-                if (Ia < a.Da && Ib < a.Db)
-                    Yb[((Ib * a.nTa + blockIdx.y) * R + c + k) * kTile + lane] = yt[lane * kYtRow + k * (kTile + 1) + r];
+                if (Ia < a.Da && Ib < a.Db) {
+                    const float *src = yt + lane * kYtRow + 4 * q * (kTile + 1) + r;
+                    reinterpret_cast<float4 *>(Yb)[((Ib * a.nTa + blockIdx.y) * (R / 4) + g) * kTile + lane] =
+                        make_float4(src[0], src[kTile + 1], src[2 * (kTile + 1)], src[3 * (kTile + 1)]);
+                }
             }
         }
         if (c == 0)
@@ -208,16 +217,12 @@ __global__ void __launch_bounds__(kThreads, 2)  // shared memory holds it to two
     }
 }
 
-// sum_k G^k_pq y_k(J): g the factor row pq (shared memory), yj this lane's entry of
-// string J's factor block (factor k at yj[32 k]: a warp reads 128 contiguous bytes).
-__device__ __forceinline__ float excitation_term(const float4 *__restrict__ g, const float *__restrict__ yj, int R4) {
+// sum_k G^k_pq y_k(J): g the factor row pq (shared memory), yj this lane's first
+// group of four factors in string J's block (group q at yj[32 q]).
+__device__ __forceinline__ float excitation_term(const float4 *__restrict__ g, const float4 *__restrict__ yj, int R4) {
     float t = 0.f;
 #pragma unroll 4
-    for (int q = 0; q < R4; ++q) {
-        const float4 gq = g[q];
-        t += gq.x * yj[(4 * q) * kTile] + gq.y * yj[(4 * q + 1) * kTile] + gq.z * yj[(4 * q + 2) * kTile] +
-             gq.w * yj[(4 * q + 3) * kTile];
-    }
+    for (int q = 0; q < R4; ++q) t += dot4(g[q], yj[q * kTile]);
     return t;
 }
 
@@ -246,12 +251,19 @@ __global__ void __launch_bounds__(kThreadsB, 2)
         float acc = 0.f;
         if (Ia < a.Da && Ib < a.Db) {
             acc = kx[Ia * a.Db + Ib];
-            const float *yi = Ya + (Ia * a.nTb + blockIdx.x) * R * kTile + lane;
-            for (int k = 0; k < R; ++k)
-                acc += yi[k * kTile] * (ga[(int64_t)k * a.Da + Ia] + gb[(int64_t)k * a.Db + Ib]);
+            const float4 *yi = reinterpret_cast<const float4 *>(Ya) + (Ia * a.nTb + blockIdx.x) * R4 * kTile + lane;
+            for (int q = 0; q < R4; ++q) {
+                const float4 v = yi[q * kTile];
+                const int k = 4 * q;
+                acc += v.x * (ga[(int64_t)k * a.Da + Ia] + gb[(int64_t)k * a.Db + Ib]) +
+                       v.y * (ga[(int64_t)(k + 1) * a.Da + Ia] + gb[(int64_t)(k + 1) * a.Db + Ib]) +
+                       v.z * (ga[(int64_t)(k + 2) * a.Da + Ia] + gb[(int64_t)(k + 2) * a.Db + Ib]) +
+                       v.w * (ga[(int64_t)(k + 3) * a.Da + Ia] + gb[(int64_t)(k + 3) * a.Db + Ib]);
+            }
             const uint2 *ex = ea + r * a.nsa;
-            const float *yb = Ya + (int64_t)blockIdx.x * R * kTile + lane;  // string J's block: yb + J * nTb * R * 32
-            const int64_t js = a.nTb * R * kTile;
+            // string J's block: yb + J * js
+            const float4 *yb = reinterpret_cast<const float4 *>(Ya) + (int64_t)blockIdx.x * R4 * kTile + lane;
+            const int64_t js = a.nTb * R4 * kTile;
             int e = 0;
             for (; e + 1 < a.nsa; e += 2) {  // two excitations' loads in flight together
                 const uint2 v0 = ex[e], v1 = ex[e + 1];
@@ -272,8 +284,8 @@ __global__ void __launch_bounds__(kThreadsB, 2)
         float acc = 0.f;
         if (Ib < a.Db && Ia < a.Da) {
             const uint2 *ex = eb + cl * a.nsb;
-            const float *yb = Yb + (int64_t)blockIdx.y * R * kTile + lane;  // string J's block: yb + J * nTa * R * 32
-            const int64_t js = a.nTa * R * kTile;
+            const float4 *yb = reinterpret_cast<const float4 *>(Yb) + (int64_t)blockIdx.y * R4 * kTile + lane;
+            const int64_t js = a.nTa * R4 * kTile;
             int e = 0;
             for (; e + 1 < a.nsb; e += 2) {
                 const uint2 v0 = ex[e], v1 = ex[e + 1];
