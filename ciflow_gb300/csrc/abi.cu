@@ -283,10 +283,11 @@ size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
 struct RowSingles {
     DevBuf<double> sgl64;
     DevBuf<float> sgl_hi, sgl_lo, diag_hi, diag_lo;
-    void make(cigpu_crs &c, FciParams &p, cudaStream_t s) {
+    // fp32: also the FP32 splits (the FP32 fills read them)
+    void make(cigpu_crs &c, FciParams &p, cudaStream_t s, bool fp32) {
         const size_t nsr = (size_t)(c.da.view.ns + c.db.view.ns);
         sgl64.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
-        if (c.precision == CIGPU_MIXED) {
+        if (fp32) {
             sgl_hi.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
             sgl_lo.alloc(std::max<size_t>((size_t)c.dim * nsr, 1));
             diag_hi.alloc(c.dim);
@@ -315,7 +316,7 @@ struct ExplicitCrs {
         }
         FciParams q = c.fp;
         RowSingles rs;
-        rs.make(c, q, s);
+        rs.make(c, q, s, c.precision == CIGPU_MIXED);
         col.alloc(std::max<int64_t>(c.nnz_full, 1));
         q.row_ptr = c.row_ptr.p;
         q.col = col.p;
@@ -394,22 +395,25 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         p.eri_lo = h.d_eri_lo.p;
         p.diag = c.diag.p;
         fci_diag_launch(p, c.diag.p, s);
-        singles.make(c, p, s);
         c.slots = slots_supported(p) &&
                   (c.precision == CIGPU_MIXED || (c.allow_compact && slots64_pay(p)));
+        // MIXED: the FP32 products as the factorised sigma vector where it applies
+        // (its factorisation runs on the host while the diagonal is computed)
+        const int smode = sigma_mode();
+        if (c.slots && c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
+            c.sig.reset(new SigmaOp);
+            if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
+                               smode == kSigmaForced, s))
+                c.sig.reset();
+            tr.mark("sigma factors");
+        }
+        // FP32 splits only for a fill of FP32 values (not for the FP64 values of the
+        // sigma-backed mixed form)
+        singles.make(c, p, s, c.precision == CIGPU_MIXED && !c.sig);
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
         if (c.slots) {
-            // MIXED: the FP32 products as the factorised sigma vector where it applies
-            const int smode = sigma_mode();
-            if (c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
-                c.sig.reset(new SigmaOp);
-                if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
-                                   smode == kSigmaForced, s))
-                    c.sig.reset();
-                tr.mark("sigma factors");
-            }
             // values-only layout: the fill counts the rows itself; MIXED stores FP32
             // hi + lo for its FP32 and FP64 products, or, with the sigma vector doing
             // the FP32 ones, the FP64 values (its anchors take the plain FP64 product)
