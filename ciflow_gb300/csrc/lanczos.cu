@@ -773,6 +773,19 @@ struct Refine {
         const double rn = ops.residual(w.p, c, E, r.p, n);
         return {E, rn};
     }
+    // the same from the FP32 product (c32, w32: FP32 scratch vectors): w = H c to
+    // FP32 accuracy, E and r as above
+    std::pair<double, double> eval32(const SolveProblem &P, double *c, float *c32, float *w32) {
+        ops.dots(c, n, 1, c, n, 0);
+        ops.scale(c, n, 0);
+        dev_convert(c, c32, n, s);
+        P.mv32(c32, w32, s);
+        dev_convert(w32, w.p, n, s);
+        ops.dots(c, n, 1, w.p, n, 0);
+        const double E = ops.fetch(1)[0];
+        const double rn = ops.residual(w.p, c, E, r.p, n);
+        return {E, rn};
+    }
 };
 
 }  // namespace
@@ -923,9 +936,9 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     std::vector<double> A((size_t)kMaxBasis * kMaxBasis, 0.0), eta(kMaxBasis, 0.0), bvec(kMaxBasis, 0.0);
     int collapses = 0;
     double E = 0, rho = 0, gap = 0, last_rho = 1e300;
-    auto anchor = [&]() {  // exact FP64 anchor evaluation
-        const auto er = ref.eval(P, c_dev);
-        ++mv64;
+    auto anchor = [&](bool fp32) {  // anchor evaluation: exact FP64, or the cold start's FP32 one
+        const auto er = fp32 ? ref.eval32(P, c_dev, V.p, HV.p) : ref.eval(P, c_dev);
+        ++(fp32 ? mv32 : mv64);
         E = er.first;
         rho = er.second;
         dev_convert(c_dev, V.p, n, s);          // slot 0
@@ -933,7 +946,11 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         dev_convert(c_dev, cr32.p, n, s);       // c32, r32 for the couplings
         dev_convert(ref.r.p, cr32.p + n, n, s);
     };
-    anchor();
+    // A cold start's first anchor only turns the start vector (residual of order
+    // |H|) into the first basis, so the FP32 product serves it; every later anchor,
+    // and so the residual the solve reports, is the exact FP64 one. A warm start
+    // may already be near the tolerance and takes the FP64 product at once.
+    anchor(!have_start);
     int k = 0;  // corrections in the basis
     double theta = E, a0 = 1.0, yv = 0;
     std::vector<double> y(kMaxBasis + 1, 0.0), yp(kMaxBasis + 1, 0.0), d(kMaxBasis + 1, 0.0);
@@ -1048,7 +1065,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
             CIGPU_CUDA(cudaGetLastError());
             count_launch(2);
             const int kf = k;
-            anchor();
+            anchor(false);
             ++collapses;
             k = 0;
             yv = 0;

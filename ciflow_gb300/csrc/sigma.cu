@@ -43,6 +43,7 @@
 #include <cmath>
 #include <vector>
 
+#include "checked.cuh"
 #include "sigma.cuh"
 #include "small_eigh.h"
 
@@ -62,14 +63,18 @@ struct SigmaArgs {
     int64_t Da, Db;
     int64_t nTa, nTb;  // 32-string tiles of each spin (the factor blocks of Ya, Yb)
     const uint32_t *sa_t, *sa_i, *sb_t, *sb_i;  // single excitations: targets and packed info per string
+    unsigned long long *err;                    // checked build: the error word
 };
 
 // The single excitations of the tile's 32 strings s0.. in shared memory, as
 // {target J, (lo * L + hi) << 1 | negative}: the orbital pair of E_pq and the sign
 // of <S|E_pq|J> (odd number of electrons between the two orbitals). Strings past
 // the space get {0, 0}.
+// (The checked build tests each target against the string count and stages a
+// failing one as {0, 0}.)
 __device__ __forceinline__ void stage_excitations(const uint32_t *__restrict__ tgt, const uint32_t *__restrict__ info,
-                                                  int64_t s0, int64_t D, int ns, int L, uint2 *dst) {
+                                                  int64_t s0, int64_t D, int ns, int L, uint2 *dst,
+                                                  unsigned long long *err) {
     for (int i = threadIdx.x; i < kTile * ns; i += blockDim.x) {
         const int r = i / ns;
         const int64_t S = s0 + r;
@@ -79,9 +84,11 @@ __device__ __forceinline__ void stage_excitations(const uint32_t *__restrict__ t
             const uint32_t inf = __ldg(info + at);
             v.x = __ldg(tgt + at);
             v.y = (((inf & 63u) * (uint32_t)L + ((inf >> 6) & 63u)) << 1) | ((inf >> 24) & 1u);
+            if (!CIGPU_CHECK(err, index_ok(v.x, (uint64_t)D), kCheckColumn, v.x)) v = make_uint2(0u, 0u);
         }
         dst[i] = v;
     }
+    (void)err;
 }
 __device__ __forceinline__ float exc_sign(uint32_t packed) { return (packed & 1u) ? -1.f : 1.f; }
 __device__ __forceinline__ float dot4(const float4 a, const float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
@@ -119,8 +126,8 @@ __global__ void __launch_bounds__(kThreads, 2)  // shared memory holds it to two
     for (int i = threadIdx.x; i < L2 * R; i += kThreads) Fs[i] = F[i];
     for (int i = threadIdx.x; i < L2; i += kThreads) Ks[i] = K1[i];
     const int64_t ta = (int64_t)blockIdx.y * kTile, tb = (int64_t)blockIdx.x * kTile;
-    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea);
-    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb);
+    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea, a.err);
+    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb, a.err);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int c = 0; c < R; c += kSigmaChunk) {
         __syncthreads();  // tables staged / the previous chunk's tile written out
@@ -240,8 +247,8 @@ __global__ void __launch_bounds__(kThreadsB, 2)
     float *st = reinterpret_cast<float *>(eb + kTile * a.nsb);   // [kTile][kTile + 1]
     for (int i = threadIdx.x; i < L2 * R; i += kThreadsB) Gs[i] = G[i];
     const int64_t ta = (int64_t)blockIdx.y * kTile, tb = (int64_t)blockIdx.x * kTile;
-    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea);
-    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb);
+    stage_excitations(a.sa_t, a.sa_i, ta, a.Da, a.nsa, a.L, ea, a.err);
+    stage_excitations(a.sb_t, a.sb_i, tb, a.Db, a.nsb, a.L, eb, a.err);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4 *G4 = reinterpret_cast<const float4 *>(Gs);
@@ -494,7 +501,8 @@ void sigma_mv32(SigmaOp &op, const FciParams &p, const float *x, float *y, cudaS
                       p.a.s_target,
                       p.a.s_info,
                       p.b.s_target,
-                      p.b.s_info};
+                      p.b.s_info,
+                      check_word_device()};
     const dim3 tgrid((unsigned)((op.Db + kTile - 1) / kTile), (unsigned)((op.Da + kTile - 1) / kTile));
     k_transpose32<<<tgrid, dim3(kTile, 8), 0, s>>>(x, op.Da, op.Db, op.xT.p);
     k_sigma_a<<<tgrid, kThreads, op.smem_a, s>>>(a, op.F.p, op.K1.p, op.fa.p, op.fb.p, op.ka.p, op.kb.p, x, op.xT.p,

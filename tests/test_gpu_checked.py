@@ -76,3 +76,11 @@ def test_checked_doci_word_stays_zero(chk, precision):
     ref = O.build_upper(O.DOCI, ints)
     e_ref, _ = O.lowest_eigenpair(ref, tol=1e-12)
     run_case(chk, ints, A.DOCI, precision, e_ref=e_ref + ints.econst)
+
+
+def test_checked_sigma_word_stays_zero(chk, monkeypatch):
+    """The mixed FCI form with its FP32 products from the factorised sigma vector
+    (forced onto L=10 5a5b, whose grid is below the automatic threshold)."""
+    monkeypatch.setenv("CIGPU_FP32_PRODUCT", "sigma")
+    meta, _ = load_golden("c4")
+    run_case(chk, integrals("c4"), A.FCI, A.MIXED, e_ref=meta["e0"])
