@@ -632,6 +632,7 @@ int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, boo
     P.mv64 = [cp](const double *x, double *y, cudaStream_t st) { crs_mv64(*cp, x, y, st); };
     if (crs.precision == CIGPU_MIXED)
         P.mv32 = [cp](const float *x, float *y, cudaStream_t st) { crs_mv32(*cp, x, y, st); };
+    P.fp32_first_anchor = crs.sig != nullptr;
     SolveOptions o;
     o.tol = tol;
     o.max_matvec = max_matvec;

@@ -947,10 +947,14 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
         dev_convert(ref.r.p, cr32.p + n, n, s);
     };
     // A cold start's first anchor only turns the start vector (residual of order
-    // |H|) into the first basis, so the FP32 product serves it; every later anchor,
-    // and so the residual the solve reports, is the exact FP64 one. A warm start
-    // may already be near the tolerance and takes the FP64 product at once.
-    anchor(!have_start);
+    // |H|) into the first basis, so the FP32 product can serve it where it is much
+    // cheaper than the FP64 one (FCI L=12 6a6b: 0.35 against 2.7 ms; one more FP32
+    // product per solve); every later anchor, and so the residual the solve reports,
+    // is the exact FP64 one. Where the two cost about the same (the DOCI pair hops:
+    // 1.1 against 1.7 ms) the FP32 anchor's error floor, relative to |E|, cost more
+    // FP32 steps than it saved (L=24 12 pairs: 24 + 2 against 21 + 3 products). A
+    // warm start may already be near the tolerance and takes the FP64 product.
+    anchor(!have_start && P.fp32_first_anchor);
     int k = 0;  // corrections in the basis
     double theta = E, a0 = 1.0, yv = 0;
     std::vector<double> y(kMaxBasis + 1, 0.0), yp(kMaxBasis + 1, 0.0), d(kMaxBasis + 1, 0.0);

@@ -27,6 +27,9 @@ struct SolveProblem {
     Matvec64 mv64;              // always present (FP64 matvec)
     Matvec32 mv32;              // mixed only
     const double *diag = nullptr;  // device, [n], H_ii (Davidson-type preconditioner)
+    // mixed cold starts: the first anchor from the FP32 product (worth it where that is
+    // several times cheaper than the FP64 one: the FCI sigma vector)
+    bool fp32_first_anchor = false;
     cudaStream_t stream = nullptr;
 };
 
