@@ -72,14 +72,14 @@ int dot_grid_for(int64_t n) {
 // the last block to finish reduces them into out[v], v < nvec, one warp per entry in
 // a fixed order (run-to-run reproducible), and resets the ticket for the next kernel
 // on the stream. Saves a separate reduction launch per dot product.
-__device__ __forceinline__ void reduce_in_last_block(const double *partial, int nvec, double *out,
+__device__ __forceinline__ bool reduce_in_last_block(const double *partial, int nvec, double *out,
                                                      unsigned *ticket) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x * gridDim.y - 1;
     __syncthreads();
-    if (!last) return;
+    if (!last) return false;
     __threadfence();
     const int G = gridDim.x, lane = threadIdx.x & 31;
     for (int v = threadIdx.x >> 5; v < nvec; v += blockDim.x >> 5) {
@@ -89,6 +89,7 @@ __device__ __forceinline__ void reduce_in_last_block(const double *partial, int 
         if (lane == 0) out[v] = s;
     }
     if (threadIdx.x == 0) *ticket = 0;
+    return true;
 }
 
 // The last of the gridDim.x blocks of one chunk (blockIdx.y) reduces the chunk's nv
@@ -133,7 +134,8 @@ template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__ V, int64_t ld, int nvec,
                                                           const WT *__restrict__ w, int64_t n,
                                                           double *__restrict__ partial, double *__restrict__ out,
-                                                          unsigned *__restrict__ tickets) {
+                                                          unsigned *__restrict__ tickets, const double *__restrict__ skip) {
+    if (skip && *skip != 0.0) return;  // a second orthogonalisation pass that the first made unnecessary
     static_assert(kDotChunk <= kVecThreads / 32, "one warp per vector of a chunk");
     const int G = gridDim.x;
     const int v0 = blockIdx.y * kDotChunk;
@@ -186,7 +188,9 @@ template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
                                                         const double *__restrict__ coef, WT *__restrict__ w, int64_t n,
                                                         double *__restrict__ nrm, double *__restrict__ nrm_out,
-                                                        unsigned *__restrict__ ticket) {
+                                                        unsigned *__restrict__ ticket, const double *__restrict__ skip,
+                                                        const double *__restrict__ gate_ref, double *__restrict__ gate_out) {
+    if (skip && *skip != 0.0) return;  // see k_multidot
     __shared__ AT c[kMaxBasis + 1];
     for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = (AT)coef[i];
     __syncthreads();
@@ -217,7 +221,10 @@ __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V
             for (int k = 0; k < kVecThreads / 32; ++k) s += sh[k];
             nrm[blockIdx.x] = s;
         }
-        reduce_in_last_block(nrm, 1, nrm_out, ticket);
+        // with a gate: 1 when the projection kept at least half of ||w||^2 (the
+        // DGKS test with eta = 1/sqrt 2), so that a second pass is not needed
+        if (reduce_in_last_block(nrm, 1, nrm_out, ticket) && gate_out && threadIdx.x == 0)
+            *gate_out = (*nrm_out >= 0.5 * *gate_ref) ? 1.0 : 0.0;
     }
 }
 
@@ -516,18 +523,26 @@ struct VecOps {
         pinned_put(h_out);
     }
     // out[dst .. dst+nvec) = V_i . w   (AT: arithmetic type of the products)
+    // skip_at >= 0: the kernel does nothing when out[skip_at] != 0
     template <typename VT, typename WT, typename AT = double>
-    void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst) {
+    void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst, int skip_at = -1) {
         dim3 grid(Gd, (nvec + kDotChunk - 1) / kDotChunk);
-        k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, out.p + dst, ticket.p);
+        k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, out.p + dst, ticket.p,
+                                                            skip_at >= 0 ? out.p + skip_at : nullptr);
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
     }
+    // skip_at >= 0: nothing when out[skip_at] != 0; gate_at >= 0 (with nrm_at):
+    // out[gate_at] = 1 when ||w||^2 after the update is at least half of out[ref_at]
     template <typename VT, typename WT, typename AT = double>
-    void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at) {
+    void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at, int skip_at = -1,
+                int ref_at = -1, int gate_at = -1) {
         k_update<VT, WT, AT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n,
                                                        nrm_at >= 0 ? partial.p : nullptr,
-                                                       nrm_at >= 0 ? out.p + nrm_at : nullptr, ticket.p);
+                                                       nrm_at >= 0 ? out.p + nrm_at : nullptr, ticket.p,
+                                                       skip_at >= 0 ? out.p + skip_at : nullptr,
+                                                       ref_at >= 0 ? out.p + ref_at : nullptr,
+                                                       gate_at >= 0 ? out.p + gate_at : nullptr);
         count_launch();
         CIGPU_CUDA(cudaGetLastError());
     }
@@ -961,7 +976,7 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
     int ky = -1, kp = -1;  // corrections behind y and yp (-1: not of the current basis)
     double a0p = 0;
     int kept = 0;
-    const int SLOT_R = 3 * (kMaxBasis + 1), SLOT_N = SLOT_R + 1;
+    const int SLOT_R = 3 * (kMaxBasis + 1), SLOT_N = SLOT_R + 1, SLOT_G = SLOT_R + 2;
     while (rho > o.tol && mv32 + mv64 < budget) {
         float *vnew = V.p + (size_t)(k + 1) * n;
         float *hvnew = HV.p + (size_t)(k + 1) * n;
@@ -976,11 +991,15 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
                                                             ops.out.p + SLOT_R, ops.ticket.p);
             count_launch();
         }
-        // orthonormalise against slots 0..k, twice (FP32 arithmetic, FP64 reductions)
-        ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0);
-        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, -1);
-        ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0);
-        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, SLOT_N);
+        // orthonormalise against slots 0..k (FP32 arithmetic, FP64 reductions): one
+        // classical Gram-Schmidt pass, and a second one only when the first removed
+        // more than half of ||t||^2 (DGKS, decided on the device: the second pass's
+        // kernels return at once otherwise). The first dots include t itself (slot
+        // k + 1), giving ||t||^2 in out[k + 1].
+        ops.dots<float, float, float>(V.p, n, k + 2, vnew, n, 0);
+        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, SLOT_N, -1, k + 1, SLOT_G);
+        ops.dots<float, float, float>(V.p, n, k + 1, vnew, n, 0, SLOT_G);
+        ops.update<float, float, float>(V.p, n, k + 1, 0, vnew, n, SLOT_N, SLOT_G);
         ops.scale(vnew, n, SLOT_N);
         P.mv32(vnew, hvnew, s);
         ++mv32;
