@@ -302,6 +302,23 @@ struct RowSingles {
     }
 };
 
+// Temporaries of the build passes, kept with the handle while a deferred pass runs.
+struct BuildTemps {
+    RowSingles singles;
+    DevBuf<uint32_t> count;
+    DevBuf<int64_t> urow, sums1, sums2;
+};
+
+void finish_deferred(cigpu_crs &c) {
+    if (!c.counts_pending) return;
+    CIGPU_CUDA(cudaEventSynchronize(c.side_done));
+    auto *t = static_cast<BuildTemps *>(c.side_keep.get());
+    CIGPU_CUDA(cudaMemcpy(&c.nnz_full, c.row_ptr.p + c.dim, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    CIGPU_CUDA(cudaMemcpy(&c.nnz_upper, t->urow.p + c.dim, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    c.side_keep.reset();
+    c.counts_pending = false;
+}
+
 // Explicit FP32 CRS (columns + hi values) of a values-only CRS, for export.
 // The explicit CRS (columns and values) of a matrix stored as slot tiles, made by
 // the CRS generator for export: FP32 hi/lo values for MIXED, FP64 for FP64.
@@ -369,8 +386,11 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
     cigpu_ham &h = *c.ham;
     const int64_t dim = c.dim;
     c.diag.alloc(dim);
-    DevBuf<uint32_t> count(dim);
-    RowSingles singles;  // FCI row singles (build only)
+    auto temps = std::make_shared<BuildTemps>();
+    temps->count.alloc(dim);
+    DevBuf<uint32_t> &count = temps->count;
+    RowSingles &singles = temps->singles;  // FCI row singles (build only)
+    cudaStream_t fs = s;                    // stream of the fill, staging tables and counts
     c.upper_off.alloc(dim);
     c.row_ptr.alloc(dim + 1);
     tr.mark("alloc small");
@@ -407,9 +427,21 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
                 c.sig.reset();
             tr.mark("sigma factors");
         }
+        if (c.sig) {
+            // the rest runs beside the solve's first Davidson cycle (see cigpu_crs::side);
+            // it starts after everything queued on s so far
+            CIGPU_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+            CIGPU_CUDA(cudaEventCreateWithFlags(&c.side_done, cudaEventDisableTiming));
+            cudaEvent_t ready = nullptr;
+            CIGPU_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+            CIGPU_CUDA(cudaEventRecord(ready, s));
+            CIGPU_CUDA(cudaStreamWaitEvent(c.side, ready, 0));
+            CIGPU_CUDA(cudaEventDestroy(ready));
+            fs = c.side;
+        }
         // FP32 splits only for a fill of FP32 values (not for the FP64 values of the
         // sigma-backed mixed form)
-        singles.make(c, p, s, c.precision == CIGPU_MIXED && !c.sig);
+        singles.make(c, p, fs, c.precision == CIGPU_MIXED && !c.sig);
         tr.mark("upload + diag + singles");
         p.row_count = count.p;
         p.upper_off = c.upper_off.p;
@@ -420,14 +452,14 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
             if (c.precision == CIGPU_MIXED && !c.sig) {
                 c.val32.alloc(slots_count(p));
                 c.val32lo.alloc(slots_count(p));
-                fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, s);
+                fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, fs);
             } else {
                 c.val64.alloc(slots_count(p));
-                fill_slots64_launch(p, c.val64.p, count.p, c.upper_off.p, s);
+                fill_slots64_launch(p, c.val64.p, count.p, c.upper_off.p, fs);
             }
             c.slot_desc.alloc(std::max<int64_t>(slot_desc_count(p), 1));
             c.slot_st.alloc(std::max<int64_t>(slot_st_count(p), 4));
-            slot_tables_launch(p, c.slot_desc.p, c.slot_st.p, s);
+            slot_tables_launch(p, c.slot_desc.p, c.slot_st.p, fs);
             p.desc_tab = c.slot_desc.p;
             p.st_tab = c.slot_st.p;
             tr.mark("slot fill");
@@ -489,6 +521,22 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         doci_launch(kCount, p, s);
         tr.mark("strings + diag + count");
     }
+    if (c.side) {
+        // deferred: the scans on the side stream, the counts read by finish_deferred
+        exclusive_scan_u32_async(count.p, c.row_ptr.p, dim, temps->sums1, fs);
+        temps->urow.alloc(dim + 1);
+        upper_counts_launch(dim, c.row_ptr.p, c.upper_off.p, count.p, fs);
+        exclusive_scan_u32_async(count.p, temps->urow.p, dim, temps->sums2, fs);
+        CIGPU_CUDA(cudaEventRecord(c.side_done, fs));
+        c.side_keep = temps;
+        c.counts_pending = true;
+        tr.mark("deferred passes queued");
+        CIGPU_CUDA(cudaStreamSynchronize(s));
+        c.fp.sgl64 = nullptr;
+        c.fp.sgl_hi = c.fp.sgl_lo = c.fp.diag_hi = c.fp.diag_lo = nullptr;
+        c.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
     exclusive_scan_u32(count.p, c.row_ptr.p, dim, s);
     CIGPU_CUDA(cudaMemcpyAsync(&c.nnz_full, c.row_ptr.p + dim, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     // upper-triangle size (the reference CRS)
@@ -546,6 +594,7 @@ void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
         return;
     }
     if (c.slots && c.val64.p) {  // FP64 slot values: the plain method, or MIXED with the sigma vector
+        if (c.side_done) CIGPU_CUDA(cudaStreamWaitEvent(s, c.side_done, 0));  // a deferred fill
         spmv_slots_f64(c.fp, c.val64.p, x, y, s);
         return;
     }
@@ -823,6 +872,11 @@ int cigpu_crs_destroy(cigpu_crs *crs) {
 
 int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full) {
     if (!crs) return CIGPU_EINVAL;
+    if (nnz_upper || nnz_full) {  // the counts of a deferred build pass (the handle's lazily read state)
+        CIGPU_TRY
+        finish_deferred(*const_cast<cigpu_crs *>(crs));
+        CIGPU_CATCH
+    }
     if (dim) *dim = crs->dim;
     if (nnz_upper) *nnz_upper = crs->nnz_upper;
     if (nnz_full) *nnz_full = crs->nnz_full;
@@ -852,8 +906,9 @@ int cigpu_crs_fp32_product(const cigpu_crs *crs, int *kind, int *rank, int *padd
 int cigpu_crs_export_upper(cigpu_crs *crs, uint32_t *row, uint32_t *col, double *val) {
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
     if (crs->onthefly) return CIGPU_ENOTSUP;
-    if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     CIGPU_TRY
+    finish_deferred(*crs);
+    if (crs->nnz_upper > (int64_t)UINT32_MAX) return CIGPU_ENOTSUP;
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
     const int64_t dim = crs->dim;
@@ -884,6 +939,7 @@ int cigpu_crs_export_full(cigpu_crs *crs, int64_t *row, uint32_t *col, double *v
     if (!crs || !row || !col || !val) return CIGPU_EINVAL;
     if (crs->onthefly) return CIGPU_ENOTSUP;
     CIGPU_TRY
+    finish_deferred(*crs);
     cudaStream_t s = crs->stream;
     StreamScope scope(s);
     ExplicitCrs ex;

@@ -687,18 +687,23 @@ __global__ void k_scan_apply(const uint32_t *in, int64_t n, const int64_t *tile_
 }
 }  // namespace
 
-void exclusive_scan_u32(const uint32_t *in, int64_t *out, int64_t n, cudaStream_t s) {
+void exclusive_scan_u32_async(const uint32_t *in, int64_t *out, int64_t n, DevBuf<int64_t> &sums, cudaStream_t s) {
     const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles == 0) {
         CIGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), s));
         return;
     }
-    DevBuf<int64_t> sums(ntiles);
+    sums.alloc(ntiles);
     k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, sums.p);
     k_scan_sums<<<1, 1024, 0, s>>>(sums.p, ntiles);
     k_scan_apply<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, sums.p, out);
     CIGPU_CUDA(cudaGetLastError());
     count_launch(3);
+}
+
+void exclusive_scan_u32(const uint32_t *in, int64_t *out, int64_t n, cudaStream_t s) {
+    DevBuf<int64_t> sums;
+    exclusive_scan_u32_async(in, out, n, sums, s);
     // keep `sums` alive until the kernels finish
     CIGPU_CUDA(cudaStreamSynchronize(s));
 }

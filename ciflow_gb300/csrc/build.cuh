@@ -123,6 +123,8 @@ void extract_upper_launch(int64_t dim, const int64_t *row_ptr, const uint32_t *u
                           cudaStream_t s);
 // out[0] = 0, out[i+1] = in[0] + ... + in[i]; out has n+1 entries.
 void exclusive_scan_u32(const uint32_t *in, int64_t *out, int64_t n, cudaStream_t s);
+// The same without waiting: the caller keeps `sums` (the tile sums) alive until s has run it.
+void exclusive_scan_u32_async(const uint32_t *in, int64_t *out, int64_t n, DevBuf<int64_t> &sums, cudaStream_t s);
 int sm_count();
 
 }  // namespace cigpu

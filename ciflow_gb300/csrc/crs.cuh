@@ -59,8 +59,23 @@ struct cigpu_crs {
     cigpu::DevBuf<uint64_t> dets;   // [dim][2 * det_words]: up words, then down words
     double build_seconds = 0;
     std::shared_ptr<cigpu::FciRdmPlan> rdm_plan;  // FCI RDM plan, made by the first RDM call
+    // A sigma-backed mixed FCI build leaves its FP64 fill, the slot staging tables
+    // and the row counts running on `side`: the first Davidson cycle needs only the
+    // string tables and the sigma factors. The FP64 products wait for side_done on
+    // the device; the row counts are read, and the passes' temporaries released, by
+    // the first call that needs them (finish_deferred).
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_done = nullptr;
+    bool counts_pending = false;
+    std::shared_ptr<void> side_keep;
 
     ~cigpu_crs() {
+        if (side) {
+            cudaStreamSynchronize(side);
+            side_keep.reset();
+            cudaStreamDestroy(side);
+        }
+        if (side_done) cudaEventDestroy(side_done);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -71,6 +86,8 @@ namespace cigpu {
 int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool fp64_tiles, cigpu_crs **out);
 // Builds the CRS for `ham` on stream `s` (throws on failure).
 void build_crs(cigpu_crs &c, cudaStream_t s);
+// Waits for a deferred build pass and reads its row counts (no-op otherwise).
+void finish_deferred(cigpu_crs &c);
 // FP64 product y = H x on the CRS stream (device pointers).
 void crs_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s);
 // FP32 product (MIXED CRS only).
