@@ -559,6 +559,8 @@ def run_cigpu(args, rank: int, world: int, dist):
             roof[tag] = {"bound": "fp32", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s", "frac": ach / peak_tf,
                          "traffic": ncu_traffic(f"sigma_fp32_{shape}"), "algorithmic_flops": w["flops"],
                          "l2_bytes_per_launch": w["l2_bytes"], "l2_gbs": w["l2_bytes"] / t / 1e9,
+                         "l2_note": "the factor vectors the kernels read per excitation live in L2 (about half of "
+                                    "those reads hit L1); ncu: L2 27% busy, issue 46-50% at L=11",
                          "layout": f"sigma-fp32 (rank {kind[1]}, padded {kind[2]})",
                          "kernels": "k_transpose32 + k_sigma_a + k_sigma_b", "ms_per_launch": t * 1000,
                          "nnz_full": nf.value,
