@@ -423,7 +423,7 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
         if (c.slots && c.precision == CIGPU_MIXED && c.allow_compact && sigma_applies(c.L) && smode != kSigmaOff) {
             c.sig.reset(new SigmaOp);
             if (!sigma_prepare(*c.sig, c.L, h.h.data(), h.eri.data(), c.ta, c.ndown == c.nup ? c.ta : c.tb,
-                               smode == kSigmaForced, s))
+                               smode == kSigmaForced || c.sigma_any_grid, s))
                 c.sig.reset();
             tr.mark("sigma factors");
         }
@@ -820,7 +820,8 @@ int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, 
 }  // extern "C"
 
 namespace cigpu {
-int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool compact, cigpu_crs **out) {
+int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool compact, cigpu_crs **out,
+                 bool sigma_any_grid) {
     if (!ham || !out) return CIGPU_EINVAL;
     *out = nullptr;
     if (method != CIGPU_FCI && method != CIGPU_DOCI) return CIGPU_EINVAL;
@@ -840,6 +841,7 @@ int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream,
     c->ndown = ham->ndown;
     c->dim = dim;
     c->allow_compact = compact;
+    c->sigma_any_grid = sigma_any_grid;
     if (stream) {
         c->stream = static_cast<cudaStream_t>(stream);
     } else {

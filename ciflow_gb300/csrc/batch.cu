@@ -786,7 +786,8 @@ extern "C" int cigpu_solve_batch(int count, const cigpu_request *req, int64_t ma
                     cigpu_ham_destroy(it.ham);
                     it.ham = rotated;
                 }
-                if (stc == CIGPU_OK) stc = cigpu_build(it.ham, q.method, q.precision, s, &it.crs);
+                // concurrent workers: the sigma FP32 product on any grid (as the server)
+                if (stc == CIGPU_OK) stc = build_handle(it.ham, q.method, q.precision, s, true, &it.crs, true);
                 if (stc == CIGPU_OK) {
                     cigpu_solve_info in{};
                     stc = cigpu_solve(it.crs, q.tol, 0, q.c0, nullptr, &in);

@@ -39,6 +39,10 @@ struct cigpu_crs {
     // compact layouts allowed: FP64 slot tiles for FP64 FCI, the matrix-free pair-hop
     // form for DOCI (the lockstep batch concatenates explicit CRS matrices)
     bool allow_compact = true;
+    // MIXED FCI: take the sigma FP32 product on any grid (builds whose solves run
+    // beside others, as in the server and the batch, where GPU work per product
+    // counts rather than one solve's latency)
+    bool sigma_any_grid = false;
     // DOCI without a stored matrix: the matvecs generate the pair hops (doci_mv.cu)
     // from the strings and K_jk; row_ptr / upper_off are filled on demand (export)
     bool pairs = false;
@@ -83,7 +87,8 @@ struct cigpu_crs {
 namespace cigpu {
 // cigpu_build with a choice of layout: fp64_tiles = false keeps an FP64 FCI matrix
 // as a CRS (the lockstep batch concatenates CRS matrices).
-int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool fp64_tiles, cigpu_crs **out);
+int build_handle(cigpu_ham *ham, int method, int precision, cigpu_stream stream, bool fp64_tiles, cigpu_crs **out,
+                 bool sigma_any_grid = false);
 // Builds the CRS for `ham` on stream `s` (throws on failure).
 void build_crs(cigpu_crs &c, cudaStream_t s);
 // Waits for a deferred build pass and reads its row counts (no-op otherwise).

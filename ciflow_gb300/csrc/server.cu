@@ -129,7 +129,10 @@ struct cigpu_server {
             cigpu_ham_destroy(ham);
             ham = rotated;
         }
-        if (st == CIGPU_OK) st = cigpu_build(ham, q.r.method, q.r.precision, s, &crs);
+        // several requests run at once: the sigma FP32 product on any grid (half the
+        // GPU work of the stored values' product on L=10 5a5b, where one solve alone
+        // is faster with the stored values)
+        if (st == CIGPU_OK) st = cigpu::build_handle(ham, q.r.method, q.r.precision, s, true, &crs, true);
         bool cancelled;
         {
             std::lock_guard<std::mutex> lock(mu);
