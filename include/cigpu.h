@@ -120,9 +120,15 @@ int cigpu_unitary_exp(int L, const double *X, double *U);
  * (CIMethod.cpp:489-561, 749-888, 611-660) filling SparseMatrix_CRS_Sym.
  * The device keeps the full symmetric matrix (both triangles, columns ascending);
  * its upper triangle is CIFlow's CRS exactly (same 1e-14 drop threshold).
- * The ham handle is borrowed and must outlive the CRS. ---- */
+ * The ham handle is borrowed and must outlive the CRS. A MIXED FCI build whose
+ * FP32 products come from the sigma operator (cigpu_crs_fp32_product) returns
+ * before its FP64 values and row counts are complete: they are made on the
+ * handle's own side stream while a solve starts, the FP64 products wait for them
+ * on the device, and cigpu_crs_dims (when asked for the nonzero counts), the
+ * exports and cigpu_crs_destroy wait for them on the host. ---- */
 int cigpu_build(cigpu_ham *ham, int method, int precision, cigpu_stream stream, cigpu_crs **out);
 int cigpu_crs_destroy(cigpu_crs *crs);
+/* dim only: no wait; nnz_upper / nnz_full: after the build's deferred part. */
 int cigpu_crs_dims(const cigpu_crs *crs, int64_t *dim, int64_t *nnz_upper, int64_t *nnz_full);
 /* Device storage of the matrix (no reference counterpart; reported with matvec
  * measurements). CIGPU_LAYOUT_CRS: full symmetric CRS, stored = nnz_full values
