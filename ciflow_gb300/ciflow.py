@@ -166,12 +166,28 @@ class SparseMatrix_CRS_Sym:
     def __init__(self, handle, ham: Hamiltonian):
         self._h = handle
         self._ham = ham  # the device Hamiltonian must outlive the CRS
-        dim, nu, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        A.check(A.lib().cigpu_crs_dims(handle.value, ctypes.byref(dim), ctypes.byref(nu), ctypes.byref(nf)))
+        dim = ctypes.c_int64()
+        # the dimension only: the nonzero counts of a build whose last part runs
+        # beside the first solve are read when first asked for (nnz_upper, nnz_full)
+        A.check(A.lib().cigpu_crs_dims(handle.value, ctypes.byref(dim), None, None))
         self.n = dim.value
-        self.nnz_upper = nu.value
-        self.nnz_full = nf.value
+        self._counts = None
         self._upper = None
+
+    def _nnz(self) -> tuple[int, int]:
+        if self._counts is None:
+            nu, nf = ctypes.c_int64(), ctypes.c_int64()
+            A.check(A.lib().cigpu_crs_dims(self._h.value, None, ctypes.byref(nu), ctypes.byref(nf)))
+            self._counts = (nu.value, nf.value)
+        return self._counts
+
+    @property
+    def nnz_upper(self) -> int:
+        return self._nnz()[0]
+
+    @property
+    def nnz_full(self) -> int:
+        return self._nnz()[1]
 
     @property
     def handle(self):

@@ -95,6 +95,32 @@ def test_mixed_build_same_pattern_fp32_values():
     np.testing.assert_array_equal(v64.astype(np.float32).astype(np.float64), v32)
 
 
+@pytest.mark.parametrize("case", ["c0", "c4"])
+def test_sigma_backed_mixed_build_defers_and_exports_the_same(case, monkeypatch):
+    """A mixed build whose FP32 products come from the sigma operator stores FP64
+    slot values and finishes its fill and row counts on a side stream: its counts
+    and exported matrix equal those of the mixed build from stored FP32 values, and
+    its FP64 product (which waits for the fill) equals the plain build's."""
+    import ctypes
+
+    ints = integrals(case)
+    monkeypatch.setenv("CIGPU_FP32_PRODUCT", "slots")
+    ref = build(FCI, ints, precision=A.MIXED).get_mat()
+    monkeypatch.setenv("CIGPU_FP32_PRODUCT", "sigma")
+    cim = build(FCI, ints, precision=A.MIXED)
+    m = cim.get_mat()
+    kind = ctypes.c_int()
+    A.check(A.lib().cigpu_crs_fp32_product(m.handle, ctypes.byref(kind), None, None))
+    assert kind.value == A.FP32_SIGMA
+    x = np.random.default_rng(4).standard_normal(m.n)
+    y = m.mvprod(x)  # FP64 product right after the build: waits for the deferred fill on the device
+    y_ref = build(FCI, ints).get_mat().mvprod(x)
+    assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+    assert (m.nnz_upper, m.nnz_full) == (ref.nnz_upper, ref.nnz_full)
+    for a, b in zip(m.full(), ref.full()):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_symmetry_zeros_dropped_like_reference():
     # BeH2 in D2h: many elements are exactly zero and must be dropped (|v| <= 1e-14)
     ints, meta, _ = beh2_integrals()
