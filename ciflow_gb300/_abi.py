@@ -117,6 +117,7 @@ SIGNATURES = {
     "cigpu_solve_batch": (_I, [_I, _P, _I64, _P, _P, _P, _P]),
     "cigpu_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
     "cigpu_build_dets": (_I, [_P, _I64, _I, _P, _P, _I, _I, _P, _P]),
+    "cigpu_build_dets_partial": (_I, [_P, _I64, _I, _P, _P, _I64, _P, _P]),
     "cigpu_dets_read": (_I, [ctypes.c_char_p, _I, _I64, _P, _P, _P, _P]),
     "cigpu_ham_read_psi4": (_I, [ctypes.c_char_p, _P, _P, _P, _P, _P, _P, _P, _P]),
     "cigpu_ham_write_psi4": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P, _D]),

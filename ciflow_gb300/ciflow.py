@@ -442,12 +442,37 @@ class FCI_File(CIMethod):
         return DensFILE(self)
 
 
+def ci_big_lines(cisize_gb: float) -> int:
+    """The determinants whose block of the matrix CI_Big keeps for a CISIZE memory
+    budget in GB: numelements = CISIZE 2^30 3 / (64 5) 10 / 2, numlines =
+    round((-1 + sqrt(1 + 8 numelements)) / 2) (CI_Big::CI_Big, CIMethod.cpp:596-598)."""
+    import math
+    numelements = int(cisize_gb * 1024.0 * 1024.0 * 1024.0 * 3 / (64.0 * 5) * 10.0 / 2.0)
+    return int(round((-1 + math.sqrt(1 + 8 * numelements)) / 2))
+
+
 class CI_Big(FCI_File):
-    """CI_Big (CIMethod.h:176-189): the determinant list without a stored matrix; every
-    matvec recomputes the elements (FP64)."""
+    """CI_Big (CIMethod.h:176-189): the determinant list with the block of the matrix
+    among its first ``keep`` determinants stored and every other element recomputed
+    in each matvec (FP64). ``keep`` defaults to none; ``cisize_gb`` sizes it as the
+    reference does from its CISIZE budget (ci_big_lines)."""
 
     name = "CI_Big"
     storage = A.DETS_ONTHEFLY
+
+    def __init__(self, ham: Hamiltonian, permfile: str | None = None, precision: int = A.FP64,
+                 up: np.ndarray | None = None, down: np.ndarray | None = None, words: int | None = None,
+                 build: bool = True, keep: int | None = None, cisize_gb: float | None = None):
+        self.keep = keep if keep is not None else (ci_big_lines(cisize_gb) if cisize_gb is not None else 0)
+        super().__init__(ham, permfile, precision, up, down, words, build)
+
+    def build_ci(self) -> None:
+        out = ctypes.c_void_p()
+        keep = max(0, min(self.keep, self._dim()))
+        A.check(A.lib().cigpu_build_dets_partial(self._ham.device(), self._dim(), self.words, A.ptr(self.up),
+                                                 A.ptr(self.down), keep, None, ctypes.byref(out)),
+                "cigpu_build_dets_partial")
+        self._mat = SparseMatrix_CRS_Sym(_Handle(out.value, A.lib().cigpu_crs_destroy), self._ham)
 
 
 class CIDens:

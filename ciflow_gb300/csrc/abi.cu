@@ -892,7 +892,11 @@ int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
                   : crs->pairs  ? CIGPU_LAYOUT_PAIRS
                   : crs->slots  ? CIGPU_LAYOUT_SLOTS
                                 : CIGPU_LAYOUT_CRS;
-    if (stored) *stored = (crs->onthefly || crs->pairs) ? 0 : crs->slots ? slots_count(crs->fp) : crs->nnz_full;
+    if (stored)
+        *stored = crs->pairs                           ? 0
+                  : crs->onthefly                      ? (crs->det_block > 0 ? crs->nnz_full : 0)
+                  : crs->slots                         ? slots_count(crs->fp)
+                                                       : crs->nnz_full;
     return CIGPU_OK;
 }
 

@@ -59,7 +59,8 @@ struct cigpu_crs {
     cigpu::DociParams dp{};
     // determinant lists (FCI_File / CI_Big)
     int det_words = 0;              // 64-bit words per spin string: 1 (L <= 64) or 2 (L <= 128)
-    bool onthefly = false;          // CI_Big: no stored matrix, elements recomputed in every matvec
+    bool onthefly = false;          // CI_Big: elements recomputed in every matvec, outside a stored leading block
+    int64_t det_block = 0;          // CI_Big: leading determinants whose block is stored (row_ptr / col / val64)
     cigpu::DevBuf<uint64_t> dets;   // [dim][2 * det_words]: up words, then down words
     double build_seconds = 0;
     std::shared_ptr<cigpu::FciRdmPlan> rdm_plan;  // FCI RDM plan, made by the first RDM call

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "crs.cuh"
+#include "spmv.cuh"
 
 namespace cigpu {
 
@@ -45,6 +46,10 @@ enum DetMode : int { kDetCount = 0, kDetFill64 = 1, kDetFill32 = 2, kDetMatvec =
 struct DetParams {
     int L, nup, ndown;
     int64_t n;
+    // rows the pass visits (count / fill: the stored rows; matvec: all n) and the
+    // stored block: count / fill take columns below `block` (n for a whole CRS); the
+    // matvec takes the pairs outside the block (row i < block: columns >= block)
+    int64_t nrows = 0, block = 0;
     const uint64_t *dets;  // [n][2W]
     const double *eri;     // chemist (pq|rs), L^4
     const double *h;       // L^2
@@ -273,15 +278,23 @@ __global__ void k_dets_diag(DetParams p, double *diag) {
     }
 }
 
-template <int W, int MODE>
+// RANGED: a stored block smaller than the list (CI_Big with a kept part), whose
+// passes skip columns outside their range; the whole-list passes carry no test.
+template <int W, int MODE, bool RANGED>
 __global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const double *__restrict__ x,
                                                               double *__restrict__ y) {
     __shared__ uint64_t tile[kDetTile * 2 * W];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    for (int64_t r0 = (int64_t)blockIdx.x * kDetWarps; r0 < p.n; r0 += (int64_t)gridDim.x * kDetWarps) {
+    constexpr bool kStoring = MODE != kDetMatvec;
+    for (int64_t r0 = (int64_t)blockIdx.x * kDetWarps; r0 < p.nrows; r0 += (int64_t)gridDim.x * kDetWarps) {
         const int64_t i = r0 + warp;
-        const bool active = i < p.n;
+        const bool active = i < p.nrows;
+        // this row's columns [cs, ce): a stored pass takes those of the block; the
+        // matvec of a partly stored matrix takes those outside it
+        const int64_t cs = (RANGED && !kStoring && i < p.block) ? p.block : 0, ce = kStoring ? p.block : p.n;
+        // the warps' common start (rows of one pass below the block skip it together)
+        const int64_t cs_all = (RANGED && !kStoring && r0 + kDetWarps <= p.block) ? p.block : 0;
         uint64_t ui[W], di[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
@@ -291,8 +304,9 @@ __global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const
         uint32_t cnt = 0, lower = 0;
         int64_t out = (MODE == kDetFill64 || MODE == kDetFill32) && active ? p.row_ptr[i] : 0;
         double acc = 0;
-        for (int64_t base = 0; base < p.n; base += kDetTile) {
-            const int tn = (int)(p.n - base < kDetTile ? p.n - base : kDetTile);
+        const int64_t cend = kStoring ? p.block : p.n;  // the same for every row of the pass
+        for (int64_t base = cs_all; base < cend; base += kDetTile) {
+            const int tn = (int)(cend - base < kDetTile ? cend - base : kDetTile);
             __syncthreads();
             for (int t = threadIdx.x; t < tn * 2 * W; t += blockDim.x) tile[t] = p.dets[base * 2 * W + t];
             __syncthreads();
@@ -302,7 +316,7 @@ __global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const
                 const int64_t j = base + jj;
                 double v = 0;
                 bool keep = false;
-                if (jj < tn) {
+                if (jj < tn && (!RANGED || (j >= cs && j < ce))) {
                     const uint64_t *uj = tile + jj * 2 * W, *dj = uj + W;
                     int nu = 0, nd = 0;
 #pragma unroll
@@ -348,7 +362,8 @@ __global__ void __launch_bounds__(32 * kDetWarps) k_dets_rows(DetParams p, const
             }
         } else if (MODE == kDetMatvec) {
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) y[i] = acc;
+            // rows of the stored block add to the stored block's product, already in y
+            if (lane == 0) y[i] = ((RANGED && i < p.block) ? y[i] : 0.0) + acc;
         }
     }
 }
@@ -367,7 +382,13 @@ int rows_grid(int64_t n) {
 
 template <int W, int MODE>
 void launch_rows(const DetParams &p, const double *x, double *y, cudaStream_t s) {
-    k_dets_rows<W, MODE><<<rows_grid(p.n), 32 * kDetWarps, 0, s>>>(p, x, y);
+    if (p.nrows == 0) return;
+    // the matvec of a partly stored list, or the stored passes of a block smaller than it
+    const bool ranged = MODE == kDetMatvec ? (p.block > 0 && p.block < p.n) : p.block < p.n;
+    if (ranged)
+        k_dets_rows<W, MODE, true><<<rows_grid(p.nrows), 32 * kDetWarps, 0, s>>>(p, x, y);
+    else
+        k_dets_rows<W, MODE, false><<<rows_grid(p.nrows), 32 * kDetWarps, 0, s>>>(p, x, y);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -390,6 +411,8 @@ DetParams params_of(const cigpu_crs &c) {
     p.eri = c.ham->d_eri.p;
     p.h = c.ham->d_h.p;
     p.diag = c.diag.p;
+    p.nrows = c.dim;
+    p.block = c.onthefly ? c.det_block : c.dim;
     return p;
 }
 
@@ -689,7 +712,10 @@ void dets_rdm(cigpu_crs &c, const double *c_dev, double *rdm1, double *aa, doubl
 
 void dets_mv64(cigpu_crs &c, const double *x, double *y, cudaStream_t s) {
     DetParams p = params_of(c);
-    rows<kDetMatvec>(p, c.det_words, x, y, s);
+    // the stored leading block first (rows and columns below det_block), then every
+    // pair outside it recomputed (CI_Big::mvprod, CIMethod.cpp:943-984)
+    if (c.det_block > 0) spmv_f64(c.det_block, c.nnz_full, c.row_ptr.p, c.col.p, c.val64.p, x, y, s);
+    if (c.det_block < c.dim) rows<kDetMatvec>(p, c.det_words, x, y, s);  // nothing outside a whole-list block
 }
 
 }  // namespace cigpu
@@ -726,14 +752,22 @@ int cigpu_dets_read(const char *path, int words, int64_t capacity, uint64_t *up,
     return (up && down && n > capacity) ? CIGPU_ENOMEM : CIGPU_OK;
 }
 
-int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
-                     int precision, cigpu_stream stream, cigpu_crs **out) {
+}  // extern "C"
+
+namespace cigpu {
+namespace {
+
+// keep: the leading determinants whose block of the matrix is stored (all of them
+// for CRS storage; 0 for CI_Big without a stored part)
+int build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
+               int precision, int64_t keep, cigpu_stream stream, cigpu_crs **out) {
     if (!ham || !up || !down || !out) return CIGPU_EINVAL;
     *out = nullptr;
     if (ndet < 1 || ndet > (int64_t)UINT32_MAX || (words != 1 && words != 2)) return CIGPU_EINVAL;
     if (storage != CIGPU_DETS_CRS && storage != CIGPU_DETS_ONTHEFLY) return CIGPU_EINVAL;
     if (precision != CIGPU_FP64 && precision != CIGPU_MIXED) return CIGPU_EINVAL;
     if (storage == CIGPU_DETS_ONTHEFLY && precision != CIGPU_FP64) return CIGPU_ENOTSUP;
+    if (keep < 0 || keep > ndet) return CIGPU_EINVAL;
     const int W = ham->L <= 64 ? 1 : 2;
     if (words < W) return CIGPU_EINVAL;
     // every determinant: nup / ndown electrons inside the L orbitals (the reference
@@ -766,6 +800,7 @@ int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up
     c->dim = ndet;
     c->det_words = W;
     c->onthefly = storage == CIGPU_DETS_ONTHEFLY;
+    c->det_block = c->onthefly ? keep : ndet;
     CIGPU_CUDA(cudaGetDevice(&c->device));
     if (stream) {
         c->stream = static_cast<cudaStream_t>(stream);
@@ -789,22 +824,26 @@ int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
     }
-    if (!c->onthefly) {
-        DevBuf<uint32_t> count(ndet);
-        c->upper_off.alloc(ndet);
-        c->row_ptr.alloc(ndet + 1);
+    if (c->det_block > 0) {
+        // the stored rows: the whole matrix (CRS storage) or the leading block of CI_Big
+        const int64_t nb = c->det_block;
+        p.nrows = nb;
+        p.block = nb;
+        DevBuf<uint32_t> count(nb);
+        c->upper_off.alloc(nb);
+        c->row_ptr.alloc(nb + 1);
         p.row_count = count.p;
         p.upper_off = c->upper_off.p;
         rows<kDetCount>(p, W, nullptr, nullptr, s);
-        exclusive_scan_u32(count.p, c->row_ptr.p, ndet, s);
+        exclusive_scan_u32(count.p, c->row_ptr.p, nb, s);
         DevBuf<unsigned long long> lower(1);
         CIGPU_CUDA(cudaMemsetAsync(lower.p, 0, sizeof(unsigned long long), s));
-        k_sum_u32<<<(int)std::min<int64_t>((ndet + 255) / 256, 1024), 256, 0, s>>>(c->upper_off.p, ndet, lower.p);
+        k_sum_u32<<<(int)std::min<int64_t>((nb + 255) / 256, 1024), 256, 0, s>>>(c->upper_off.p, nb, lower.p);
         CIGPU_CUDA(cudaGetLastError());
         count_launch();
         int64_t nnz = 0;
         unsigned long long nlow = 0;
-        CIGPU_CUDA(cudaMemcpyAsync(&nnz, c->row_ptr.p + ndet, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        CIGPU_CUDA(cudaMemcpyAsync(&nnz, c->row_ptr.p + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaMemcpyAsync(&nlow, lower.p, sizeof(nlow), cudaMemcpyDeviceToHost, s));
         CIGPU_CUDA(cudaStreamSynchronize(s));
         c->nnz_full = nnz;
@@ -829,6 +868,22 @@ int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up
     *out = c.release();
     return CIGPU_OK;
     CIGPU_CATCH
+}
+
+}  // namespace
+}  // namespace cigpu
+
+extern "C" {
+
+int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
+                     int precision, cigpu_stream stream, cigpu_crs **out) {
+    return build_dets(ham, ndet, words, up, down, storage, precision, storage == CIGPU_DETS_CRS ? ndet : 0, stream,
+                      out);
+}
+
+int cigpu_build_dets_partial(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down,
+                             int64_t keep, cigpu_stream stream, cigpu_crs **out) {
+    return build_dets(ham, ndet, words, up, down, CIGPU_DETS_ONTHEFLY, CIGPU_FP64, keep, stream, out);
 }
 
 }  // extern "C"

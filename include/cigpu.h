@@ -289,6 +289,15 @@ int cigpu_solve_batch(int count, const cigpu_request *req, int64_t max_batched_d
 enum { CIGPU_DETS_CRS = 0, CIGPU_DETS_ONTHEFLY = 1 };
 int cigpu_build_dets(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down, int storage,
                      int precision, cigpu_stream stream, cigpu_crs **out);
+/* CI_Big with its stored part (CI_Big::CI_Big and CI_Big::mvprod, CIMethod.cpp:591-609,
+ * 943-984): the block of the matrix among the first `keep` determinants of the list
+ * (0 <= keep <= ndet) is stored as a CRS; every matvec multiplies it and recomputes
+ * each element outside it (rows or columns at or past `keep`). FP64 only. The
+ * reference sizes keep from its CISIZE memory budget (numlines, CIMethod.cpp:596-598);
+ * keep = 0 is CIGPU_DETS_ONTHEFLY, keep = ndet stores everything. cigpu_crs_dims
+ * and cigpu_crs_layout report the stored block's elements. */
+int cigpu_build_dets_partial(cigpu_ham *ham, int64_t ndet, int words, const uint64_t *up, const uint64_t *down,
+                             int64_t keep, cigpu_stream stream, cigpu_crs **out);
 /* Permutator_File::read_file (Permutator.cpp:179-224): a determinant file with one
  * "<up>|<down>" line per determinant (binary strings, orbital 0 rightmost; lines
  * holding '#' are skipped). Call with up/down NULL to count: *ndet = number of

@@ -88,6 +88,34 @@ def test_onthefly_matches_stored(tag):
     assert fly.get_ci_energy() == pytest.approx(meta["e0_oracle"], abs=1e-9)
 
 
+@pytest.mark.parametrize("tag", ["beh2", "be70"])
+@pytest.mark.parametrize("frac", [0.0, 0.3, 0.77, 1.0])
+def test_ci_big_stored_block_matches_stored(tag, frac):
+    """CI_Big with the block of its first `keep` determinants stored (CI_Big::mvprod,
+    CIMethod.cpp:943-984): the matvec (stored block + every other element recomputed)
+    equals the fully stored matrix's for keep = 0, a part of the list and all of it,
+    the stored element count is the block's, and the energy is the known one."""
+    ints, up, down, words, meta = dets_case(tag)
+    ham = Hamiltonian.from_integrals(ints)
+    n = meta["dim"]
+    keep = int(round(frac * n))
+    stored = FCI_File(ham, up=up, down=down, words=words)
+    big = CI_Big(ham, up=up, down=down, words=words, keep=keep)
+    layout, stored_n = ctypes.c_int(), ctypes.c_int64()
+    A.check(A.lib().cigpu_crs_layout(big.get_mat().handle, ctypes.byref(layout), ctypes.byref(stored_n)))
+    assert layout.value == A.LAYOUT_ONTHEFLY
+    # the block's elements: those of the stored matrix with row and column below keep
+    r, c, _ = stored.get_mat().full()
+    rows = np.repeat(np.arange(n), np.diff(r.astype(np.int64)))
+    assert stored_n.value == int(np.count_nonzero((rows < keep) & (c < keep)))
+    x = np.random.default_rng(2).standard_normal(n)
+    y1, y2 = stored.get_mat().mvprod(x), big.get_mat().mvprod(x)
+    assert np.max(np.abs(y1 - y2)) <= 1e-12 * np.max(np.abs(y1))
+    if frac in (0.3, 0.77):
+        big.solve(tol=1e-10)
+        assert big.get_ci_energy() == pytest.approx(meta["e0_oracle"], abs=1e-9)
+
+
 def test_dets_rejections():
     ints, up, down, words, meta = dets_case("beh2")
     ham = Hamiltonian.from_integrals(ints)
