@@ -673,6 +673,7 @@ int validate_integrals(int L, const double *h, const double *eri, bool *exact_ou
 int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, bool have_start, cigpu_solve_info &info,
               cudaStream_t stream) {
     cudaStream_t s = stream ? stream : crs.stream;
+    Trace tr("solve", s);  // an NVTX range around the eigensolve
     cigpu_crs *cp = &crs;
     SolveProblem P;
     P.n = crs.dim;
