@@ -691,6 +691,15 @@ int solve_crs(cigpu_crs &crs, double tol, int64_t max_matvec, double *c_dev, boo
                                                 : solve_fp64(P, o, c_dev, have_start, info);
     info.e0 += crs.ham->econst;
     info.precision = crs.precision;
+    // a deferred build part that has completed by now: read its counts and release
+    // its temporaries (the FP64 row singles among them) without waiting
+    if (crs.counts_pending) {
+        const cudaError_t q = cudaEventQuery(crs.side_done);
+        if (q == cudaSuccess)
+            finish_deferred(crs);
+        else if (cudaPeekAtLastError() == q)
+            cudaGetLastError();  // "not ready" is not an error here
+    }
     return st;
 }
 
