@@ -28,6 +28,7 @@
 
 #include "lanczos.cuh"
 #include "small_eigh.h"
+#include <type_traits>
 
 namespace cigpu {
 
@@ -183,6 +184,105 @@ __global__ void __launch_bounds__(kVecThreads) k_multidot(const VT *__restrict__
     reduce_chunk_in_last_block(partial + (int64_t)v0 * G, nv, out + v0, tickets + blockIdx.y);
 }
 
+// The FP32 dots of k_multidot<float, float, float> with 16-byte loads: V rows and w
+// as float4 (a length divisible by 4, rows 16-byte aligned), four elements per
+// thread and step (at most 64 registers: the grid is four blocks per SM).
+__global__ void __launch_bounds__(kVecThreads, 4) k_multidot_f4(const float4 *__restrict__ V, int64_t ld4, int nvec,
+                                                             const float4 *__restrict__ w, int64_t n4,
+                                                             double *__restrict__ partial, double *__restrict__ out,
+                                                             unsigned *__restrict__ tickets,
+                                                             const double *__restrict__ skip) {
+    if (skip && *skip != 0.0) return;  // a second orthogonalisation pass that the first made unnecessary
+    const int G = gridDim.x;
+    const int v0 = blockIdx.y * kDotChunk;
+    const int nv = min(kDotChunk, nvec - v0);
+    float acc[kDotChunk];
+#pragma unroll
+    for (int i = 0; i < kDotChunk; ++i) acc[i] = 0.f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n4; r += (int64_t)gridDim.x * blockDim.x) {
+        const float4 wr = w[r];
+        float4 va[kDotChunk];
+#pragma unroll
+        for (int i = 0; i < kDotChunk; ++i)
+            if (i < nv) va[i] = V[(int64_t)(v0 + i) * ld4 + r];
+#pragma unroll
+        for (int i = 0; i < kDotChunk; ++i)
+            if (i < nv) acc[i] += (va[i].x * wr.x + va[i].y * wr.y) + (va[i].z * wr.z + va[i].w * wr.w);
+    }
+    __shared__ double sh[kDotChunk][kVecThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < kDotChunk; ++i) {
+        float a = acc[i];  // warp tree in FP32, block and grid sums in FP64
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[i][warp] = (double)a;
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double t = 0;
+        for (int k = 0; k < kVecThreads / 32; ++k) t += sh[threadIdx.x][k];
+        partial[(int64_t)(v0 + threadIdx.x) * G + blockIdx.x] = t;
+    }
+    reduce_chunk_in_last_block(partial + (int64_t)v0 * G, nv, out + v0, tickets + blockIdx.y);
+}
+
+// k_update<float, float, float> with 16-byte loads (the same per-element order of
+// subtractions; see k_multidot_f4 for the shapes).
+__global__ void __launch_bounds__(kVecThreads) k_update_f4(const float4 *__restrict__ V, int64_t ld4, int nvec,
+                                                           const double *__restrict__ coef, float4 *__restrict__ w,
+                                                           int64_t n4, double *__restrict__ nrm,
+                                                           double *__restrict__ nrm_out, unsigned *__restrict__ ticket,
+                                                           const double *__restrict__ skip,
+                                                           const double *__restrict__ gate_ref,
+                                                           double *__restrict__ gate_out) {
+    if (skip && *skip != 0.0) return;
+    __shared__ float c[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < nvec; i += blockDim.x) c[i] = (float)coef[i];
+    __syncthreads();
+    float acc = 0.f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n4; r += (int64_t)gridDim.x * blockDim.x) {
+        float4 x = w[r];
+        int i = 0;
+        for (; i + 4 <= nvec; i += 4) {  // four vectors' loads in flight, products subtracted in order
+            float4 v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = V[(int64_t)(i + q) * ld4 + r];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float cq = c[i + q];
+                x.x -= v[q].x * cq;
+                x.y -= v[q].y * cq;
+                x.z -= v[q].z * cq;
+                x.w -= v[q].w * cq;
+            }
+        }
+        for (; i < nvec; ++i) {
+            const float4 v = V[(int64_t)i * ld4 + r];
+            const float ci = c[i];
+            x.x -= v.x * ci;
+            x.y -= v.y * ci;
+            x.z -= v.z * ci;
+            x.w -= v.w * ci;
+        }
+        w[r] = x;
+        acc += (x.x * x.x + x.y * x.y) + (x.z * x.z + x.w * x.w);
+    }
+    if (nrm) {
+        __shared__ double sh[kVecThreads / 32];
+        float a = acc;
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)a;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int k = 0; k < kVecThreads / 32; ++k) t += sh[k];
+            nrm[blockIdx.x] = t;
+        }
+        if (reduce_in_last_block(nrm, 1, nrm_out, ticket) && gate_out && threadIdx.x == 0)
+            *gate_out = (*nrm_out >= 0.5 * *gate_ref) ? 1.0 : 0.0;
+    }
+}
+
 // w -= sum_{i<nvec} V_i coef_i (arithmetic in AT); partial ||w||^2 per block when nrm != nullptr.
 template <typename VT, typename WT, typename AT = double>
 __global__ void __launch_bounds__(kVecThreads) k_update(const VT *__restrict__ V, int64_t ld, int nvec,
@@ -284,6 +384,79 @@ __global__ void __launch_bounds__(kVecThreads) k_dav_residual32(const float *__r
         float d = fsig - diag32[r];  // FP32 (no per-element FP64 or conversion work)
         if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
         t[r] = ru / d;
+    }
+    __shared__ double sh[kVecThreads / 32];
+    float a = acc;  // warp tree in FP32, block sum in FP64
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0;
+        for (int q = 0; q < kVecThreads / 32; ++q) sum += sh[q];
+        nrm[blockIdx.x] = sum;
+    }
+    reduce_in_last_block(nrm, 1, nrm_out, ticket);
+}
+
+// k_dav_residual32 with 16-byte loads: every vector as float4 (a length divisible by
+// 4, 16-byte aligned rows); the same per-element order of terms.
+__device__ __forceinline__ float dav_precond(float ru, float fsig, float dg) {
+    float d = fsig - dg;
+    if (fabsf(d) < 1e-2f) d = d < 0 ? -1e-2f : 1e-2f;
+    return ru / d;
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_dav_residual32_f4(const float4 *__restrict__ r32,
+                                                                   const float4 *__restrict__ c32,
+                                                                   const float4 *__restrict__ V,
+                                                                   const float4 *__restrict__ HV, int64_t ld4, int k,
+                                                                   const double *__restrict__ y, double a0,
+                                                                   double a0_de, double theta,
+                                                                   const double *__restrict__ dmin,
+                                                                   const float4 *__restrict__ diag32,
+                                                                   float4 *__restrict__ t, int64_t n4,
+                                                                   double *__restrict__ nrm,
+                                                                   double *__restrict__ nrm_out,
+                                                                   unsigned *__restrict__ ticket) {
+    __shared__ float ys[kMaxBasis + 1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = (float)y[i];
+    __syncthreads();
+    const float fa0 = (float)a0, fa0de = (float)a0_de, fth = (float)theta, fsig = (float)fmin(theta, *dmin);
+    float acc = 0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n4; r += (int64_t)gridDim.x * blockDim.x) {
+        const float4 rr = r32[r], cc = c32[r];
+        float4 ru = make_float4(fa0 * rr.x + fa0de * cc.x, fa0 * rr.y + fa0de * cc.y, fa0 * rr.z + fa0de * cc.z,
+                                fa0 * rr.w + fa0de * cc.w);
+        int i = 0;
+        for (; i + 2 <= k; i += 2) {  // four 16-byte loads in flight, terms added in order
+            float4 hv[2], vv[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int64_t o = (int64_t)(i + q + 1) * ld4 + r;  // corrections live in slots 1..k
+                hv[q] = HV[o];
+                vv[q] = V[o];
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float yq = ys[i + q];
+                ru.x += yq * (hv[q].x - fth * vv[q].x);
+                ru.y += yq * (hv[q].y - fth * vv[q].y);
+                ru.z += yq * (hv[q].z - fth * vv[q].z);
+                ru.w += yq * (hv[q].w - fth * vv[q].w);
+            }
+        }
+        for (; i < k; ++i) {
+            const int64_t o = (int64_t)(i + 1) * ld4 + r;
+            const float4 hv = HV[o], vv = V[o];
+            ru.x += ys[i] * (hv.x - fth * vv.x);
+            ru.y += ys[i] * (hv.y - fth * vv.y);
+            ru.z += ys[i] * (hv.z - fth * vv.z);
+            ru.w += ys[i] * (hv.w - fth * vv.w);
+        }
+        acc += (ru.x * ru.x + ru.y * ru.y) + (ru.z * ru.z + ru.w * ru.w);
+        const float4 dg = diag32[r];
+        t[r] = make_float4(dav_precond(ru.x, fsig, dg.x), dav_precond(ru.y, fsig, dg.y),
+                           dav_precond(ru.z, fsig, dg.z), dav_precond(ru.w, fsig, dg.w));
     }
     __shared__ double sh[kVecThreads / 32];
     float a = acc;  // warp tree in FP32, block sum in FP64
@@ -501,6 +674,12 @@ void pinned_put(double *p) {
     g_pinned_pool.push_back(p);
 }
 
+// FP32 vectors the 16-byte-load kernels take: length and row stride divisible by 4,
+// 16-byte aligned start.
+inline bool vec4_ok(const float *p, int64_t ld, int64_t n) {
+    return n % 4 == 0 && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(p) & 15) == 0;
+}
+
 struct VecOps {
     static constexpr int kTickets = (kMaxBasis + 2 + kDotChunk - 1) / kDotChunk;
     cudaStream_t s;
@@ -527,6 +706,18 @@ struct VecOps {
     template <typename VT, typename WT, typename AT = double>
     void dots(const VT *V, int64_t ld, int nvec, const WT *w, int64_t n, int dst, int skip_at = -1) {
         dim3 grid(Gd, (nvec + kDotChunk - 1) / kDotChunk);
+        if constexpr (std::is_same<VT, float>::value && std::is_same<WT, float>::value &&
+                      std::is_same<AT, float>::value) {
+            if (vec4_ok(V, ld, n) && vec4_ok(w, 0, n)) {
+                k_multidot_f4<<<grid, kVecThreads, 0, s>>>(reinterpret_cast<const float4 *>(V), ld / 4, nvec,
+                                                           reinterpret_cast<const float4 *>(w), n / 4, partial.p,
+                                                           out.p + dst, ticket.p,
+                                                           skip_at >= 0 ? out.p + skip_at : nullptr);
+                CIGPU_CUDA(cudaGetLastError());
+                count_launch();
+                return;
+            }
+        }
         k_multidot<VT, WT, AT><<<grid, kVecThreads, 0, s>>>(V, ld, nvec, w, n, partial.p, out.p + dst, ticket.p,
                                                             skip_at >= 0 ? out.p + skip_at : nullptr);
         CIGPU_CUDA(cudaGetLastError());
@@ -537,6 +728,19 @@ struct VecOps {
     template <typename VT, typename WT, typename AT = double>
     void update(const VT *V, int64_t ld, int nvec, int coef_at, WT *w, int64_t n, int nrm_at, int skip_at = -1,
                 int ref_at = -1, int gate_at = -1) {
+        if constexpr (std::is_same<VT, float>::value && std::is_same<WT, float>::value &&
+                      std::is_same<AT, float>::value) {
+            if (vec4_ok(V, ld, n) && vec4_ok(w, 0, n)) {
+                k_update_f4<<<vec_grid_for(n / 4), kVecThreads, 0, s>>>(
+                    reinterpret_cast<const float4 *>(V), ld / 4, nvec, out.p + coef_at, reinterpret_cast<float4 *>(w),
+                    n / 4, nrm_at >= 0 ? partial.p : nullptr, nrm_at >= 0 ? out.p + nrm_at : nullptr, ticket.p,
+                    skip_at >= 0 ? out.p + skip_at : nullptr, ref_at >= 0 ? out.p + ref_at : nullptr,
+                    gate_at >= 0 ? out.p + gate_at : nullptr);
+                CIGPU_CUDA(cudaGetLastError());
+                count_launch();
+                return;
+            }
+        }
         k_update<VT, WT, AT><<<G, kVecThreads, 0, s>>>(V, ld, nvec, out.p + coef_at, w, n,
                                                        nrm_at >= 0 ? partial.p : nullptr,
                                                        nrm_at >= 0 ? out.p + nrm_at : nullptr, ticket.p,
@@ -986,9 +1190,19 @@ int solve_mixed(const SolveProblem &P, const SolveOptions &o, double *c_dev, boo
             count_launch();
         } else {
             CIGPU_CUDA(cudaMemcpyAsync(yd.p, y.data() + 1, sizeof(double) * k, cudaMemcpyHostToDevice, s));
-            k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(cr32.p + n, cr32.p, V.p, HV.p, n, k, yd.p, a0,
-                                                            a0 * (E - theta), theta, dmin, diag32.p, vnew, n, ops.partial.p,
-                                                            ops.out.p + SLOT_R, ops.ticket.p);
+            if (vec4_ok(cr32.p + n, n, n) && vec4_ok(V.p, n, n) && vec4_ok(HV.p, n, n) && vec4_ok(diag32.p, 0, n) &&
+                vec4_ok(vnew, 0, n)) {
+                using F4 = const float4 *;
+                k_dav_residual32_f4<<<vec_grid_for(n / 4), kVecThreads, 0, s>>>(
+                    F4(cr32.p + n), F4(cr32.p), F4(V.p), F4(HV.p), n / 4, k, yd.p, a0, a0 * (E - theta), theta, dmin,
+                    F4(diag32.p), reinterpret_cast<float4 *>(vnew), n / 4, ops.partial.p, ops.out.p + SLOT_R,
+                    ops.ticket.p);
+            } else {
+                k_dav_residual32<<<ops.G, kVecThreads, 0, s>>>(cr32.p + n, cr32.p, V.p, HV.p, n, k, yd.p, a0,
+                                                                a0 * (E - theta), theta, dmin, diag32.p, vnew, n,
+                                                                ops.partial.p, ops.out.p + SLOT_R, ops.ticket.p);
+            }
+            CIGPU_CUDA(cudaGetLastError());
             count_launch();
         }
         // orthonormalise against slots 0..k (FP32 arithmetic, FP64 reductions): one
