@@ -251,6 +251,20 @@ int sigma_mode() {
     return kSigmaAuto;
 }
 
+// FP64 slot tiles, read at every build from CIGPU_SLOTS64: "compact" leaves out the
+// alpha-single x beta-single block (the matvec forms it from the integrals) wherever
+// its tables fit, anything else stores every slot. The products are the same bit
+// for bit. Compact tiles hold 3.4x fewer values at L=12 6a6b (3.8 against 13.0 GB)
+// and fill faster (whole build 5.5 against 8.3 ms), but their product takes 3.8
+// against 2.7 ms: forming the block is bound by the shared-memory and L1 gathers
+// (its integrals and x), not by the FP64 pipe. A mixed solve's three FP64 anchors
+// then cost more than the smaller fill saves (55.1 against 54.1 ms per build +
+// solve), so the full tiles are the default and the compact ones a memory saver.
+bool slots64_compact() {
+    const char *e = std::getenv("CIGPU_SLOTS64");
+    return e && std::strcmp(e, "compact") == 0;
+}
+
 size_t estimate_bytes(int L, int nup, int ndown, int method, int precision) {
     int64_t dim, W;
     dim = std::max<int64_t>(space_dim(method, L, nup, ndown), 0);
@@ -454,7 +468,8 @@ void build_crs(cigpu_crs &c, cudaStream_t s) {
                 c.val32lo.alloc(slots_count(p));
                 fill_slots_launch(p, c.val32.p, c.val32lo.p, count.p, c.upper_off.p, fs);
             } else {
-                c.val64.alloc(slots_count(p));
+                p.fly = slots64_compact() && slots64_fly_fits(p) ? 1 : 0;
+                c.val64.alloc(std::max<int64_t>(slots_stored(p), 4));
                 fill_slots64_launch(p, c.val64.p, count.p, c.upper_off.p, fs);
             }
             c.slot_desc.alloc(std::max<int64_t>(slot_desc_count(p), 1));
@@ -905,7 +920,7 @@ int cigpu_crs_layout(const cigpu_crs *crs, int *layout, int64_t *stored) {
     if (stored)
         *stored = crs->pairs                           ? 0
                   : crs->onthefly                      ? (crs->det_block > 0 ? crs->nnz_full : 0)
-                  : crs->slots                         ? slots_count(crs->fp)
+                  : crs->slots                         ? slots_stored(crs->fp)
                                                        : crs->nnz_full;
     return CIGPU_OK;
 }

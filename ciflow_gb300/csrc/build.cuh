@@ -19,6 +19,7 @@ struct FciParams {
     const double *eri;  // chemist (pq|rs), L^4
     const float *eri_hi, *eri_lo;  // FP32 split of eri, zero where |v| <= 1e-14
     int staged;         // alpha-single integral slices fit in shared memory
+    int fly = 0;        // FP64 slot tiles without the alpha-single x beta-single block (formed in the matvec)
     const double *diag; // [dim] row diagonals
     const float *diag_hi, *diag_lo;  // FP32 split of diag (MIXED)
     // single-excitation elements per row: [dim][ns_a + ns_b], alpha singles first

@@ -31,6 +31,7 @@
 // the CRS generator (build.cu), in slot order, and counts each row's stored
 // nonzeros and lower-triangle nonzeros on the way (the CRS row pointers of export).
 #include <algorithm>
+#include <stdexcept>
 #include "slots.cuh"
 #include "spmv_formats.cuh"
 
@@ -44,6 +45,9 @@ constexpr int kRowWarps = kTileRows / 32;                // warps covering the t
 constexpr int kSplits = kSlotThreads / 32 / kRowWarps;  // quad ranges per row
 
 __host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
+
+// |v| > 1e-14 (the reference's drop threshold) on the bit pattern of v (integer pipe)
+__device__ __forceinline__ bool above_drop(uint64_t u) { return (u & 0x7FFFFFFFFFFFFFFFull) > 0x3D06849B86A12B9Bull; }
 
 // Segment starts S1..S4 and the padded width Wp.
 struct SlotMap {
@@ -262,6 +266,158 @@ __global__ void __launch_bounds__(kSlotThreads, SlotOccupancy<F>::kMinBlocks) k_
 }
 
 // ---------------------------------------------------------------------------
+// FP64 matvec of compact tiles (p.fly): the quads of S0..S3 are stored
+// (val[((tile * Qs + c) * kTileRows + row) * 4 + j], Qs = S4 / 4), and the alpha-single
+// x beta-single block S4 -- 71% of the slots at L=12 6a6b -- is formed here from the
+// staged integral slices: element (xa, xb) of row (Ia, Ib) is (ar ac|br bc) with the
+// sign of both phases, zero where |v| <= 1e-14, the value the fill would store. The
+// quad ranges, the order of the terms and the sums of the ranges are those of
+// k_spmv_slots<Plain<double>>, so the product equals the full tiles' bit for bit.
+// The values read from HBM drop from 8 Wp to 8 S4 bytes per row, but an S4 element
+// costs a random 8-byte shared-memory gather of its integral and three more
+// shared-memory reads besides the x gather both forms make, and the L1 / shared-
+// memory data path, not the FP64 pipe, bounds the product: 3.81 against 2.71 ms at
+// L=12 6a6b (0.65 of the FP64-pipe floor against 0.95). A memory saver, not a
+// faster product.
+// Shared memory: descriptors [Wp], beta single targets [nsb][kTileRows], beta pairs
+// and parities [nsb][kTileRows], alpha parities [pad4(nsa)], alpha integral row
+// offsets [pad4(nsa)], integral slices [nsa][L^2] (FP64).
+__global__ void __launch_bounds__(kSlotThreads, 3) k_spmv_slots_fly(const FciParams p, const Plain<double> f,
+                                                                    double *__restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double part[kSplits][kTileRows];
+    const SlotMap m = slot_map(p);
+    const int Q = m.wp >> 2, Qs = m.s4 >> 2;
+    const int L2 = p.L * p.L, nsa = p.a.ns, nsb = p.b.ns;
+    uint64_t *desc = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *st = reinterpret_cast<uint32_t *>(desc + m.wp);
+    uint32_t *sbi = st + nsb * kTileRows;
+    uint32_t *sai = sbi + nsb * kTileRows;
+    uint32_t *roff = sai + pad4(nsa);
+    double *sl64 = reinterpret_cast<double *>(roff + pad4(nsa));  // 16-byte aligned: every region is a multiple of 16 bytes
+    const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
+    const int64_t tile = blockIdx.x;
+    const int64_t ia = tile / T, t = tile - ia * T;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rr = (warp % kRowWarps) * 32 + lane, ks = warp / kRowWarps;
+    const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
+    const int cs = min(c1, Qs);  // stored quads of this range end here
+    const int64_t qbase = tile * (int64_t)Qs;
+    if (lane == 0 && warp % kRowWarps == 0 && cs > c0)
+        f.prefetch((qbase + c0) * kTileRows * 4, (int64_t)min(cs - c0, kPrefetchQuads) * kTileRows * 4);
+    stage_tile_tab(p, m, ia, t, desc, st);
+    // beta singles of the tile's rows: orbital pair br * L + bc | parity << 31 (read
+    // in the table's order, row-major, and stored single-major)
+    for (int i = threadIdx.x; i < nsb * kTileRows; i += blockDim.x) {
+        const int r = i / nsb, xb = i - r * nsb;
+        const int64_t ibr = t * kTileRows + r;
+        uint32_t w = 0;
+        if (ibr < p.Db) {
+            const uint32_t info = __ldg(p.b.s_info + ibr * nsb + xb);
+            w = (((info >> 12) & 63) * p.L + ((info >> 18) & 63)) | (((info >> 24) & 1u) << 31);
+        }
+        sbi[xb * kTileRows + r] = w;
+    }
+    for (int xa = threadIdx.x; xa < nsa; xa += blockDim.x) {
+        const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
+        sai[xa] = ((info >> 24) & 1u) << 31;
+        roff[xa] = (((info >> 12) & 63) * p.L + ((info >> 18) & 63)) * L2;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsa * L2; i += blockDim.x) {
+        const int xa = i / L2;
+        sl64[i] = __ldg(p.eri + roff[xa] + (i - xa * L2));
+    }
+    __syncthreads();
+    const int64_t ib_raw = t * kTileRows + rr;
+    const bool active = ib_raw < p.Db;
+    const int64_t ib = active ? ib_raw : p.Db - 1;
+    const uint32_t ib32 = (uint32_t)ib;
+    const uint32_t *dt = p.b.d_target + ib * p.b.nd;
+    const uint32_t *stl = st + rr;  // this row's beta single targets, kTileRows apart
+    constexpr int kQuadsInFlight = SlotInFlight<Plain<double>>::kQuads;
+    Plain<double>::Acc acc{};
+    Plain<double>::Chunk v[kQuadsInFlight];
+    // stored quads: the loop of k_spmv_slots
+    for (int c = c0; c < cs; c += kQuadsInFlight) {
+#pragma unroll
+        for (int u = 0; u < kQuadsInFlight; ++u) {
+            if (c + u < cs)
+                f.load4(((qbase + c + u) * kTileRows + rr) * 4, v[u]);
+            else
+                f.zero(v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kQuadsInFlight; ++u) {
+            if (c + u < cs) {
+                const uint4 *dq = reinterpret_cast<const uint4 *>(desc + 4 * (c + u));
+                const uint32_t kind = reinterpret_cast<const uint32_t *>(dq)[1] & 3u;  // one kind per quad
+                uint32_t col[4];
+                const uint4 q0 = dq[0], q1 = dq[1];
+                if (kind == kSelf) {
+                    col[0] = q0.x + ib32;
+                    col[1] = q0.z + ib32;
+                    col[2] = q1.x + ib32;
+                    col[3] = q1.z + ib32;
+                } else if (kind == kSingle) {
+                    col[0] = q0.x + stl[q0.y >> 2];
+                    col[1] = q0.z + stl[q0.w >> 2];
+                    col[2] = q1.x + stl[q1.y >> 2];
+                    col[3] = q1.z + stl[q1.w >> 2];
+                } else {
+                    col[0] = q0.x + __ldg(dt + (q0.y >> 2));
+                    col[1] = q0.z + __ldg(dt + (q0.w >> 2));
+                    col[2] = q1.x + __ldg(dt + (q1.y >> 2));
+                    col[3] = q1.z + __ldg(dt + (q1.w >> 2));
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) f.term(v[u], j, (int64_t)col[j], acc);
+            }
+        }
+    }
+    // S4 quads, formed: slot k = 4c + j is element i = k - S4 = xa * nsb + xb
+    const int c4 = max(c0, Qs);
+    if (c4 < c1) {
+        const int npair = nsa * nsb;
+        int i = 4 * c4 - m.s4;
+        int xa = i / nsb, xb = i - xa * nsb;
+        for (int c = c4; c < c1; ++c) {
+            const uint4 *dq = reinterpret_cast<const uint4 *>(desc + 4 * c);  // kind single: Ja * Db, xb * kTileRows
+            const uint4 q0 = dq[0], q1 = dq[1];
+            const uint32_t col[4] = {q0.x + stl[q0.y >> 2], q0.z + stl[q0.w >> 2], q1.x + stl[q1.y >> 2],
+                                     q1.z + stl[q1.w >> 2]};
+            Plain<double>::Chunk e;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                uint64_t u = 0;  // padding slots hold zero
+                if (i < npair) {
+                    const uint32_t w = sbi[xb * kTileRows + rr];
+                    const uint64_t odd = (uint64_t)((sai[xa] ^ w) >> 31);
+                    u = (uint64_t)__double_as_longlong(sl64[xa * L2 + (int)(w & 0xFFFu)]) ^ (odd << 63);
+                    if (!above_drop(u)) u = 0;
+                    if (++xb == nsb) {
+                        xb = 0;
+                        ++xa;
+                    }
+                }
+                ++i;
+                e.v[j] = __longlong_as_double((long long)u);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) f.term(e, j, (int64_t)col[j], acc);
+        }
+    }
+    part[ks][rr] = acc.s;
+    __syncthreads();
+    if (ks == 0 && active) {
+        double sum = part[0][rr];
+#pragma unroll
+        for (int q = 1; q < kSplits; ++q) sum += part[q][rr];
+        y[ia * p.Db + ib_raw] = sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Fill: the same element values as the CRS generator, as FP32 hi + lo splits (zero
 // where |v| <= 1e-14; F64 = false) or as FP64 values (zero where |v| <= 1e-14;
 // F64 = true, the plain method's tiles), with each row's nonzero count and
@@ -285,7 +441,7 @@ struct FillVals<true> {  // FP64, |v| <= 1e-14 stored as zero
     uint64_t b[4] = {0, 0, 0, 0};
     __device__ __forceinline__ void set(int j, double x) {
         const uint64_t u = (uint64_t)__double_as_longlong(x);
-        b[j] = (u & 0x7FFFFFFFFFFFFFFFull) > 0x3D06849B86A12B9Bull ? u : 0ull;  // bits of 1e-14
+        b[j] = above_drop(u) ? u : 0ull;
     }
     __device__ __forceinline__ bool nonzero(int j) const { return b[j] != 0ull; }
     __device__ __forceinline__ void clear(int j) { b[j] = 0ull; }
@@ -345,6 +501,31 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
         }
     }
     __syncthreads();
+    // Compact FP64 tiles (p.fly; the slices are not staged): the alpha-single x
+    // beta-single block (S4) is not stored. Its element for alpha single xa and beta
+    // pair tt has the magnitude of the integral (ar ac|tt), so a row's S4 nonzeros are
+    // a sum over its beta singles of nz[tt] (alpha singles whose integral with tt
+    // exceeds 1e-14) and its lower-triangle ones of nzl[tt] (those with Ja < Ia).
+    uint32_t *nz = nullptr, *nzl = nullptr;
+    if constexpr (F64) {
+        if (p.fly) {
+            nz = reinterpret_cast<uint32_t *>(sai + pad4(nsa));
+            nzl = nz + L2;
+            for (int tt = threadIdx.x; tt < L2; tt += blockDim.x) {
+                uint32_t na = 0, nl = 0;
+                for (int xa = 0; xa < nsa; ++xa) {
+                    const uint32_t info = __ldg(p.a.s_info + ia * nsa + xa);
+                    const size_t at = (((info >> 12) & 63) * (size_t)p.L + ((info >> 18) & 63)) * L2 + tt;
+                    const bool keep = above_drop((uint64_t)__double_as_longlong(__ldg(p.eri + at)));
+                    na += keep;
+                    nl += keep && ((sai[xa] >> 30) & 1u);
+                }
+                nz[tt] = na;
+                nzl[tt] = nl;
+            }
+            __syncthreads();
+        }
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = (warp % kRowWarps) * 32 + lane, ks = warp / kRowWarps;
     const int64_t ib_raw = t * kTileRows + rr;
@@ -352,11 +533,14 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
     const int64_t ib = active ? ib_raw : p.Db - 1;
     const int64_t r = ia * p.Db + ib;
     const int c0 = (int)((int64_t)Q * ks / kSplits), c1 = (int)((int64_t)Q * (ks + 1) / kSplits);
-    const int64_t qbase = (ia * T + t) * (int64_t)Q;
+    const bool fly = F64 && p.fly;
+    const int Qs = fly ? m.s4 >> 2 : Q;  // stored quads per row
+    const int cs = min(c1, Qs);
+    const int64_t qbase = (ia * T + t) * (int64_t)Qs;
     const int nsb = p.b.ns, ndb = p.b.nd, nda = p.a.nd, nsr = nsa + nsb, L = p.L;
     uint32_t n_keep = 0, n_low = 0;
     // one quad at a time; a quad lies in one segment, so the branch is uniform
-    for (int c = c0; c < c1; ++c) {
+    for (int c = c0; c < cs; ++c) {
         const int k0 = 4 * c;
         FillVals<F64> q;
         bool lw[4] = {false, false, false, false};  // column below the diagonal
@@ -466,6 +650,12 @@ __global__ void __launch_bounds__(kSlotThreads) k_fill_slots(const FciParams p, 
             *reinterpret_cast<float4 *>(lo + at) = make_float4(q.l[0], q.l[1], q.l[2], q.l[3]);
         }
     }
+    if (fly && ks == kSplits - 1)
+        for (int xb = 0; xb < nsb; ++xb) {
+            const uint32_t tt = sbi[xb * kTileRows + rr] & 0xFFFu;
+            n_keep += nz[tt];
+            n_low += nzl[tt];
+        }
     cnt[ks][rr] = n_keep;
     low[ks][rr] = n_low;
     __syncthreads();
@@ -487,6 +677,10 @@ size_t fill_smem(const FciParams &p) {
     return tile_smem(p) + (size_t)p.b.ns * kTileRows * 4 + (size_t)pad4(p.a.ns) * 4;
 }
 size_t slice_smem(const FciParams &p) { return (size_t)p.a.ns * p.L * p.L * 8; }  // hi + lo slices
+// compact FP64 tiles: the fill stages no slices but two histograms over the beta
+// pairs; the matvec stages the slices and the alpha integral row offsets
+size_t fly_smem(const FciParams &p) { return fill_smem(p) + (size_t)8 * p.L * p.L; }
+size_t fly_mv_smem(const FciParams &p) { return fill_smem(p) + slice_smem(p) + (size_t)pad4(p.a.ns) * 4; }
 
 template <typename F>
 void launch_slots(const FciParams &p, const F &f0, typename F::X *y, cudaStream_t s) {
@@ -515,6 +709,15 @@ int64_t slots_count(const FciParams &p) {
     return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * (int64_t)slot_map(p).wp;
 }
 
+bool slots64_fly_fits(const FciParams &p) {
+    return p.a.ns > 0 && p.b.ns > 0 && fly_smem(p) <= kSlotsMaxSmem && fly_mv_smem(p) <= kSlotsMaxSmem;
+}
+
+int64_t slots_stored(const FciParams &p) {
+    if (!p.fly) return slots_count(p);
+    return p.a.D * ((p.Db + kTileRows - 1) / kTileRows) * kTileRows * (int64_t)slot_map(p).s4;
+}
+
 void fill_slots_launch(const FciParams &p0, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s) {
     FciParams p = p0;
     const size_t base = fill_smem(p), sl = slice_smem(p);
@@ -535,14 +738,19 @@ void fill_slots64_launch(const FciParams &p0, double *v64, uint32_t *count, uint
     FciParams p = p0;
     const size_t base = fill_smem(p), sl = slice_smem(p);  // an FP64 slice takes the bytes of hi + lo
     p.staged = base + sl <= kSlotsMaxSmem ? 1 : 0;
+    size_t smem = p.staged ? base + sl : base;
+    if (p.fly) {  // no S4 elements to form: no slices, the two histograms in their place
+        if (!slots64_fly_fits(p)) throw std::logic_error("compact FP64 slot tiles do not fit this space");
+        p.staged = 0;
+        smem = fly_smem(p);
+    }
     static const bool attr_set = [] {  // thread-safe one-time init
         cudaFuncSetAttribute(k_fill_slots<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
         return true;
     }();
     (void)attr_set;
     const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
-    k_fill_slots<true><<<(unsigned)(p.a.D * T), kSlotThreads, p.staged ? base + sl : base, s>>>(p, nullptr, nullptr,
-                                                                                               v64, count, lower);
+    k_fill_slots<true><<<(unsigned)(p.a.D * T), kSlotThreads, smem, s>>>(p, nullptr, nullptr, v64, count, lower);
     CIGPU_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -568,7 +776,24 @@ void spmv_slots_hilo(const FciParams &p, const float *hi, const float *lo, const
 }
 
 void spmv_slots_f64(const FciParams &p, const double *val, const double *x, double *y, cudaStream_t s) {
-    launch_slots(p, Plain<double>{val, x}, y, s);
+    if (!p.fly) {
+        launch_slots(p, Plain<double>{val, x}, y, s);
+        return;
+    }
+    Plain<double> f{val, x};
+    f.nx = (uint64_t)(p.a.D * p.Db);
+    f.err = check_word_device();
+    static const bool attr_set = [] {  // thread-safe one-time init; three blocks of ~76 KB per SM at L=12 6a6b
+        cudaFuncSetAttribute(k_spmv_slots_fly, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotsMaxSmem);
+        cudaFuncSetAttribute(k_spmv_slots_fly, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        return true;
+    }();
+    (void)attr_set;
+    const int64_t T = (p.Db + kTileRows - 1) / kTileRows;
+    k_spmv_slots_fly<<<(unsigned)(p.a.D * T), kSlotThreads, fly_mv_smem(p), s>>>(p, f, y);
+    CIGPU_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace cigpu

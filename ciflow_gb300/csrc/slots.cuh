@@ -16,8 +16,15 @@ int64_t slots_count(const FciParams &p);
 // Fills the FP32 hi/lo slot values (needs the row singles and FP32 tables in p) and
 // each row's stored-nonzero count and lower-triangle count (count, lower: [dim]).
 void fill_slots_launch(const FciParams &p, float *hi, float *lo, uint32_t *count, uint32_t *lower, cudaStream_t s);
+// Compact FP64 tiles (p.fly = 1): the alpha-single x beta-single block of every row
+// (71% of the slots at L=12 6a6b) is not stored but formed by the FP64 matvec from
+// the integrals; the product equals the full tiles' bit for bit (and takes ~40%
+// longer). Whether the kernels' shared-memory tables fit for this space:
+bool slots64_fly_fits(const FciParams &p);
+// Values the FP64 tiles store: slots_count(p), or fewer with p.fly.
+int64_t slots_stored(const FciParams &p);
 // Fills FP64 slot values (|v| <= 1e-14 stored as zero; needs the FP64 row singles
-// in p) and the same row counts: the plain method's tiles.
+// in p) and the same row counts: the plain method's tiles (compact with p.fly).
 void fill_slots64_launch(const FciParams &p, double *v64, uint32_t *count, uint32_t *lower, cudaStream_t s);
 // Whether FP64 tiles pay off: the tiles' padding rows add at most a quarter.
 inline bool slots64_pay(const FciParams &p) {

@@ -116,9 +116,72 @@ def test_sigma_backed_mixed_build_defers_and_exports_the_same(case, monkeypatch)
     y = m.mvprod(x)  # FP64 product right after the build: waits for the deferred fill on the device
     y_ref = build(FCI, ints).get_mat().mvprod(x)
     assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+    # the same build on compact FP64 tiles (the alpha-single x beta-single block left
+    # out, its deferred fill counting it from histograms): the same counts, exports
+    # and FP64 product, bit for bit
+    monkeypatch.setenv("CIGPU_SLOTS64", "compact")
+    comp = build(FCI, ints, precision=A.MIXED).get_mat()
+    np.testing.assert_array_equal(comp.mvprod(x), y)
+    s4, wp = _slot_widths(ints.L, ints.nup, ints.ndown)
+    lay, stored = _layout(comp)
+    assert lay == A.LAYOUT_SLOTS and stored % s4 == 0 and stored // s4 * wp == _layout(m)[1]
+    assert (comp.nnz_upper, comp.nnz_full) == (ref.nnz_upper, ref.nnz_full)
+    for a, b in zip(comp.full(), ref.full()):
+        np.testing.assert_array_equal(a, b)
     assert (m.nnz_upper, m.nnz_full) == (ref.nnz_upper, ref.nnz_full)
     for a, b in zip(m.full(), ref.full()):
         np.testing.assert_array_equal(a, b)
+
+
+def _slot_widths(L, nup, ndown):
+    """(S4, Wp) of the FCI slot tiles: the start of the alpha-single x beta-single
+    block and the padded row width (segments padded to multiples of 4)."""
+    from math import comb
+
+    def pad4(n):
+        return (n + 3) & ~3
+
+    nsa, nsb = nup * (L - nup), ndown * (L - ndown)
+    nda, ndb = comb(nup, 2) * comb(L - nup, 2), comb(ndown, 2) * comb(L - ndown, 2)
+    s4 = 4 + pad4(nsb) + pad4(ndb) + pad4(nsa + nda)
+    return s4, s4 + pad4(nsa * nsb)
+
+
+def _layout(m):
+    import ctypes
+
+    lay, stored = ctypes.c_int(), ctypes.c_int64()
+    A.check(A.lib().cigpu_crs_layout(m.handle, ctypes.byref(lay), ctypes.byref(stored)))
+    return lay.value, stored.value
+
+
+@pytest.mark.parametrize("L,nup,ndown", [(10, 5, 5), (11, 5, 4), (10, 4, 5)])
+def test_compact_fp64_tiles_equal_full_tiles(L, nup, ndown, monkeypatch):
+    """FP64 slot tiles that leave out the alpha-single x beta-single block (the
+    matvec forms it from the integrals) store S4 of the Wp values per row and give
+    the full tiles' product bit for bit, the same row counts (the fill counts the
+    block from per-pair histograms) and the same exported matrix. With 25 beta
+    singles (10 orbitals, 5 beta electrons) quads of the block span two alpha
+    singles."""
+    ints = make_integrals(L, nup, ndown, nchol=8, seed=3 * L + 5 * nup + ndown)
+    monkeypatch.setenv("CIGPU_SLOTS64", "full")
+    full = build(FCI, ints).get_mat()
+    monkeypatch.setenv("CIGPU_SLOTS64", "compact")
+    comp = build(FCI, ints).get_mat()
+    (lf, sf), (lc, sc) = _layout(full), _layout(comp)
+    assert lf == lc == A.LAYOUT_SLOTS
+    s4, wp = _slot_widths(L, nup, ndown)
+    assert sf % wp == 0 and sc == sf // wp * s4
+    x = np.random.default_rng(L + nup).standard_normal(full.n)
+    np.testing.assert_array_equal(comp.mvprod(x), full.mvprod(x))
+    assert (comp.nnz_upper, comp.nnz_full) == (full.nnz_upper, full.nnz_full)
+    for a, b in zip(comp.full(), full.full()):
+        np.testing.assert_array_equal(a, b)
+    if full.n <= 70000:  # and the oracle's CRS (the larger case takes the oracle long)
+        ref = O.build_upper(O.FCI, ints)
+        row, col, val = comp.upper()
+        np.testing.assert_array_equal(val, ref.val)
+        np.testing.assert_array_equal(col, ref.col)
 
 
 def test_symmetry_zeros_dropped_like_reference():
